@@ -1,0 +1,137 @@
+"""Generate tests/golden/*.npz from the reference's own CPU code.
+
+Runs fastEmbedR's src/tsne_neighbors.cpp and src/fast_knn_umap.cpp, compiled where
+they lie against the test-only Rcpp shim (``make -C oracle ref``), on small seeded
+inputs and stores inputs + outputs. The fixtures travel with the repository; the
+reference sources do not. Re-run with:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+import oracle as O  # noqa: E402
+from fastembedr_gb300 import synthetic as S  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def cm(a, t):
+    return np.ascontiguousarray(np.asarray(a, t).T).ravel()
+
+
+def force_case(name, x_seed, n, dim, k, perp, grid, layout_sd, layout=None, x=None):
+    R = O.ref()
+    rng = np.random.default_rng(x_seed)
+    if x is None:
+        x = rng.standard_normal((n, dim)).astype(np.float32)
+    idx, dist = S.exact_knn_numpy(x, k)
+    n = idx.shape[0]
+    if layout is None:
+        layout = (rng.standard_normal((n, 2)) * layout_sd).astype(np.float32)
+    cap = 2 * n * k
+    att, rex, rff = np.zeros(2 * n), np.zeros(2 * n), np.zeros(2 * n)
+    rp = np.zeros(n + 1, np.int32)
+    col = np.zeros(cap, np.int32)
+    w = np.zeros(cap)
+    nnz, sq, kl = C.c_longlong(), C.c_double(), C.c_double()
+    st = R.ref_force_diagnostic(cm(idx, np.int32), cm(dist, np.float64), cm(layout, np.float64), n, k,
+                                float(perp), 1.0, int(grid), 1, att, rex, rff, rp, col, w, cap, C.byref(nnz),
+                                C.byref(sq), C.byref(kl))
+    assert st == 0, R.ref_last_error()
+    m = nnz.value
+    np.savez_compressed(
+        os.path.join(OUT, f"force_{name}.npz"), idx=idx, dist=dist, layout=layout, perplexity=perp, grid=grid,
+        row_ptr=rp, col=col[:m], weight=w[:m], attractive=att.reshape(2, n).T, rep_exact=rex.reshape(2, n).T,
+        rep_fft=rff.reshape(2, n).T, sum_q=sq.value, kl=kl.value)
+
+
+def tsne_run_case():
+    R = O.ref()
+    x, _ = S.mixture(2000, 20, 5, 11, centre_sd=4.0, within_sd=1.0)
+    idx, dist = S.exact_knn_numpy(x, 30)
+    n, k = idx.shape
+    init = S.tsne_init(n, 5)
+    y = np.zeros(2 * n)
+    costs = np.zeros(64)
+    nc, g = C.c_int(), C.c_int()
+    st = R.ref_tsne_run(cm(idx, np.int32), cm(dist, np.float64), cm(init, np.float64), n, k, 10.0, 250, 750, 12.0,
+                        1.0, -1.0, 1, 0.8, 0.8, 0.01, 5.0, b"fft", 1, 4, 1, y, costs, C.byref(nc), C.byref(g))
+    assert st == 0, R.ref_last_error()
+    np.savez_compressed(os.path.join(OUT, "tsne_run_2k.npz"), idx=idx, dist=dist, init=init, perplexity=10.0,
+                        early_iter=250, n_iter=750, y=y.reshape(2, n).T, itercosts=costs[: nc.value],
+                        grid=g.value)
+
+
+def umap_case():
+    R = O.ref()
+    x, _ = S.mixture(3000, 20, 6, 12, centre_sd=3.0, lognormal_sizes=True, anisotropic=True)
+    idx, dist = S.exact_knn_numpy(x, 15)
+    n, k = idx.shape
+    cap = 2 * n * k
+    off = np.zeros(n + 1, np.int32)
+    nb = np.zeros(cap, np.int32)
+    w, e = np.zeros(cap), np.zeros(cap)
+    nnz, mw = C.c_longlong(), C.c_double()
+    st = R.ref_umap_graph(cm(idx, np.int32), cm(dist, np.float64), n, k, 1, off, nb, w, e, cap, C.byref(nnz),
+                          C.byref(mw))
+    assert st == 0, R.ref_last_error()
+    m = nnz.value
+    init = np.random.default_rng(3).uniform(-10, 10, (n, 2))
+    out = np.zeros(2 * n)
+    st = R.ref_umap_sgd(off, nb[:m].copy(), w[:m].copy(), cm(init, np.float64), n, m, 200, 0.01, 5, 1.0, 1.0, 1,
+                        42, out)
+    assert st == 0, R.ref_last_error()
+    np.savez_compressed(os.path.join(OUT, "umap_3k.npz"), idx=idx, dist=dist, offsets=off, neighbors=nb[:m],
+                        weights=w[:m], epochs_per_sample=e[:m], max_weight=mw.value, init=init,
+                        y=out.reshape(2, n).T, n_epochs=200, seed=42)
+
+
+def transform_case():
+    R = O.ref()
+    xr, _ = S.mixture(2500, 20, 5, 13, centre_sd=4.0, within_sd=1.0)
+    xq = xr[:300] + np.random.default_rng(1).normal(0, 0.3, (300, 20)).astype(np.float32)
+    ref = xr[300:]
+    refy = np.random.default_rng(2).normal(0, 10, (ref.shape[0], 2))
+    d2 = ((xq[:, None, :].astype(np.float64) - ref[None, :, :]) ** 2).sum(-1)
+    qi = np.argsort(d2, 1)[:, :30].astype(np.int32)
+    qd = np.sqrt(np.take_along_axis(d2, qi, 1))
+    outs = {}
+    for tag, nneg, thr in (("exact", 256, 4096), ("sampled", 64, 10)):
+        y = np.zeros(600)
+        st = R.ref_transform(cm(refy, np.float64), refy.shape[0], cm(qi, np.int32), cm(qd, np.float64), 300, 30,
+                             None, 0, b"median", 5.0, 250, 0, 0.1, 4.0, 1.5, 0.8, 0.8, 0.25, np.inf, nneg, thr, 1, 4,
+                             y)
+        assert st == 0, R.ref_last_error()
+        outs[tag] = y.reshape(2, 300).T
+    np.savez_compressed(os.path.join(OUT, "transform_2k.npz"), ref_y=refy, idx=qi, dist=qd,
+                        y_exact=outs["exact"], y_sampled=outs["sampled"])
+
+
+def main():
+    O.build(ref=True)
+    force_case("n48", 701, 48, 6, 15, 5.0, 64, 0.3)
+    force_case("n300", 7011, 300, 6, 15, 5.0, 64, 0.3)
+    # pathological inputs of tests/testthat/test-tsne-numerics.R:120-160
+    rng = np.random.default_rng(705)
+    dup = np.vstack([np.zeros((8, 4)), np.ones((8, 4)), rng.normal(0, 1e-8, (8, 4))]).astype(np.float32)
+    force_case("duplicated", 705, 24, 4, 6, 2.0, 64, 0.1, x=dup)
+    force_case("coincident", 705, 24, 4, 6, 2.0, 64, 0.1, x=dup, layout=np.zeros((24, 2), np.float32))
+    ext = np.tile(np.array([[-1e4, 1e4]], np.float32), (24, 1))
+    force_case("extreme", 705, 24, 4, 6, 2.0, 64, 0.1, x=dup, layout=ext)
+    dis = np.vstack([rng.normal(-20, 0.01, (12, 4)), rng.normal(20, 0.01, (12, 4))]).astype(np.float32)
+    force_case("disconnected", 7051, 24, 4, 6, 2.0, 64, 0.1, x=dis)
+    tsne_run_case()
+    umap_case()
+    transform_case()
+    print("golden fixtures written to", OUT)
+
+
+if __name__ == "__main__":
+    main()

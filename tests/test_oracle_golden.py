@@ -1,0 +1,79 @@
+"""The CPU oracle against golden vectors produced by the reference's own CPU code.
+
+The fixtures in tests/golden were made by tests/golden/make_golden.py from fastEmbedR
+src/tsne_neighbors.cpp and src/fast_knn_umap.cpp (compiled unchanged against the
+test-only Rcpp shim). Matching them pins the plain-C restatement that the GPU parity
+tests then use as their checker.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+
+
+@pytest.mark.parametrize("case", ["n48", "n300", "duplicated", "coincident", "extreme", "disconnected"])
+def test_force_diagnostic_matches_reference(golden, case):
+    g = golden("force_" + case)
+    rp, col, val, _ = O.tsne_csr(g["idx"], g["dist"], float(g["perplexity"]))
+    # (a) symmetrised CSR: integer structure bit-exact, values identical
+    np.testing.assert_array_equal(rp, g["row_ptr"])
+    np.testing.assert_array_equal(col, g["col"])
+    np.testing.assert_array_equal(val.astype(np.float64), g["weight"])
+    y = g["layout"].astype(np.float32)
+    att = O.attractive(rp, col, val, y, 1.0)
+    np.testing.assert_array_equal(att.astype(np.float64), g["attractive"])
+    rex, sq = O.exact_rep_f32(y)
+    np.testing.assert_allclose(rex, g["rep_exact"], rtol=0, atol=1e-6 * max(1e-30, np.abs(g["rep_exact"]).max()))
+    rff, _ = O.fft_grid_rep_f32(y, int(g["grid"]))
+    np.testing.assert_allclose(rff, g["rep_fft"], rtol=0, atol=1e-6 * max(1e-30, np.abs(g["rep_fft"]).max()))
+    assert O.kl(rp, col, val, y) == pytest.approx(float(g["kl"]), rel=1e-12)
+    assert np.all(np.isfinite(rff)) and np.all(np.isfinite(rex))
+
+
+def test_full_tsne_run_matches_reference_bitwise(golden):
+    g = golden("tsne_run_2k")
+    y, trace, its = O.tsne_run(g["idx"], g["dist"], g["init"], perplexity=float(g["perplexity"]),
+                               early_iter=int(g["early_iter"]), n_iter=int(g["n_iter"]), kl_every=True)
+    np.testing.assert_array_equal(y.astype(np.float64), g["y"])
+    np.testing.assert_allclose(trace, g["itercosts"], rtol=1e-12)
+
+
+def test_umap_graph_and_serial_sgd_match_reference(golden):
+    g = golden("umap_3k")
+    off, nb, w, e, mw = O.umap_graph(g["idx"], g["dist"])
+    np.testing.assert_array_equal(off, g["offsets"])
+    np.testing.assert_array_equal(nb, g["neighbors"])
+    np.testing.assert_array_equal(w.astype(np.float64), g["weights"])
+    np.testing.assert_array_equal(e.astype(np.float64), g["epochs_per_sample"])
+    n = off.size - 1
+    emb = np.ascontiguousarray(g["init"].T).ravel().copy()
+    a, b = O.umap_ab(0.01)
+    O.orc().orc_umap_sgd_serial(n, off, nb, w, emb, int(g["n_epochs"]), a, b, 5, 1.0, 1.0, int(g["seed"]))
+    np.testing.assert_array_equal(emb.reshape(2, n).T, g["y"])
+
+
+@pytest.mark.parametrize("tag,nneg,thr", [("exact", 256, 4096), ("sampled", 64, 10)])
+def test_transform_matches_reference(golden, tag, nneg, thr):
+    g = golden("transform_2k")
+    y = O.transform_tsne(g["ref_y"], g["idx"], g["dist"], init_mode=1, n_negatives=nneg, exact_threshold=thr)
+    np.testing.assert_array_equal(y, g["y_" + tag])
+
+
+def test_umap_ab_policies():
+    # CPU policy hard-codes min_dist = 0.01 (src/fast_knn_umap.cpp:437-440); the CUDA host
+    # path grid-fits it (src/embedding_cuda_impl.cpp:491-545)
+    assert O.umap_ab(0.01) == (1.895605865596314, 0.8006377738365004)
+    a, b = O.umap_ab(0.01, cuda_host=True)
+    assert abs(a - 1.8956) < 0.05 and abs(b - 0.8006) < 0.01
+
+
+def test_fp64_probability_oracle_tracks_fp32_reference(golden):
+    """The FP64 bisection (the reference's test helper) and the FP32 CPU path agree on the
+    symmetric P within the reference's own check: testthat all.equal mean relative
+    difference < 2e-6 (tests/testthat/test-tsne-numerics.R:18-22)."""
+    g = golden("force_n300")
+    p32 = O.row_p_f32(g["dist"], 5.0)
+    p64, _ = O.row_p_f64(g["dist"], 5.0)
+    _, _, v32, _ = O.csr_from_p(g["idx"], p32)
+    _, _, v64, _ = O.csr_from_p(g["idx"], p64.astype(np.float32))
+    assert np.abs(v32.astype(np.float64) - v64).sum() / np.abs(v64).sum() < 2e-6
