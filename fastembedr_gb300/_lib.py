@@ -1,0 +1,95 @@
+"""ctypes binding of the native library (C ABI declared in include/fastembedr_cuda.h).
+
+The library is the only compute path: if it is missing or no CUDA device is present, calls
+raise instead of falling back to anything else.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_LIB = None
+
+i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+vp = C.c_void_p
+I, U, F, D, L = C.c_int, C.c_uint, C.c_float, C.c_double, C.c_longlong
+
+# name -> (restype, argtypes); argtypes use void* for arrays so host numpy arrays and raw
+# device pointers (ints) are both accepted.
+SIGNATURES = {
+    "fastembedr_cuda_available": (C.c_bool, []),
+    "fastembedr_cuda_embedding_last_error": (C.c_char_p, []),
+    "fastembedr_cuda_opentsne_fft_grid_size": (I, [I]),
+    "fastembedr_cuda_opentsne_fft_from_knn_float": (I, [vp, vp, vp, I, I, I, I, F, I, I, F, F, F, I, F, F, F, F, U,
+                                                        I, vp]),
+    "fastembedr_cuda_opentsne_fft_from_knn": (I, [vp, vp, vp, I, I, I, I, F, I, I, F, F, F, I, F, F, F, F, U, I, vp]),
+    "fastembedr_cuda_opentsne_fft_from_device_knn_float": (I, [vp, vp, vp, I, I, I, I, F, I, I, F, F, F, I, F, F, F, F,
+                                                               U, I, vp]),
+    "fastembedr_cuda_tsne_affinities": (I, [vp, vp, I, I, F, I, vp, vp, vp, L, C.POINTER(L), vp, vp, C.POINTER(D)]),
+    "fastembedr_cuda_tsne_force_diagnostic": (I, [vp, vp, vp, I, I, F, F, I, I, I, vp, vp, C.POINTER(D), vp,
+                                                  C.POINTER(D), C.POINTER(D)]),
+    "fastembedr_tsne_plan_create": (I, [vp, vp, vp, I, I, F, I, I, I, U, C.POINTER(vp)]),
+    "fastembedr_tsne_plan_run": (I, [vp, I, F, F, F, F, F, I]),
+    "fastembedr_tsne_plan_profile": (I, [vp, I, F, F, F, F, F, C.POINTER(F), C.POINTER(F), C.POINTER(F)]),
+    "fastembedr_tsne_plan_synchronize": (I, [vp]),
+    "fastembedr_tsne_plan_stream": (vp, [vp]),
+    "fastembedr_tsne_plan_layout": (I, [vp, vp]),
+    "fastembedr_tsne_plan_info": (I, [vp, C.POINTER(L), C.POINTER(I), C.POINTER(I), C.POINTER(I)]),
+    "fastembedr_tsne_plan_kl": (I, [vp, C.POINTER(D)]),
+    "fastembedr_tsne_plan_destroy": (None, [vp]),
+}
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True) -> C.CDLL:
+    """Load the native library, building it first when it is absent."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(_build.LIB):
+            if not build_if_missing:
+                raise FileNotFoundError(f"{_build.LIB} is missing; run fastembedr_gb300.build.build()")
+            _build.build()
+        lib = C.CDLL(_build.LIB)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name, None)
+            if fn is None:
+                continue
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = lib
+    return _LIB
+
+
+class CudaEmbeddingError(RuntimeError):
+    pass
+
+
+def check(status: int, what: str) -> None:
+    if status != 0:
+        msg = load().fastembedr_cuda_embedding_last_error()
+        raise CudaEmbeddingError(f"{what} failed: {msg.decode() if msg else 'unknown error'}")
+
+
+def require_gpu() -> C.CDLL:
+    lib = load()
+    if not lib.fastembedr_cuda_available():
+        raise CudaEmbeddingError("No CUDA device is available.")
+    return lib
+
+
+def ptr(a) -> int:
+    """Address of a numpy array or a torch tensor (host or device)."""
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    return a.ctypes.data

@@ -1,0 +1,232 @@
+"""Python mirror of fastEmbedR's R-facing entry points for the CUDA backend.
+
+R is the reference's host language; this module restates the same signatures, argument
+meaning, defaults and recorded configuration (``attr(layout, "fastEmbedR_config")`` /
+``fit$parameters``) over the C ABI, so that the tests and the benchmark drive the library the
+way ``tsne_knn(..., backend = "cuda")`` drives ``knn_tsne_opentsne_cuda_float_cpp``.
+
+Inputs follow the R conventions: ``indices`` is an (n, k) integer matrix (1- or 0-based, self
+excluded or not), ``distances`` the matching (n, k) matrix; layouts are (n, 2) arrays.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+
+
+def _colmajor(a, dtype):
+    return np.asfortranarray(np.asarray(a, dtype=dtype))
+
+
+def knn_index_offset(indices) -> int:
+    """1 when every index lies in [1, n], else 0 (src/embedding_cuda_impl.cpp:933,
+    src/tsne_neighbors.cpp:90-101)."""
+    idx = np.asarray(indices)
+    n = idx.shape[0]
+    return 1 if idx.min() >= 1 and idx.max() <= n else 0
+
+
+@dataclass
+class TsneFit:
+    layout: np.ndarray
+    config: dict = field(default_factory=dict)
+
+
+def fft_grid_size(n: int) -> int:
+    return int(_lib.load().fastembedr_cuda_opentsne_fft_grid_size(int(n)))
+
+
+def tsne_knn(indices, distances, n_neighbors=None, perplexity=None, n_components=2, Y_init=None, seed=4,
+             learning_rate="auto", early_exaggeration_iter=None, early_exaggeration="auto", n_iter=None,
+             exaggeration=None, initial_momentum=0.8, final_momentum=0.8, max_step_norm="auto",
+             negative_gradient_method="auto", min_gain=0.01, auto_config=True, backend="cuda") -> TsneFit:
+    """t-SNE from a supplied KNN graph (R/fast_knn_tsne.R:216-261, policy of R/tsne_control.R:113-231
+    and R/tsne_optimizer_helpers.R:151-221), run by the GB300 library."""
+    if backend != "cuda":
+        raise ValueError("fastembedr_gb300 implements backend = 'cuda' only")
+    method = str(negative_gradient_method).lower()
+    if method not in ("fft", "fitsne", "fit_sne", "interpolation", "auto"):
+        raise ValueError('CUDA openTSNE supports `negative_gradient_method = "fft"` only.')
+    if int(n_components) != 2:
+        raise ValueError("CUDA openTSNE FFT-grid currently supports exactly two output components.")
+    idx = np.asarray(indices)
+    dist = np.asarray(distances, np.float32)
+    if idx.shape != dist.shape or idx.ndim != 2:
+        raise ValueError("KNN `indices` and `distances` must have the same dimensions.")
+    k_all = idx.shape[1]
+    k = int(n_neighbors) if n_neighbors is not None else k_all
+    idx = idx[:, :k]
+    dist = dist[:, :k]
+    n = idx.shape[0]
+    # tsne_auto_parameters_cpp, src/tsne_neighbors.cpp:1820-1868
+    max_pn, max_pk = max(1, (n - 1) // 3), max(1, k // 3)
+    perp = float(min(30, max_pn, max_pk)) if perplexity is None else float(perplexity)
+    if perplexity is None:
+        perp = max(1.0, min(perp, float(min(max_pn, max_pk))))
+    ee_iter = 250 if early_exaggeration_iter is None else int(early_exaggeration_iter)
+    nn_iter = 500 if n_iter is None else int(n_iter)
+    ee = 12.0 if (isinstance(early_exaggeration, str) and early_exaggeration == "auto") else float(early_exaggeration)
+    ex = 1.0 if exaggeration is None else float(exaggeration)
+    opt_sne = bool(auto_config) and isinstance(learning_rate, str) and learning_rate.lower() == "auto"
+    if opt_sne:
+        lr_auto, lr_value = 0, n / 12.0
+    elif isinstance(learning_rate, str):
+        lr_auto, lr_value = 1, -1.0
+    else:
+        lr_auto, lr_value = 0, float(learning_rate)
+    if isinstance(max_step_norm, str):
+        msn = 5.0
+    elif max_step_norm is None or (isinstance(max_step_norm, float) and math.isnan(max_step_norm)):
+        msn = float("nan")
+    else:
+        msn = float(max_step_norm)
+    has_init = Y_init is not None
+    init = np.ascontiguousarray(Y_init, np.float32) if has_init else np.zeros((n, 2), np.float32)
+    if has_init and init.shape != (n, 2):
+        raise ValueError("CUDA openTSNE FFT-grid requires a two-dimensional initialization.")
+    if has_init and not np.all(np.isfinite(init)):
+        raise ValueError("`Y_init` must contain only finite coordinates.")
+    out = np.zeros((n, 2), np.float32)
+    lib = _lib.require_gpu()
+    idx_cm = _colmajor(idx, np.int32)
+    dist_cm = _colmajor(dist, np.float32)
+    st = lib.fastembedr_cuda_opentsne_fft_from_knn_float(
+        idx_cm.ctypes.data, dist_cm.ctypes.data, init.ctypes.data, int(has_init), n, k, 2, perp, ee_iter, nn_iter,
+        ee, ex, lr_value, lr_auto, float(initial_momentum), float(final_momentum), float(min_gain), msn,
+        int(seed) & 0xFFFFFFFF, knn_index_offset(idx), out.ctypes.data)
+    _lib.check(st, "CUDA openTSNE FFT-grid")
+    lr_early = n / ee if lr_auto else lr_value
+    lr_normal = n / max(ex, 1.0) if lr_auto else lr_value
+    config = dict(
+        method="tsne", backend="cuda", n=n, n_neighbors=k, perplexity=perp, early_exaggeration_iter=ee_iter,
+        n_iter=nn_iter, max_iter=ee_iter + nn_iter, early_exaggeration_iter_actual=ee_iter, n_iter_actual=nn_iter,
+        max_iter_actual=ee_iter + nn_iter,
+        learning_rate="auto_opt_sne_n_over_early_exaggeration" if opt_sne else ("auto" if lr_auto else lr_value),
+        learning_rate_early=lr_early, learning_rate_normal=lr_normal, early_exaggeration=ee, exaggeration=ex,
+        initial_momentum=float(initial_momentum), final_momentum=float(final_momentum), min_gain=float(min_gain),
+        max_step_norm=msn, optimizer="opentsne_fitsne_fft_grid_native_cuda", repulsion="fft_grid_cuda_gb300",
+        fft_grid_size=fft_grid_size(n), probabilities="symmetric_sparse_knn_cuda_float32", precision="float32",
+        auto_kld_stop=False, auto_stop_reason="cuda_fft_no_host_kld_monitor", seed=int(seed))
+    return TsneFit(out, config)
+
+
+def tsne_affinities(indices, distances, perplexity, index_offset=None):
+    """Symmetrised CSR P and directed P / entropies from the GPU (diagnostic)."""
+    idx = np.asarray(indices)
+    n, k = idx.shape
+    off = knn_index_offset(idx) if index_offset is None else int(index_offset)
+    cap = 2 * n * k
+    rp = np.zeros(n + 1, np.int32)
+    col = np.zeros(cap, np.int32)
+    val = np.zeros(cap, np.float32)
+    p = np.zeros((n, k), np.float32)
+    h = np.zeros(n, np.float64)
+    nnz = C.c_longlong()
+    tot = C.c_double()
+    lib = _lib.require_gpu()
+    st = lib.fastembedr_cuda_tsne_affinities(_colmajor(idx, np.int32).ctypes.data,
+                                             _colmajor(distances, np.float32).ctypes.data, n, k, float(perplexity),
+                                             off, rp.ctypes.data, col.ctypes.data, val.ctypes.data, cap,
+                                             C.byref(nnz), p.ctypes.data, h.ctypes.data, C.byref(tot))
+    _lib.check(st, "CUDA t-SNE affinities")
+    m = nnz.value
+    return dict(row_ptr=rp, col=col[:m].copy(), val=val[:m].copy(), p_directed=p, entropy=h, total_mass=tot.value)
+
+
+def tsne_force_diagnostic(indices, distances, layout, perplexity, exaggeration=1.0, grid_size=0, interpolation=1,
+                          exact=True, kl=True, index_offset=None):
+    """GPU twin of opentsne_force_diagnostic_cpp (src/tsne_neighbors.cpp:1698-1817)."""
+    idx = np.asarray(indices)
+    n, k = idx.shape
+    off = knn_index_offset(idx) if index_offset is None else int(index_offset)
+    y = np.ascontiguousarray(layout, np.float32)
+    att = np.zeros((n, 2), np.float32)
+    rep = np.zeros((n, 2), np.float32)
+    rex = np.zeros((n, 2), np.float32) if exact else None
+    zg, ze, kv = C.c_double(), C.c_double(), C.c_double()
+    lib = _lib.require_gpu()
+    st = lib.fastembedr_cuda_tsne_force_diagnostic(
+        _colmajor(idx, np.int32).ctypes.data, _colmajor(distances, np.float32).ctypes.data, y.ctypes.data, n, k,
+        float(perplexity), float(exaggeration), int(grid_size), int(interpolation), off, att.ctypes.data,
+        rep.ctypes.data, C.byref(zg), rex.ctypes.data if exact else None, C.byref(ze) if exact else None,
+        C.byref(kv) if kl else None)
+    _lib.check(st, "CUDA t-SNE force diagnostic")
+    out = dict(attractive_force=att, repulsive_force_fft=rep, z_grid=zg.value)
+    if exact:
+        out.update(repulsive_force_exact=rex, sum_q=ze.value)
+    if kl:
+        out["kl"] = kv.value
+    return out
+
+
+class TsnePlan:
+    """Resident t-SNE instance (P, layout and optimizer state stay in HBM).
+
+    ``indices`` / ``distances`` are device tensors (column-major n x k, i.e. the transpose of a
+    row-major (k, n) tensor) or anything exposing ``data_ptr()``.
+    """
+
+    def __init__(self, d_indices_cm, d_distances_cm, n, k, perplexity, init=None, index_offset=0, grid_size=0,
+                 interpolation=1, seed=4):
+        self.lib = _lib.require_gpu()
+        self.n = int(n)
+        h = C.c_void_p()
+        init_a = None if init is None else np.ascontiguousarray(init, np.float32)
+        st = self.lib.fastembedr_tsne_plan_create(_lib.ptr(d_indices_cm), _lib.ptr(d_distances_cm),
+                                                  None if init_a is None else init_a.ctypes.data, self.n, int(k),
+                                                  float(perplexity), int(index_offset), int(grid_size),
+                                                  int(interpolation), int(seed) & 0xFFFFFFFF, C.byref(h))
+        _lib.check(st, "t-SNE plan create")
+        self.h = h
+
+    def run(self, iters, exaggeration, learning_rate, momentum=0.8, min_gain=0.01, max_step_norm=5.0, graph=True):
+        _lib.check(self.lib.fastembedr_tsne_plan_run(self.h, int(iters), float(exaggeration), float(learning_rate),
+                                                     float(momentum), float(min_gain), float(max_step_norm),
+                                                     int(bool(graph))), "t-SNE plan run")
+
+    def profile(self, iters, exaggeration, learning_rate, momentum=0.8, min_gain=0.01, max_step_norm=5.0):
+        tot, stp, grd = C.c_float(), C.c_float(), C.c_float()
+        _lib.check(self.lib.fastembedr_tsne_plan_profile(self.h, int(iters), float(exaggeration),
+                                                         float(learning_rate), float(momentum), float(min_gain),
+                                                         float(max_step_norm), C.byref(tot), C.byref(stp),
+                                                         C.byref(grd)), "t-SNE plan profile")
+        return dict(total_ms=tot.value, step_kernel_ms=stp.value, grid_stage_ms=grd.value)
+
+    def synchronize(self):
+        _lib.check(self.lib.fastembedr_tsne_plan_synchronize(self.h), "t-SNE plan synchronize")
+
+    @property
+    def stream(self) -> int:
+        return int(self.lib.fastembedr_tsne_plan_stream(self.h) or 0)
+
+    def layout(self):
+        out = np.zeros((self.n, 2), np.float32)
+        _lib.check(self.lib.fastembedr_tsne_plan_layout(self.h, out.ctypes.data), "t-SNE plan layout")
+        return out
+
+    def info(self):
+        nnz, g, it, la = C.c_longlong(), C.c_int(), C.c_int(), C.c_int()
+        _lib.check(self.lib.fastembedr_tsne_plan_info(self.h, C.byref(nnz), C.byref(g), C.byref(it), C.byref(la)),
+                   "t-SNE plan info")
+        return dict(nnz=nnz.value, grid_size=g.value, interpolation=it.value, launches_per_iteration=la.value)
+
+    def kl(self):
+        v = C.c_double()
+        _lib.check(self.lib.fastembedr_tsne_plan_kl(self.h, C.byref(v)), "t-SNE plan KL")
+        return v.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fastembedr_tsne_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,43 @@
+// Internal interfaces between the t-SNE translation units (affinities, grid
+// repulsion, fused update, C ABI). Device pointers only; the stream is explicit.
+#pragma once
+
+#include "common.cuh"
+
+namespace fe {
+
+// Symmetrised sparse P on the device: CSR with ascending columns per row, the same
+// integers and float values as build_tsne_probabilities_float
+// (fastEmbedR src/tsne_neighbors.cpp:616-724).
+struct DeviceCsr {
+  int n = 0;
+  long long nnz = 0;
+  int* row_ptr = nullptr;  // n + 1
+  int* col = nullptr;      // nnz
+  float* val = nullptr;    // nnz
+  double total_mass = 0.0;
+  Arena arena;
+};
+
+// Validate KNN input (column-major n x k); throws with the reference CPU messages.
+void validate_knn(const int* d_idx, const float* d_dist, int n, int k, int offset, cudaStream_t s);
+
+// Per-row perplexity bisection (FP32 exp, FP64 sums); writes directed P row-major n x k and,
+// when non-null, the entropy reached by each row.
+void row_probabilities(const int* d_idx, const float* d_dist, int n, int k, float perplexity,
+                       float* d_p, double* d_entropy, cudaStream_t s);
+
+// Emit both directions of every non-self directed edge, bucket by row, sort each row by
+// column, sum duplicates in double and fill the CSR (allocated inside `out`).
+void symmetrise(const int* d_idx, const float* d_p, int n, int k, int offset, DeviceCsr& out,
+                cudaStream_t s);
+
+// Grid policy of the reference CUDA path (src/embedding_cuda_kernels.cpp:5610-5623), including
+// the FASTEMBEDR_TSNE_FFT_GRID override.
+int cuda_fft_grid_size(int n);
+
+// Interpolation scheme of the grid repulsion.
+enum InterpMode { kInterpBilinear = 0, kInterpLagrange3 = 1 };
+int interp_mode_from_env();
+
+}  // namespace fe

@@ -1,0 +1,533 @@
+// t-SNE affinities on the GPU: KNN validation, perplexity bisection and the bit-exact
+// symmetrised CSR.
+//
+// Reference behaviour followed (fastEmbedR):
+//   - index/distance validation and messages: src/tsne_neighbors.cpp:630-640
+//   - per-row bisection: src/tsne_neighbors.cpp:532-614 (control flow, tolerance 1e-5,
+//     200 iterations, uniform fallback) evaluated with FP32 exp and FP64 sums as in the
+//     FP64 test oracle tests/testthat/helper-tsne-reference.R:1-54
+//   - symmetrisation: src/tsne_neighbors.cpp:616-724 (self edges skipped, duplicate
+//     directed edges summed in double, value = float(sum) * float(0.5 / total))
+//
+// GPU layout: the CPU sorts 64-bit (min, max) pair keys once; here every directed edge is
+// emitted into both endpoint rows (bucketed by an atomic counting pass), each row bucket is
+// sorted by (column, p bits) with an always-ascending bitonic network, and runs of equal
+// columns are reduced. This yields exactly the CPU's CSR structure: the same column set per
+// row, ascending, with the same double sums per pair.
+#include <cfloat>
+#include <climits>
+#include <cmath>
+#include <cstdlib>
+
+#include "tsne.cuh"
+
+namespace fe {
+
+// ---------------------------------------------------------------- validation
+__global__ void validate_knn_kernel(const int* __restrict__ idx, const float* __restrict__ dist,
+                                    long long total, int n, int offset, unsigned* flags) {
+  unsigned local = 0u;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int nb = idx[t] - offset;
+    if (nb < 0 || nb >= n) local |= 1u;
+    const float d = dist[t];
+    if (!isfinite(d) || d < 0.0f) local |= 2u;
+  }
+  if (local) atomicOr(flags, local);
+}
+
+void validate_knn(const int* d_idx, const float* d_dist, int n, int k, int offset, cudaStream_t s) {
+  unsigned* d_flags = nullptr;
+  FE_CUDA(cudaMallocAsync(&d_flags, sizeof(unsigned), s));
+  FE_CUDA(cudaMemsetAsync(d_flags, 0, sizeof(unsigned), s));
+  const long long total = (long long)n * k;
+  const int blocks = std::max(1, std::min(ceil_div(total, 256), sm_count() * 8));
+  validate_knn_kernel<<<blocks, 256, 0, s>>>(d_idx, d_dist, total, n, offset, d_flags);
+  FE_LAUNCH("validate_knn_kernel");
+  unsigned flags = 0u;
+  FE_CUDA(cudaMemcpyAsync(&flags, d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  FE_CUDA(cudaStreamSynchronize(s));
+  FE_CUDA(cudaFreeAsync(d_flags, s));
+  if (flags & 1u) throw Error("KNN indices are out of range.");
+  if (flags & 2u) throw Error("KNN distances must be finite and non-negative.");
+}
+
+// ---------------------------------------------------------------- bisection
+// One warp per row. The CTA first stages a tile of `rows` rows x k columns of the
+// column-major distances in shared memory (each column read is `rows` consecutive floats),
+// then every warp bisects its rows out of shared memory.
+constexpr int kBisectWarps = 8;
+
+__global__ void __launch_bounds__(kBisectWarps * 32)
+row_probabilities_kernel(const float* __restrict__ dist, int n, int k, int rows,
+                         double log_perplexity, float* __restrict__ p_out,
+                         double* __restrict__ entropy_out) {
+  extern __shared__ float tile[];  // rows x k, row-major
+  const int r0 = blockIdx.x * rows;
+  const int nrows = min(rows, n - r0);
+  for (int t = threadIdx.x; t < rows * k; t += blockDim.x) {
+    const int rr = t % rows, j = t / rows;
+    if (rr < nrows) tile[rr * k + j] = dist[(long long)j * n + r0 + rr];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int rr = warp; rr < nrows; rr += kBisectWarps) {
+    const float* d = tile + rr * k;
+    double min_d2 = DBL_MAX, max_d2 = 0.0;
+    for (int j = lane; j < k; j += 32) {
+      const double dj = d[j];
+      const double d2 = dj * dj;  // exact: a float squared fits in a double
+      min_d2 = fmin(min_d2, d2);
+      max_d2 = fmax(max_d2, d2);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      min_d2 = fmin(min_d2, __shfl_xor_sync(0xffffffffu, min_d2, o));
+      max_d2 = fmax(max_d2, __shfl_xor_sync(0xffffffffu, max_d2, o));
+    }
+    float* prow = p_out + (long long)(r0 + rr) * k;
+    if (max_d2 - min_d2 <= DBL_EPSILON * fmax(1.0, max_d2)) {
+      const float u = 1.0f / (float)k;
+      for (int j = lane; j < k; j += 32) prow[j] = u;
+      if (entropy_out && lane == 0) entropy_out[r0 + rr] = log((double)k);
+      continue;
+    }
+    double beta = 1.0, beta_min = -DBL_MAX, beta_max = DBL_MAX;
+    double beta_eval = beta, sum_eval = 1.0, entropy_eval = 0.0;
+    for (int it = 0; it < 200; ++it) {
+      double sp = 0.0, sw = 0.0;
+      for (int j = lane; j < k; j += 32) {
+        const double dj = d[j];
+        const double s = dj * dj - min_d2;
+        const double p = (double)expf((float)(-beta * s));
+        sp += p;
+        sw += s * p;
+      }
+      sp = warp_sum(sp);
+      sw = warp_sum(sw);
+      const double entropy = beta * sw / sp + log(sp);
+      beta_eval = beta;
+      sum_eval = sp;
+      entropy_eval = entropy;
+      const double diff = entropy - log_perplexity;
+      if (fabs(diff) < 1e-5) break;
+      if (diff > 0.0) {
+        beta_min = beta;
+        beta = (beta_max == DBL_MAX) ? beta * 2.0 : 0.5 * (beta + beta_max);
+      } else {
+        beta_max = beta;
+        beta = (beta_min == -DBL_MAX) ? beta * 0.5 : 0.5 * (beta + beta_min);
+      }
+      if (!isfinite(beta)) break;
+    }
+    const double inv = 1.0 / sum_eval;
+    for (int j = lane; j < k; j += 32) {
+      const double dj = d[j];
+      const double s = dj * dj - min_d2;
+      prow[j] = (float)((double)expf((float)(-beta_eval * s)) * inv);
+    }
+    if (entropy_out && lane == 0) entropy_out[r0 + rr] = entropy_eval;
+  }
+}
+
+void row_probabilities(const int* /*d_idx*/, const float* d_dist, int n, int k, float perplexity,
+                       float* d_p, double* d_entropy, cudaStream_t s) {
+  int rows = 32;
+  while (rows > 1 && (std::size_t)rows * k * sizeof(float) > 96 * 1024) rows >>= 1;
+  const std::size_t smem = (std::size_t)rows * k * sizeof(float);
+  if (smem > 48 * 1024)
+    FE_CUDA(cudaFuncSetAttribute(row_probabilities_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem));
+  row_probabilities_kernel<<<ceil_div(n, rows), kBisectWarps * 32, smem, s>>>(
+      d_dist, n, k, rows, std::log((double)perplexity), d_p, d_entropy);
+  FE_LAUNCH("row_probabilities_kernel");
+}
+
+// ---------------------------------------------------------------- scan
+// Exclusive scan of n int32 counts into n + 1 int64 offsets (three passes).
+constexpr int kScanBlock = 1024;
+
+__global__ void scan_blocks_kernel(const int* __restrict__ in, long long* __restrict__ out, int n,
+                                   long long* __restrict__ block_sums) {
+  __shared__ long long warp_tot[32];
+  const int i = blockIdx.x * kScanBlock + threadIdx.x;
+  long long v = i < n ? in[i] : 0;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  long long x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_tot[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    long long w = warp_tot[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    warp_tot[lane] = w;
+  }
+  __syncthreads();
+  const long long before = (warp > 0 ? warp_tot[warp - 1] : 0) + x - v;
+  if (i < n) out[i] = before;
+  if (threadIdx.x == kScanBlock - 1) block_sums[blockIdx.x] = warp_tot[31];
+}
+
+__global__ void scan_sums_kernel(long long* sums, int nb, long long* total_out) {
+  // single block: sequential carry over chunks of 1024
+  __shared__ long long warp_tot[32];
+  __shared__ long long carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int base = 0; base < nb; base += kScanBlock) {
+    const int i = base + threadIdx.x;
+    const long long v = i < nb ? sums[i] : 0;
+    long long x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      long long w = warp_tot[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const long long y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += y;
+      }
+      warp_tot[lane] = w;
+    }
+    __syncthreads();
+    const long long excl = carry + (warp > 0 ? warp_tot[warp - 1] : 0) + x - v;
+    if (i < nb) sums[i] = excl;
+    __syncthreads();
+    if (threadIdx.x == 0) carry += warp_tot[31];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total_out = carry;
+}
+
+__global__ void scan_add_kernel(long long* out, int n, const long long* sums) {
+  const int i = blockIdx.x * kScanBlock + threadIdx.x;
+  if (i < n) out[i] += sums[blockIdx.x];
+}
+
+// out must hold n + 1 values; out[n] = total. tmp must hold ceil(n / 1024) values.
+static void exclusive_scan(const int* in, long long* out, int n, long long* tmp, cudaStream_t s) {
+  const int nb = std::max(1, ceil_div(n, kScanBlock));
+  scan_blocks_kernel<<<nb, kScanBlock, 0, s>>>(in, out, n, tmp);
+  FE_LAUNCH("scan_blocks_kernel");
+  scan_sums_kernel<<<1, kScanBlock, 0, s>>>(tmp, nb, out + n);
+  FE_LAUNCH("scan_sums_kernel");
+  scan_add_kernel<<<nb, kScanBlock, 0, s>>>(out, n, tmp);
+  FE_LAUNCH("scan_add_kernel");
+}
+
+// ---------------------------------------------------------------- symmetrisation
+__global__ void count_edges_kernel(const int* __restrict__ idx, int n, int k, int offset,
+                                   int* __restrict__ counts) {
+  const long long total = (long long)n * k;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % n);
+    const int nb = idx[t] - offset;  // column-major: t = j * n + i
+    if (nb == i) continue;
+    atomicAdd(counts + i, 1);
+    atomicAdd(counts + nb, 1);
+  }
+}
+
+__device__ __forceinline__ unsigned long long edge_key(int col, float p) {
+  return ((unsigned long long)(unsigned)col << 32) | (unsigned long long)__float_as_uint(p);
+}
+
+__global__ void fill_buckets_kernel(const int* __restrict__ idx, const float* __restrict__ p, int n, int k,
+                                    int offset, unsigned long long* __restrict__ cursor,
+                                    unsigned long long* __restrict__ bucket) {
+  const long long total = (long long)n * k;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % n);
+    const int j = (int)(t / n);
+    const int nb = idx[t] - offset;
+    if (nb == i) continue;
+    const float pv = p[(long long)i * k + j];
+    bucket[atomicAdd(cursor + i, 1ull)] = edge_key(nb, pv);
+    bucket[atomicAdd(cursor + nb, 1ull)] = edge_key(i, pv);
+  }
+}
+
+constexpr int kSortThreads = 256;
+constexpr int kSortCap = 8192;  // entries of a row sorted in shared memory
+
+// Always-ascending bitonic network over `pw` (power of two) slots; compare(i, j) keeps the
+// minimum at i. Slots at or beyond `len` hold +inf (explicitly in shared memory, virtually
+// in global memory), which this formulation never moves below a real key.
+template <bool kGlobal>
+__device__ void bitonic_sort(unsigned long long* a, int len, int pw) {
+  for (int size = 2; size <= pw; size <<= 1) {
+    const int half = size >> 1;
+    for (int t = threadIdx.x; t < pw / 2; t += blockDim.x) {
+      const int blk = t / half, off = t % half;
+      const int i = blk * size + off, j = blk * size + size - 1 - off;
+      if (!kGlobal || j < len) {
+        const unsigned long long x = a[i], y = a[j];
+        if (y < x) {
+          a[i] = y;
+          a[j] = x;
+        }
+      }
+    }
+    __syncthreads();
+    for (int stride = half >> 1; stride > 0; stride >>= 1) {
+      for (int t = threadIdx.x; t < pw / 2; t += blockDim.x) {
+        const int blk = t / stride, off = t % stride;
+        const int i = blk * 2 * stride + off, j = i + stride;
+        if (!kGlobal || j < len) {
+          const unsigned long long x = a[i], y = a[j];
+          if (y < x) {
+            a[i] = y;
+            a[j] = x;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// Sort each row bucket by (column, p bits); rows above kSortCap are queued for the
+// global-memory path. Then collapse runs of equal columns: the compacted (column, float(sum))
+// entries are written back to the start of the bucket, `ucount` gets the unique count and
+// `row_mass` the double sum of the row's pair sums.
+__global__ void __launch_bounds__(kSortThreads)
+sort_unique_rows_kernel(unsigned long long* __restrict__ bucket, const long long* __restrict__ offs, int n,
+                        int* __restrict__ ucount, double* __restrict__ row_mass, int* __restrict__ big_rows,
+                        int* __restrict__ big_count) {
+  extern __shared__ unsigned long long sm[];
+  __shared__ int warp_cnt[kSortThreads / 32];
+  __shared__ double warp_mass[kSortThreads / 32];
+  for (int row = blockIdx.x; row < n; row += gridDim.x) {
+    const long long b = offs[row];
+    const int len = (int)(offs[row + 1] - b);
+    if (len > kSortCap) {
+      if (threadIdx.x == 0) big_rows[atomicAdd(big_count, 1)] = row;
+      continue;
+    }
+    int pw = 1;
+    while (pw < len) pw <<= 1;
+    for (int t = threadIdx.x; t < pw; t += blockDim.x) sm[t] = t < len ? bucket[b + t] : ~0ull;
+    __syncthreads();
+    if (len > 1) bitonic_sort<false>(sm, len, pw);
+    // run starts and sums; each start owns the run that follows it
+    int my_cnt = 0;
+    double my_mass = 0.0;
+    for (int base = 0; base < len; base += blockDim.x) {
+      const int t = base + threadIdx.x;
+      bool start = false;
+      if (t < len) start = (t == 0) || ((sm[t] >> 32) != (sm[t - 1] >> 32));
+      const unsigned ballot = __ballot_sync(0xffffffffu, start);
+      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+      if (lane == 0) warp_cnt[warp] = __popc(ballot);
+      __syncthreads();
+      int before = 0;
+      for (int w = 0; w < warp; ++w) before += warp_cnt[w];
+      if (start) {
+        double sum = 0.0;
+        const unsigned col = (unsigned)(sm[t] >> 32);
+        for (int u = t; u < len && (unsigned)(sm[u] >> 32) == col; ++u) sum += (double)__uint_as_float((unsigned)sm[u]);
+        const int pos = my_cnt + before + __popc(ballot & ((1u << lane) - 1u));
+        bucket[b + pos] = ((unsigned long long)col << 32) | (unsigned long long)__float_as_uint((float)sum);
+        my_mass += sum;
+      }
+      int chunk_total = 0;
+      for (int w = 0; w < (int)(blockDim.x / 32); ++w) chunk_total += warp_cnt[w];
+      my_cnt += chunk_total;  // identical in every thread
+      __syncthreads();
+    }
+    // row mass: block reduction in a fixed order
+    double m = warp_sum(my_mass);
+    if ((threadIdx.x & 31) == 0) warp_mass[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double tot = 0.0;
+      for (int w = 0; w < (int)(blockDim.x / 32); ++w) tot += warp_mass[w];
+      row_mass[row] = tot;
+      ucount[row] = my_cnt;
+    }
+    __syncthreads();
+  }
+}
+
+// Rows longer than kSortCap: one CTA sorts the bucket in place in global memory, then a
+// single thread collapses the runs (rare, pathological in-degree).
+__global__ void __launch_bounds__(1024)
+sort_unique_big_rows_kernel(unsigned long long* __restrict__ bucket, const long long* __restrict__ offs,
+                            const int* __restrict__ big_rows, const int* __restrict__ big_count,
+                            int* __restrict__ ucount, double* __restrict__ row_mass) {
+  const int count = *big_count;
+  for (int r = blockIdx.x; r < count; r += gridDim.x) {
+    const int row = big_rows[r];
+    const long long b = offs[row];
+    const int len = (int)(offs[row + 1] - b);
+    int pw = 1;
+    while (pw < len) pw <<= 1;
+    bitonic_sort<true>(bucket + b, len, pw);
+    if (threadIdx.x == 0) {
+      int w = 0;
+      double mass = 0.0;
+      for (int t = 0; t < len;) {
+        const unsigned col = (unsigned)(bucket[b + t] >> 32);
+        double sum = 0.0;
+        while (t < len && (unsigned)(bucket[b + t] >> 32) == col) {
+          sum += (double)__uint_as_float((unsigned)bucket[b + t]);
+          ++t;
+        }
+        bucket[b + w] = ((unsigned long long)col << 32) | (unsigned long long)__float_as_uint((float)sum);
+        ++w;
+        mass += sum;
+      }
+      ucount[row] = w;
+      row_mass[row] = mass;
+    }
+    __syncthreads();
+  }
+}
+
+// Deterministic total: one block, fixed assignment and fixed tree.
+__global__ void total_mass_kernel(const double* __restrict__ row_mass, int n, double* out_total, float* out_norm) {
+  __shared__ double part[1024];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += row_mass[i];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) part[threadIdx.x] += part[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double total = 0.5 * part[0];  // every pair sum appears in both of its rows
+    *out_total = total;
+    *out_norm = (float)(0.5 / total);
+  }
+}
+
+__global__ void fill_csr_kernel(const unsigned long long* __restrict__ bucket, const long long* __restrict__ offs,
+                                const long long* __restrict__ row_ptr64, int n, const float* __restrict__ norm,
+                                int* __restrict__ row_ptr, int* __restrict__ col, float* __restrict__ val) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp > n) return;
+  if (lane == 0) row_ptr[warp] = (int)row_ptr64[warp];
+  if (warp == n) return;
+  const float nm = *norm;
+  const long long src = offs[warp];
+  const long long dst = row_ptr64[warp];
+  const int cnt = (int)(row_ptr64[warp + 1] - dst);
+  for (int t = lane; t < cnt; t += 32) {
+    const unsigned long long e = bucket[src + t];
+    col[dst + t] = (int)(e >> 32);
+    val[dst + t] = __uint_as_float((unsigned)e) * nm;
+  }
+}
+
+void symmetrise(const int* d_idx, const float* d_p, int n, int k, int offset, DeviceCsr& out, cudaStream_t s) {
+  const long long directed = (long long)n * k;
+  const int nscan = std::max(1, ceil_div(n, kScanBlock));
+  int* counts = nullptr;
+  long long* offs = nullptr;
+  long long* scan_tmp = nullptr;
+  unsigned long long* cursor = nullptr;
+  unsigned long long* bucket = nullptr;
+  int* ucount = nullptr;
+  double* row_mass = nullptr;
+  int* big_rows = nullptr;
+  int* big_count = nullptr;
+  long long* row_ptr64 = nullptr;
+  double* d_total = nullptr;
+  float* d_norm = nullptr;
+  Arena work;
+  work.reserve(&counts, n);
+  work.reserve(&offs, n + 1);
+  work.reserve(&scan_tmp, nscan);
+  work.reserve(&cursor, n);
+  work.reserve(&bucket, 2 * directed);
+  work.reserve(&ucount, n);
+  work.reserve(&row_mass, n);
+  work.reserve(&big_rows, n);
+  work.reserve(&big_count, 1);
+  work.reserve(&row_ptr64, n + 1);
+  work.reserve(&d_total, 1);
+  work.reserve(&d_norm, 1);
+  work.commit("t-SNE symmetrisation workspace");
+
+  const int grid = std::max(1, std::min(ceil_div(directed, 256), sm_count() * 16));
+  FE_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * n, s));
+  FE_CUDA(cudaMemsetAsync(big_count, 0, sizeof(int), s));
+  count_edges_kernel<<<grid, 256, 0, s>>>(d_idx, n, k, offset, counts);
+  FE_LAUNCH("count_edges_kernel");
+  exclusive_scan(counts, offs, n, scan_tmp, s);
+  FE_CUDA(cudaMemcpyAsync(cursor, offs, sizeof(long long) * n, cudaMemcpyDeviceToDevice, s));
+  fill_buckets_kernel<<<grid, 256, 0, s>>>(d_idx, d_p, n, k, offset, cursor, bucket);
+  FE_LAUNCH("fill_buckets_kernel");
+
+  const std::size_t smem = kSortCap * sizeof(unsigned long long);
+  FE_CUDA(cudaFuncSetAttribute(sort_unique_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  sort_unique_rows_kernel<<<std::min(n, sm_count() * 8), kSortThreads, smem, s>>>(bucket, offs, n, ucount,
+                                                                                  row_mass, big_rows, big_count);
+  FE_LAUNCH("sort_unique_rows_kernel");
+  sort_unique_big_rows_kernel<<<sm_count(), 1024, 0, s>>>(bucket, offs, big_rows, big_count, ucount, row_mass);
+  FE_LAUNCH("sort_unique_big_rows_kernel");
+  exclusive_scan(ucount, row_ptr64, n, scan_tmp, s);
+  total_mass_kernel<<<1, 1024, 0, s>>>(row_mass, n, d_total, d_norm);
+  FE_LAUNCH("total_mass_kernel");
+
+  long long nnz = 0;
+  double total = 0.0;
+  FE_CUDA(cudaMemcpyAsync(&nnz, row_ptr64 + n, sizeof(long long), cudaMemcpyDeviceToHost, s));
+  FE_CUDA(cudaMemcpyAsync(&total, d_total, sizeof(double), cudaMemcpyDeviceToHost, s));
+  FE_CUDA(cudaStreamSynchronize(s));
+  if (nnz <= 0) throw Error("KNN graph produced no non-self t-SNE edges.");
+  if (nnz > INT_MAX) throw Error("symmetrised t-SNE graph exceeds 2^31 - 1 entries.");
+  if (!std::isfinite(total) || total <= 0.0) throw Error("t-SNE probability normalization failed.");
+
+  out.n = n;
+  out.nnz = nnz;
+  out.total_mass = total;
+  out.arena.release();
+  out.arena.reserve(&out.row_ptr, n + 1);
+  out.arena.reserve(&out.col, nnz);
+  out.arena.reserve(&out.val, nnz);
+  out.arena.commit("t-SNE CSR");
+  fill_csr_kernel<<<ceil_div((long long)(n + 1) * 32, 256), 256, 0, s>>>(bucket, offs, row_ptr64, n, d_norm,
+                                                                          out.row_ptr, out.col, out.val);
+  FE_LAUNCH("fill_csr_kernel");
+  FE_CUDA(cudaStreamSynchronize(s));
+}
+
+int cuda_fft_grid_size(int n) {
+  int g = 512;
+  if (n < 20000) g = 256;
+  if (n >= 100000) g = 1024;
+  const char* env = std::getenv("FASTEMBEDR_TSNE_FFT_GRID");
+  if (env && env[0]) {
+    const int r = std::atoi(env);
+    if (r == 32 || r == 64 || r == 128 || r == 256 || r == 512 || r == 1024) g = r;
+  }
+  return g;
+}
+
+int interp_mode_from_env() {
+  const char* env = std::getenv("FASTEMBEDR_TSNE_INTERPOLATION");
+  if (env && (env[0] == 'b' || env[0] == 'B')) return kInterpBilinear;
+  return kInterpLagrange3;
+}
+
+}  // namespace fe

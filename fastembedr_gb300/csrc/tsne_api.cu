@@ -1,0 +1,469 @@
+// C ABI of the t-SNE optimizer (see include/fastembedr_cuda.h) and the host driver behind it:
+// the GB300 counterpart of fastembedr_cuda_opentsne_fft_from_knn_impl
+// (fastEmbedR src/embedding_cuda_kernels.cpp:5629-6176) and of the validation in
+// knn_tsne_opentsne_cuda_float_impl (src/embedding_cuda_impl.cpp:2239-2370).
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <tuple>
+#include <type_traits>
+#include <vector>
+
+#include "../../include/fastembedr_cuda.h"
+#include "philox.cuh"
+#include "tsne_exact.cuh"
+#include "tsne_grid.cuh"
+
+namespace fe {
+
+// Seeded N(0, 1e-4^2) layout (Box-Muller on Philox4x32-10 draws) for has_init = 0.
+__global__ void random_init_kernel(float2* __restrict__ y, int n, unsigned seed) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint4 r = philox4x32_10(make_uint4((unsigned)i, 0u, 0x7a5e11u, 0u), make_uint2(seed, 0x1badb002u));
+    const float u1 = fmaxf(u01(r.x), 1.0e-12f), u2 = u01(r.y);
+    const float rad = 1.0e-4f * sqrtf(-2.0f * logf(u1));
+    float sn, cs;
+    sincospif(2.0f * u2, &sn, &cs);
+    y[i] = make_float2(rad * cs, rad * sn);
+  }
+}
+
+__global__ void double_to_float_kernel(const double* __restrict__ in, float* __restrict__ out, long long m) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < m; t += (long long)gridDim.x * blockDim.x)
+    out[t] = (float)in[t];
+}
+
+bool graph_capture_enabled() {
+  const char* env = std::getenv("FASTEMBEDR_CUDA_GRAPH_CAPTURE");
+  if (!env || !env[0]) return true;
+  return !(std::strcmp(env, "0") == 0 || std::strcmp(env, "false") == 0 || std::strcmp(env, "FALSE") == 0 ||
+           std::strcmp(env, "no") == 0 || std::strcmp(env, "NO") == 0);
+}
+
+// Optimizer state of one t-SNE instance resident on the device.
+struct TsneJob {
+  DeviceCsr P;
+  TsneDevice D;
+  Stream stream;
+  // graph cache keyed by (iterations, exaggeration, lr, momentum, min_gain, max_step)
+  using Key = std::tuple<int, float, float, float, float, float>;
+  std::map<Key, std::pair<cudaGraph_t, cudaGraphExec_t>> graphs;
+  ~TsneJob() {
+    for (auto& kv : graphs) {
+      if (kv.second.second) cudaGraphExecDestroy(kv.second.second);
+      if (kv.second.first) cudaGraphDestroy(kv.second.first);
+    }
+  }
+
+  // KNN (device, column-major) -> P (CSR) -> optimizer state with the given init.
+  void prepare(const int* d_idx, const float* d_dist, const float* init_host, int n, int k, float perplexity,
+               int offset, int grid, int mode, unsigned seed) {
+    cudaStream_t s = stream.s;
+    validate_knn(d_idx, d_dist, n, k, offset, s);
+    {
+      float* d_p = nullptr;
+      Arena tmp;
+      tmp.reserve(&d_p, (std::size_t)n * k);
+      tmp.commit("t-SNE directed probabilities");
+      row_probabilities(d_idx, d_dist, n, k, perplexity, d_p, nullptr, s);
+      symmetrise(d_idx, d_p, n, k, offset, P, s);
+    }
+    tsne_device_alloc(D, n, grid, mode);
+    float2* d_init = nullptr;
+    Arena tmp;
+    tmp.reserve(&d_init, n);
+    tmp.commit("t-SNE init");
+    if (init_host) {
+      FE_CUDA(cudaMemcpyAsync(d_init, init_host, sizeof(float2) * n, cudaMemcpyHostToDevice, s));
+    } else {
+      random_init_kernel<<<std::max(1, std::min(ceil_div(n, 256), sm_count() * 8)), 256, 0, s>>>(d_init, n, seed);
+      FE_LAUNCH("random_init_kernel");
+    }
+    tsne_device_init(D, reinterpret_cast<const float*>(d_init), s);
+    FE_CUDA(cudaStreamSynchronize(s));
+  }
+
+  void run(int iters, float exag, float lr, float mom, float min_gain, float max_step, bool use_graph) {
+    cudaStream_t s = stream.s;
+    if (iters <= 0) return;
+    if (!use_graph || !graph_capture_enabled()) {
+      for (int it = 0; it < iters; ++it) tsne_iteration(D, P, exag, lr, mom, min_gain, max_step, s);
+      return;
+    }
+    constexpr int kChunk = 25;  // iterations per graph, as the reference's graph chunks
+    int left = iters;
+    while (left > 0) {
+      const int c = std::min(kChunk, left);
+      const Key key{c, exag, lr, mom, min_gain, max_step};
+      auto it = graphs.find(key);
+      if (it == graphs.end()) {
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t ge = nullptr;
+        FE_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        try {
+          for (int r = 0; r < c; ++r) tsne_iteration(D, P, exag, lr, mom, min_gain, max_step, s);
+        } catch (...) {
+          cudaStreamEndCapture(s, &g);
+          if (g) cudaGraphDestroy(g);
+          throw;
+        }
+        FE_CUDA(cudaStreamEndCapture(s, &g));
+        FE_CUDA(cudaGraphInstantiate(&ge, g, 0));
+        it = graphs.emplace(key, std::make_pair(g, ge)).first;
+      }
+      FE_CUDA(cudaGraphLaunch(it->second.second, s));
+      left -= c;
+    }
+  }
+
+  void schedule(int early_iter, int n_iter, float early_exag, float exag, float lr, int lr_auto, float m0, float m1,
+                float min_gain, float max_step) {
+    const int n = D.n;
+    const float lr_early = lr_auto ? (float)((double)n / std::max((double)early_exag, 1e-300)) : lr;
+    const float lr_normal = lr_auto ? (float)((double)n / std::max((double)exag, 1e-300)) : lr;
+    run(early_iter, early_exag, lr_early, m0, min_gain, max_step, true);
+    run(n_iter, exag, lr_normal, m1, min_gain, max_step, true);
+  }
+
+  void layout(float* out_host) {
+    cudaStream_t s = stream.s;
+    float* d_out = nullptr;
+    Arena tmp;
+    tmp.reserve(&d_out, 2 * (std::size_t)D.n);
+    tmp.commit("t-SNE output");
+    tsne_finalize(D, d_out, s);
+    FE_CUDA(cudaMemcpyAsync(out_host, d_out, sizeof(float) * 2 * D.n, cudaMemcpyDeviceToHost, s));
+    FE_CUDA(cudaStreamSynchronize(s));
+  }
+};
+
+// Argument checks of fastembedr_cuda_opentsne_fft_from_knn_impl (src/embedding_cuda_kernels.cpp:5661-5671).
+void check_tsne_args(const void* idx, const void* dist, const float* init, int has_init, int n, int k,
+                     int n_components, float perplexity, int early_iter, int n_iter, float early_exag, float exag,
+                     float lr, int lr_auto, float m0, float m1, float min_gain, const float* out) {
+  if (idx == nullptr || dist == nullptr || out == nullptr || (has_init && init == nullptr))
+    throw Error("null CUDA openTSNE input pointer");
+  if (n < 2 || k < 1 || k > 1024 || n_components != 2 || !(perplexity > 0.0f) || early_iter < 0 || n_iter < 0 ||
+      early_iter + n_iter < 1 || !(early_exag > 0.0f) || !(exag > 0.0f) || (!lr_auto && !(lr > 0.0f)) || m0 < 0.0f ||
+      m1 < 0.0f || !(min_gain > 0.0f))
+    throw Error("invalid CUDA openTSNE FFT-grid dimensions or parameters");
+}
+
+template <typename DistT>
+int run_tsne_from_knn(const int* indices, const DistT* distances, bool on_device, const float* init, int has_init,
+                      int n, int k, int n_components, float perplexity, int early_iter, int n_iter, float early_exag,
+                      float exag, float lr, int lr_auto, float m0, float m1, float min_gain, float max_step,
+                      unsigned seed, int offset, float* out) {
+  return guarded([&] {
+    check_tsne_args(indices, distances, init, has_init, n, k, n_components, perplexity, early_iter, n_iter,
+                    early_exag, exag, lr, lr_auto, m0, m1, min_gain, out);
+    auto job = std::make_unique<TsneJob>();
+    cudaStream_t s = job->stream.s;
+    const std::size_t items = (std::size_t)n * k;
+    int* d_idx = nullptr;
+    float* d_dist = nullptr;
+    DistT* d_raw = nullptr;
+    Arena in;
+    if (!on_device) in.reserve(&d_idx, items);
+    if (!on_device || !std::is_same<DistT, float>::value) in.reserve(&d_dist, items);
+    if (!on_device && !std::is_same<DistT, float>::value) in.reserve(&d_raw, items);
+    in.commit("CUDA openTSNE KNN input");
+    const int* idx_ptr = on_device ? indices : d_idx;
+    if (!on_device) FE_CUDA(cudaMemcpyAsync(d_idx, indices, sizeof(int) * items, cudaMemcpyHostToDevice, s));
+    const float* dist_ptr = nullptr;
+    if constexpr (std::is_same<DistT, float>::value) {
+      if (on_device) {
+        dist_ptr = distances;
+      } else {
+        FE_CUDA(cudaMemcpyAsync(d_dist, distances, sizeof(float) * items, cudaMemcpyHostToDevice, s));
+        dist_ptr = d_dist;
+      }
+    } else {
+      const DistT* src = distances;
+      if (!on_device) {
+        FE_CUDA(cudaMemcpyAsync(d_raw, distances, sizeof(DistT) * items, cudaMemcpyHostToDevice, s));
+        src = d_raw;
+      }
+      double_to_float_kernel<<<std::max(1, std::min(ceil_div((long long)items, 256), sm_count() * 8)), 256, 0, s>>>(
+          src, d_dist, (long long)items);
+      FE_LAUNCH("double_to_float_kernel");
+      dist_ptr = d_dist;
+    }
+    job->prepare(idx_ptr, dist_ptr, has_init ? init : nullptr, n, k, perplexity, offset, cuda_fft_grid_size(n),
+                 interp_mode_from_env(), seed);
+    in.release();
+    job->schedule(early_iter, n_iter, early_exag, exag, lr, lr_auto, m0, m1, min_gain, max_step);
+    job->layout(out);
+  });
+}
+
+}  // namespace fe
+
+struct fastembedr_tsne_plan {
+  fe::TsneJob job;
+};
+
+extern "C" {
+
+bool fastembedr_cuda_available(void) {
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return count > 0;
+}
+
+const char* fastembedr_cuda_embedding_last_error(void) { return fe::last_error(); }
+
+int fastembedr_cuda_opentsne_fft_grid_size(int n) { return fe::cuda_fft_grid_size(n); }
+
+int fastembedr_cuda_opentsne_fft_from_knn_float(const int* indices, const float* distances, const float* init,
+                                                int has_init, int n, int k, int n_components, float perplexity,
+                                                int early_iter, int n_iter, float early_exag, float exag, float lr,
+                                                int lr_auto, float m0, float m1, float min_gain, float max_step,
+                                                unsigned int seed, int index_offset, float* out) {
+  return fe::run_tsne_from_knn<float>(indices, distances, false, init, has_init, n, k, n_components, perplexity,
+                                      early_iter, n_iter, early_exag, exag, lr, lr_auto, m0, m1, min_gain, max_step,
+                                      seed, index_offset, out);
+}
+
+int fastembedr_cuda_opentsne_fft_from_knn(const int* indices, const double* distances, const float* init,
+                                          int has_init, int n, int k, int n_components, float perplexity,
+                                          int early_iter, int n_iter, float early_exag, float exag, float lr,
+                                          int lr_auto, float m0, float m1, float min_gain, float max_step,
+                                          unsigned int seed, int index_offset, float* out) {
+  return fe::run_tsne_from_knn<double>(indices, distances, false, init, has_init, n, k, n_components, perplexity,
+                                       early_iter, n_iter, early_exag, exag, lr, lr_auto, m0, m1, min_gain,
+                                       max_step, seed, index_offset, out);
+}
+
+int fastembedr_cuda_opentsne_fft_from_device_knn_float(const int* indices, const float* distances,
+                                                       const float* init, int has_init, int n, int k,
+                                                       int n_components, float perplexity, int early_iter,
+                                                       int n_iter, float early_exag, float exag, float lr,
+                                                       int lr_auto, float m0, float m1, float min_gain,
+                                                       float max_step, unsigned int seed, int index_offset,
+                                                       float* out) {
+  return fe::run_tsne_from_knn<float>(indices, distances, true, init, has_init, n, k, n_components, perplexity,
+                                      early_iter, n_iter, early_exag, exag, lr, lr_auto, m0, m1, min_gain, max_step,
+                                      seed, index_offset, out);
+}
+
+int fastembedr_cuda_tsne_affinities(const int* indices, const float* distances, int n, int k, float perplexity,
+                                    int index_offset, int* row_ptr, int* col, float* val, long long capacity,
+                                    long long* nnz, float* p_directed, double* entropy, double* total_mass) {
+  return fe::guarded([&] {
+    if (!indices || !distances || !row_ptr || !nnz) throw fe::Error("null CUDA t-SNE affinity pointer");
+    if (n < 2 || k < 1 || k > 1024 || !(perplexity > 0.0f)) throw fe::Error("invalid CUDA t-SNE affinity parameters");
+    fe::Stream st;
+    const std::size_t items = (std::size_t)n * k;
+    int* d_idx = nullptr;
+    float* d_dist = nullptr;
+    float* d_p = nullptr;
+    double* d_h = nullptr;
+    fe::Arena a;
+    a.reserve(&d_idx, items);
+    a.reserve(&d_dist, items);
+    a.reserve(&d_p, items);
+    a.reserve(&d_h, n);
+    a.commit("t-SNE affinity diagnostic");
+    FE_CUDA(cudaMemcpyAsync(d_idx, indices, sizeof(int) * items, cudaMemcpyHostToDevice, st.s));
+    FE_CUDA(cudaMemcpyAsync(d_dist, distances, sizeof(float) * items, cudaMemcpyHostToDevice, st.s));
+    fe::validate_knn(d_idx, d_dist, n, k, index_offset, st.s);
+    fe::row_probabilities(d_idx, d_dist, n, k, perplexity, d_p, d_h, st.s);
+    fe::DeviceCsr P;
+    fe::symmetrise(d_idx, d_p, n, k, index_offset, P, st.s);
+    *nnz = P.nnz;
+    if (total_mass) *total_mass = P.total_mass;
+    FE_CUDA(cudaMemcpyAsync(row_ptr, P.row_ptr, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, st.s));
+    if (col && val && P.nnz <= capacity) {
+      FE_CUDA(cudaMemcpyAsync(col, P.col, sizeof(int) * P.nnz, cudaMemcpyDeviceToHost, st.s));
+      FE_CUDA(cudaMemcpyAsync(val, P.val, sizeof(float) * P.nnz, cudaMemcpyDeviceToHost, st.s));
+    }
+    if (p_directed) FE_CUDA(cudaMemcpyAsync(p_directed, d_p, sizeof(float) * items, cudaMemcpyDeviceToHost, st.s));
+    if (entropy) FE_CUDA(cudaMemcpyAsync(entropy, d_h, sizeof(double) * n, cudaMemcpyDeviceToHost, st.s));
+    FE_CUDA(cudaStreamSynchronize(st.s));
+  });
+}
+
+int fastembedr_cuda_tsne_force_diagnostic(const int* indices, const float* distances, const float* layout, int n,
+                                          int k, float perplexity, float exaggeration, int grid_size,
+                                          int interpolation, int index_offset, float* attractive, float* repulsive,
+                                          double* z_grid, float* repulsive_exact, double* z_exact, double* kl) {
+  return fe::guarded([&] {
+    if (!indices || !distances || !layout || !attractive || !repulsive)
+      throw fe::Error("null CUDA t-SNE diagnostic pointer");
+    if (n < 2 || k < 1 || k > 1024 || !(perplexity > 0.0f) || !(exaggeration > 0.0f))
+      throw fe::Error("invalid CUDA t-SNE diagnostic parameters");
+    for (long long t = 0; t < 2LL * n; ++t)
+      if (!std::isfinite(layout[t])) throw fe::Error("`layout` must contain only finite coordinates.");
+    const int grid = grid_size > 0 ? grid_size : fe::cuda_fft_grid_size(n);
+    if (grid < 8 || grid > 2048 || (grid & (grid - 1)) != 0)
+      throw fe::Error("`grid_size` must be a power of two between 8 and 2048.");
+    fe::TsneJob job;
+    cudaStream_t s = job.stream.s;
+    const std::size_t items = (std::size_t)n * k;
+    int* d_idx = nullptr;
+    float* d_dist = nullptr;
+    float* d_y = nullptr;
+    float* d_attr = nullptr;
+    float* d_rep = nullptr;
+    double* d_rex = nullptr;
+    double* d_zrow = nullptr;
+    double* d_work = nullptr;
+    double* d_sc = nullptr;
+    fe::Arena a;
+    a.reserve(&d_idx, items);
+    a.reserve(&d_dist, items);
+    a.reserve(&d_y, 2 * (std::size_t)n);
+    a.reserve(&d_attr, 2 * (std::size_t)n);
+    a.reserve(&d_rep, 2 * (std::size_t)n);
+    a.reserve(&d_rex, 2 * (std::size_t)n);
+    a.reserve(&d_zrow, n);
+    a.reserve(&d_work, n);
+    a.reserve(&d_sc, 4);
+    a.commit("t-SNE force diagnostic");
+    FE_CUDA(cudaMemcpyAsync(d_idx, indices, sizeof(int) * items, cudaMemcpyHostToDevice, s));
+    FE_CUDA(cudaMemcpyAsync(d_dist, distances, sizeof(float) * items, cudaMemcpyHostToDevice, s));
+    FE_CUDA(cudaMemcpyAsync(d_y, layout, sizeof(float) * 2 * n, cudaMemcpyHostToDevice, s));
+    FE_CUDA(cudaStreamSynchronize(s));
+    job.prepare(d_idx, d_dist, layout, n, k, perplexity, index_offset, grid,
+                interpolation == 0 ? fe::kInterpBilinear : fe::kInterpLagrange3, 0u);
+    fe::tsne_forces(job.D, job.P, exaggeration, d_attr, d_rep, s);
+    FE_CUDA(cudaMemcpyAsync(attractive, d_attr, sizeof(float) * 2 * n, cudaMemcpyDeviceToHost, s));
+    FE_CUDA(cudaMemcpyAsync(repulsive, d_rep, sizeof(float) * 2 * n, cudaMemcpyDeviceToHost, s));
+    if (z_grid) FE_CUDA(cudaMemcpyAsync(z_grid, &job.D.cur->z, sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (repulsive_exact || z_exact) {
+      fe::exact_repulsion(d_y, n, d_rex, d_zrow, d_sc, s);
+      std::vector<double> rex(2 * (std::size_t)n);
+      double zt = 0.0;
+      FE_CUDA(cudaMemcpyAsync(rex.data(), d_rex, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, s));
+      FE_CUDA(cudaMemcpyAsync(&zt, d_sc, sizeof(double), cudaMemcpyDeviceToHost, s));
+      FE_CUDA(cudaStreamSynchronize(s));
+      if (repulsive_exact)
+        for (long long t = 0; t < 2LL * n; ++t) repulsive_exact[t] = (float)(rex[t] / zt);
+      if (z_exact) *z_exact = zt;
+    }
+    if (kl) {
+      fe::exact_kl(job.P, d_y, d_zrow, d_work, d_sc + 2, s);
+      FE_CUDA(cudaMemcpyAsync(kl, d_sc + 3, sizeof(double), cudaMemcpyDeviceToHost, s));
+    }
+    FE_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int fastembedr_tsne_plan_create(const int* indices, const float* distances, const float* init, int n, int k,
+                                float perplexity, int index_offset, int grid_size, int interpolation,
+                                unsigned int seed, fastembedr_tsne_plan** plan) {
+  return fe::guarded([&] {
+    if (!indices || !distances || !plan) throw fe::Error("null CUDA t-SNE plan pointer");
+    if (n < 2 || k < 1 || k > 1024 || !(perplexity > 0.0f)) throw fe::Error("invalid CUDA t-SNE plan parameters");
+    const int grid = grid_size > 0 ? grid_size : fe::cuda_fft_grid_size(n);
+    if (grid < 8 || grid > 2048 || (grid & (grid - 1)) != 0)
+      throw fe::Error("`grid_size` must be a power of two between 8 and 2048.");
+    auto p = std::make_unique<fastembedr_tsne_plan>();
+    p->job.prepare(indices, distances, init, n, k, perplexity, index_offset, grid,
+                   interpolation == 0 ? fe::kInterpBilinear : fe::kInterpLagrange3, seed);
+    *plan = p.release();
+  });
+}
+
+int fastembedr_tsne_plan_run(fastembedr_tsne_plan* plan, int iters, float exag, float lr, float mom, float min_gain,
+                             float max_step, int use_graph) {
+  return fe::guarded([&] {
+    if (!plan) throw fe::Error("null CUDA t-SNE plan");
+    plan->job.run(iters, exag, lr, mom, min_gain, max_step, use_graph != 0);
+  });
+}
+
+int fastembedr_tsne_plan_profile(fastembedr_tsne_plan* plan, int iters, float exag, float lr, float mom,
+                                 float min_gain, float max_step, float* ms_total, float* ms_step_kernel,
+                                 float* ms_grid_stage) {
+  return fe::guarded([&] {
+    if (!plan || iters < 1) throw fe::Error("invalid CUDA t-SNE profile request");
+    fe::TsneJob& J = plan->job;
+    cudaStream_t s = J.stream.s;
+    std::vector<cudaEvent_t> ev(3 * (std::size_t)iters);
+    for (auto& e : ev) FE_CUDA(cudaEventCreate(&e));
+    for (int it = 0; it < iters; ++it) {
+      FE_CUDA(cudaEventRecord(ev[3 * it], s));
+      fe::tsne_grid_stage(J.D, s);
+      FE_CUDA(cudaEventRecord(ev[3 * it + 1], s));
+      fe::tsne_step_stage(J.D, J.P, exag, lr, mom, min_gain, max_step, s);
+      FE_CUDA(cudaEventRecord(ev[3 * it + 2], s));
+    }
+    FE_CUDA(cudaStreamSynchronize(s));
+    float tot = 0.0f, stp = 0.0f, grd = 0.0f;
+    for (int it = 0; it < iters; ++it) {
+      float a = 0.0f, b = 0.0f;
+      FE_CUDA(cudaEventElapsedTime(&a, ev[3 * it], ev[3 * it + 1]));
+      FE_CUDA(cudaEventElapsedTime(&b, ev[3 * it + 1], ev[3 * it + 2]));
+      grd += a;
+      stp += b;
+    }
+    FE_CUDA(cudaEventElapsedTime(&tot, ev[0], ev[3 * (std::size_t)iters - 1]));
+    for (auto& e : ev) cudaEventDestroy(e);
+    if (ms_total) *ms_total = tot;
+    if (ms_step_kernel) *ms_step_kernel = stp;
+    if (ms_grid_stage) *ms_grid_stage = grd;
+  });
+}
+
+int fastembedr_tsne_plan_synchronize(fastembedr_tsne_plan* plan) {
+  return fe::guarded([&] {
+    if (!plan) throw fe::Error("null CUDA t-SNE plan");
+    FE_CUDA(cudaStreamSynchronize(plan->job.stream.s));
+  });
+}
+
+void* fastembedr_tsne_plan_stream(fastembedr_tsne_plan* plan) {
+  return plan ? static_cast<void*>(plan->job.stream.s) : nullptr;
+}
+
+int fastembedr_tsne_plan_layout(fastembedr_tsne_plan* plan, float* out) {
+  return fe::guarded([&] {
+    if (!plan || !out) throw fe::Error("null CUDA t-SNE plan or output");
+    plan->job.layout(out);
+  });
+}
+
+int fastembedr_tsne_plan_info(fastembedr_tsne_plan* plan, long long* nnz, int* grid_size, int* interpolation,
+                              int* launches) {
+  return fe::guarded([&] {
+    if (!plan) throw fe::Error("null CUDA t-SNE plan");
+    if (nnz) *nnz = plan->job.P.nnz;
+    if (grid_size) *grid_size = plan->job.D.grid;
+    if (interpolation) *interpolation = plan->job.D.mode;
+    if (launches) *launches = fe::tsne_launches_per_iteration();
+  });
+}
+
+int fastembedr_tsne_plan_kl(fastembedr_tsne_plan* plan, double* kl) {
+  return fe::guarded([&] {
+    if (!plan || !kl) throw fe::Error("null CUDA t-SNE plan or output");
+    fe::TsneJob& J = plan->job;
+    cudaStream_t s = J.stream.s;
+    const int n = J.D.n;
+    float* d_y = nullptr;
+    double* d_zrow = nullptr;
+    double* d_work = nullptr;
+    double* d_sc = nullptr;
+    fe::Arena a;
+    a.reserve(&d_y, 2 * (std::size_t)n);
+    a.reserve(&d_zrow, n);
+    a.reserve(&d_work, n);
+    a.reserve(&d_sc, 2);
+    a.commit("t-SNE KL");
+    fe::tsne_finalize(J.D, d_y, s);
+    fe::exact_kl(J.P, d_y, d_zrow, d_work, d_sc, s);
+    FE_CUDA(cudaMemcpyAsync(kl, d_sc + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
+    FE_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+void fastembedr_tsne_plan_destroy(fastembedr_tsne_plan* plan) { delete plan; }
+
+}  // extern "C"

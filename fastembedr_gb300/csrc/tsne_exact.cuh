@@ -1,0 +1,16 @@
+// Exact all-pairs t-SNE quantities (diagnostics, KL, the FP64-normalised exact repulsion).
+#pragma once
+
+#include "tsne.cuh"
+
+namespace fe {
+
+// d_rep (2n doubles): -sum_j q_ij^2 (y_i - y_j), not yet divided by Z; d_zrow (n): sum_j q_ij;
+// d_ztotal: sum over all ordered pairs i != j.
+void exact_repulsion(const float* d_y, int n, double* d_rep, double* d_zrow, double* d_ztotal, cudaStream_t s);
+
+// d_scalars[0] = all-pairs Z, d_scalars[1] = KL. d_zrow, d_work: n doubles each.
+void exact_kl(const DeviceCsr& P, const float* d_y, double* d_zrow, double* d_work, double* d_scalars,
+              cudaStream_t s);
+
+}  // namespace fe

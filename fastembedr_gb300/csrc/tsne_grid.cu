@@ -1,0 +1,713 @@
+// Per-iteration kernels of the t-SNE gradient loop on the GPU.
+//
+// Reference algorithm (fastEmbedR src/tsne_neighbors.cpp:1152-1260 on the CPU,
+// src/embedding_cuda_kernels.cpp:2472-2886 on CUDA): bound the layout by a square,
+// interpolate charges {1, x, y} onto a uniform grid, convolve with the kernels
+// q = 1/(1 + d^2) and q^2 by FFT on the zero-padded 2G x 2G torus, interpolate the potentials
+// back, combine with the sparse attractive term and apply the gains/momentum update.
+//
+// GB300 layout of one iteration (5 launches):
+//   1. scatter_kernel            points -> float4 charges (vector red to L2-resident grid)
+//   2. rows_forward_kernel       row FFTs of the charges (2 packed planes) and of the kernel
+//   3. columns_convolve_kernel   column FFT of kernel + charges, Z by Parseval, multiply,
+//                                inverse column FFT, all in shared memory
+//   4. rows_inverse_kernel       inverse row FFTs -> float4 potentials, Z finalised
+//   5. fused_step_kernel         warp-per-row CSR attractive force + potential gather +
+//                                gains/momentum/step clip + recentring; epilogue reduces the
+//                                new bounding box / mean into the next iteration's grid
+// Interpolation: the reference bilinear splat on G shared nodes, or (default) 3 equispaced
+// Lagrange nodes per box over floor(G / 3) boxes, as in FIt-SNE-style interpolation.
+#include <cfloat>
+#include <cmath>
+#include <vector>
+
+#include "tsne_grid.cuh"
+
+namespace fe {
+
+constexpr int kStepThreads = 256;
+constexpr int kFftThreads = 256;
+
+// ---------------------------------------------------------------- stencils
+template <int TAPS>
+struct Stencil {
+  int base;
+  float w[TAPS];
+};
+
+// Bilinear (TAPS = 2): bilinear_grid_value_t / the scatter of src/tsne_neighbors.cpp:1194-1213.
+// Lagrange (TAPS = 3): nodes at x0 + (3b + j + 0.5) h, j = 0..2, of box b.
+template <int TAPS>
+__device__ __forceinline__ Stencil<TAPS> make_stencil(float x, float x0, float inv_h, float inv_box, int nodes) {
+  Stencil<TAPS> s;
+  if constexpr (TAPS == 2) {
+    const float raw = (x - x0) * inv_h;
+    const float c = fmaxf(0.0f, fminf((float)(nodes - 1), raw));
+    int u0 = (int)floorf(c);
+    u0 = max(0, min(nodes - 2, u0));
+    const float f = c - (float)u0;
+    s.base = u0;
+    s.w[0] = 1.0f - f;
+    s.w[1] = f;
+  } else {
+    const int nbox = nodes / 3;
+    int b = (int)floorf((x - x0) * inv_box);
+    b = max(0, min(nbox - 1, b));
+    const float t = (x - x0) * inv_h - (float)(3 * b) - 0.5f;
+    s.base = 3 * b;
+    s.w[0] = 0.5f * (t - 1.0f) * (t - 2.0f);
+    s.w[1] = t * (2.0f - t);
+    s.w[2] = 0.5f * t * (t - 1.0f);
+  }
+  return s;
+}
+
+// ---------------------------------------------------------------- layout statistics
+// Fixed-order reduction of the per-block partials into the grid of the next iteration
+// (the bounding-square rule of src/tsne_neighbors.cpp:1168-1184).
+__device__ void finish_layout_stats(const StepPartial* __restrict__ part, int nblocks, int n, int grid, int mode,
+                                    GridState* __restrict__ next) {
+  __shared__ float s_min_x[kStepThreads], s_max_x[kStepThreads], s_min_y[kStepThreads], s_max_y[kStepThreads];
+  __shared__ double s_sx[kStepThreads], s_sy[kStepThreads];
+  float mnx = FLT_MAX, mxx = -FLT_MAX, mny = FLT_MAX, mxy = -FLT_MAX;
+  double sx = 0.0, sy = 0.0;
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+    const StepPartial p = part[b];
+    mnx = fminf(mnx, p.min_x);
+    mxx = fmaxf(mxx, p.max_x);
+    mny = fminf(mny, p.min_y);
+    mxy = fmaxf(mxy, p.max_y);
+    sx += p.sum_x;
+    sy += p.sum_y;
+  }
+  s_min_x[threadIdx.x] = mnx;
+  s_max_x[threadIdx.x] = mxx;
+  s_min_y[threadIdx.x] = mny;
+  s_max_y[threadIdx.x] = mxy;
+  s_sx[threadIdx.x] = sx;
+  s_sy[threadIdx.x] = sy;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      s_min_x[threadIdx.x] = fminf(s_min_x[threadIdx.x], s_min_x[threadIdx.x + w]);
+      s_max_x[threadIdx.x] = fmaxf(s_max_x[threadIdx.x], s_max_x[threadIdx.x + w]);
+      s_min_y[threadIdx.x] = fminf(s_min_y[threadIdx.x], s_min_y[threadIdx.x + w]);
+      s_max_y[threadIdx.x] = fmaxf(s_max_y[threadIdx.x], s_max_y[threadIdx.x + w]);
+      s_sx[threadIdx.x] += s_sx[threadIdx.x + w];
+      s_sy[threadIdx.x] += s_sy[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const float min_x = s_min_x[0], max_x = s_max_x[0], min_y = s_min_y[0], max_y = s_max_y[0];
+    GridState g;
+    g.cx = 0.5f * (min_x + max_x);
+    g.cy = 0.5f * (min_y + max_y);
+    float span = fmaxf(max_x - min_x, max_y - min_y);
+    if (!isfinite(span) || span <= 0.0f) span = 1.0f;
+    const float half = 0.55f * span + 1.0e-3f;
+    g.x0 = g.cx - half;
+    g.y0 = g.cy - half;
+    if (mode == kInterpBilinear) {
+      g.nodes = grid;
+      g.h = (2.0f * half) / (float)(grid - 1);
+      g.box = g.h;
+    } else {
+      const int nbox = grid / 3;
+      g.nodes = 3 * nbox;
+      g.box = (2.0f * half) / (float)nbox;
+      g.h = g.box / 3.0f;
+    }
+    g.inv_h = 1.0f / g.h;
+    g.inv_box = 1.0f / g.box;
+    g.mean_x = s_sx[0] / (double)n;
+    g.mean_y = s_sy[0] / (double)n;
+    g.z = 0.0;
+    g.inv_z = 0.0f;
+    *next = g;
+  }
+}
+
+__device__ __forceinline__ void block_partial(float mnx, float mxx, float mny, float mxy, double sx, double sy,
+                                              StepPartial* out) {
+  __shared__ StepPartial s_part[kStepThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  mnx = warp_min(mnx);
+  mxx = warp_max(mxx);
+  mny = warp_min(mny);
+  mxy = warp_max(mxy);
+  sx = warp_sum(sx);
+  sy = warp_sum(sy);
+  if (lane == 0) s_part[warp] = StepPartial{mnx, mxx, mny, mxy, sx, sy};
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    StepPartial p = s_part[0];
+    for (int w = 1; w < (int)(blockDim.x / 32); ++w) {
+      p.min_x = fminf(p.min_x, s_part[w].min_x);
+      p.max_x = fmaxf(p.max_x, s_part[w].max_x);
+      p.min_y = fminf(p.min_y, s_part[w].min_y);
+      p.max_y = fmaxf(p.max_y, s_part[w].max_y);
+      p.sum_x += s_part[w].sum_x;
+      p.sum_y += s_part[w].sum_y;
+    }
+    *out = p;
+  }
+}
+
+// Returns true in exactly one block: the last one to finish (counter reset for reuse).
+__device__ __forceinline__ bool last_block_done(unsigned* counter) {
+  __shared__ bool s_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned prev = atomicAdd(counter, 1u);
+    s_last = prev == gridDim.x - 1;
+    if (s_last) *counter = 0u;
+  }
+  __syncthreads();
+  if (s_last) __threadfence();
+  return s_last;
+}
+
+// Initial statistics of ynew (setup, and after an external layout write).
+__global__ void __launch_bounds__(kStepThreads)
+layout_stats_kernel(const float2* __restrict__ ynew, int n, int grid, int mode, StepPartial* __restrict__ part,
+                    unsigned* __restrict__ counter, GridState* __restrict__ next) {
+  float mnx = FLT_MAX, mxx = -FLT_MAX, mny = FLT_MAX, mxy = -FLT_MAX;
+  double sx = 0.0, sy = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float2 p = ynew[i];
+    mnx = fminf(mnx, p.x);
+    mxx = fmaxf(mxx, p.x);
+    mny = fminf(mny, p.y);
+    mxy = fmaxf(mxy, p.y);
+    sx += p.x;
+    sy += p.y;
+  }
+  block_partial(mnx, mxx, mny, mxy, sx, sy, part + blockIdx.x);
+  if (last_block_done(counter)) finish_layout_stats(part, gridDim.x, n, grid, mode, next);
+}
+
+// ---------------------------------------------------------------- scatter
+// Each point adds (w, w*(x - cx), w*(y - cy)) to its TAPS x TAPS stencil nodes. The layout the
+// gradient reads (y) is refreshed from the update's output (ynew) on the way.
+template <int TAPS>
+__global__ void __launch_bounds__(256)
+scatter_kernel(const float2* __restrict__ ynew, float2* __restrict__ y, int n, int grid,
+               GridState* __restrict__ cur, const GridState* __restrict__ next, float4* __restrict__ charges) {
+  const GridState g = *next;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *cur = g;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float2 p = ynew[i];
+    y[i] = p;
+    const Stencil<TAPS> sx = make_stencil<TAPS>(p.x, g.x0, g.inv_h, g.inv_box, g.nodes);
+    const Stencil<TAPS> sy = make_stencil<TAPS>(p.y, g.y0, g.inv_h, g.inv_box, g.nodes);
+    const float dx = p.x - g.cx, dy = p.y - g.cy;
+#pragma unroll
+    for (int a = 0; a < TAPS; ++a) {
+      float4* row = charges + (long long)(sy.base + a) * grid + sx.base;
+#pragma unroll
+      for (int b = 0; b < TAPS; ++b) {
+        const float w = sy.w[a] * sx.w[b];
+        atomicAdd(row + b, make_float4(w, w * dx, w * dy, 0.0f));
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------- shared-memory FFT
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ int bitrev(int i, int logm) { return (int)(__brev((unsigned)i) >> (32 - logm)); }
+
+// Radix-2 decimation in time over `count` sequences of length 2^logm at buf + s * 2^logm:
+// input in bit-reversed order, output in natural order. tw[t] = exp(-2 pi i t / 2^logm).
+__device__ void fft_dit(float2* buf, int count, int logm, const float2* __restrict__ tw, bool inverse) {
+  const int halfm = 1 << (logm - 1);
+  const int work = count * halfm;
+  for (int s = 0; s < logm; ++s) {
+    const int half = 1 << s;
+    const int shift = logm - 1 - s;
+    for (int t = threadIdx.x; t < work; t += blockDim.x) {
+      const int seq = t >> (logm - 1);
+      const int b = t & (halfm - 1);
+      const int j = b & (half - 1);
+      const int i0 = ((b >> s) << (s + 1)) + j;
+      float2* a = buf + (seq << logm);
+      float2 w = tw[j << shift];
+      if (inverse) w.y = -w.y;
+      const float2 u = a[i0];
+      const float2 v = cmul(a[i0 + half], w);
+      a[i0] = make_float2(u.x + v.x, u.y + v.y);
+      a[i0 + half] = make_float2(u.x - v.x, u.y - v.y);
+    }
+    __syncthreads();
+  }
+}
+
+// Radix-2 decimation in frequency: natural-order input, bit-reversed output.
+__device__ void fft_dif(float2* buf, int count, int logm, const float2* __restrict__ tw, bool inverse) {
+  const int halfm = 1 << (logm - 1);
+  const int work = count * halfm;
+  for (int s = logm - 1; s >= 0; --s) {
+    const int half = 1 << s;
+    const int shift = logm - 1 - s;
+    for (int t = threadIdx.x; t < work; t += blockDim.x) {
+      const int seq = t >> (logm - 1);
+      const int b = t & (halfm - 1);
+      const int j = b & (half - 1);
+      const int i0 = ((b >> s) << (s + 1)) + j;
+      float2* a = buf + (seq << logm);
+      float2 w = tw[j << shift];
+      if (inverse) w.y = -w.y;
+      const float2 u = a[i0];
+      const float2 v = a[i0 + half];
+      a[i0] = make_float2(u.x + v.x, u.y + v.y);
+      a[i0 + half] = cmul(make_float2(u.x - v.x, u.y - v.y), w);
+    }
+    __syncthreads();
+  }
+}
+
+// Row pass. Blocks [0, nodes): charge row r -> forward FFT of the two packed planes
+// A = (x-charge) + i (y-charge), B = mass (the charge row is cleared for the next scatter).
+// Blocks [nodes, 2 nodes): kernel row dy = r - nodes -> forward FFT of (q + i q^2); the
+// kernel is even in dx, so the transform is real-even and only M/2 + 1 entries are kept.
+__global__ void __launch_bounds__(kFftThreads)
+rows_forward_kernel(float4* __restrict__ charges, int grid, int nodes, int logm, const float2* __restrict__ tw,
+                    const GridState* __restrict__ cur, float2* __restrict__ rows, float2* __restrict__ krows) {
+  extern __shared__ float2 sbuf[];
+  const int m = 1 << logm;
+  const int r = blockIdx.x;
+  if (r < nodes) {
+    float4* crow = charges + (long long)r * grid;
+    for (int c = threadIdx.x; c < m; c += blockDim.x) {
+      float2 a = make_float2(0.0f, 0.0f), b = make_float2(0.0f, 0.0f);
+      if (c < nodes) {
+        const float4 q = crow[c];
+        crow[c] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        a = make_float2(q.y, q.z);
+        b = make_float2(q.x, 0.0f);
+      }
+      const int rc = bitrev(c, logm);
+      sbuf[rc] = a;
+      sbuf[m + rc] = b;
+    }
+    __syncthreads();
+    fft_dit(sbuf, 2, logm, tw, false);
+    float2* outa = rows + (long long)r * m;
+    float2* outb = rows + (long long)(nodes + r) * m;
+    for (int c = threadIdx.x; c < m; c += blockDim.x) {
+      outa[c] = sbuf[c];
+      outb[c] = sbuf[m + c];
+    }
+  } else {
+    const int kr = r - nodes;
+    const float h = cur->h;
+    const float yo = (float)kr * h;
+    for (int c = threadIdx.x; c < m; c += blockDim.x) {
+      const int dx = c < (m >> 1) ? c : c - m;
+      float2 v = make_float2(0.0f, 0.0f);
+      if (dx <= nodes - 1 && dx >= -(nodes - 1)) {
+        const float xo = (float)dx * h;
+        const float d2 = xo * xo + yo * yo;
+        const float q = 1.0f / (1.0f + d2);
+        v = make_float2(q, q * q);
+      }
+      sbuf[bitrev(c, logm)] = v;
+    }
+    __syncthreads();
+    fft_dit(sbuf, 1, logm, tw, false);
+    float2* out = krows + (long long)kr * ((m >> 1) + 1);
+    for (int c = threadIdx.x; c <= (m >> 1); c += blockDim.x) out[c] = sbuf[c];
+  }
+}
+
+// Column pass for `cc` adjacent columns: transform the kernel column (giving the real
+// spectra Kq + i Kq2) and the two charge planes, accumulate sum |F_mass|^2 Kq (Parseval form
+// of sum_nodes mass * (mass conv q), i.e. Z + n up to the 1/M^2 scale), multiply the charge
+// spectra by Kq2 and transform back. Only rows < nodes of the result are written.
+__global__ void __launch_bounds__(kFftThreads)
+columns_convolve_kernel(float2* __restrict__ rows, const float2* __restrict__ krows, int nodes, int logm, int cc,
+                        const float2* __restrict__ tw, double* __restrict__ zpart) {
+  extern __shared__ float2 sbuf[];  // [2 cc charge sequences][cc kernel sequences]
+  __shared__ double s_z[kFftThreads / 32];
+  const int m = 1 << logm;
+  const int half = m >> 1;
+  const int c0 = blockIdx.x * cc;
+  float2* kbuf = sbuf + (2 * cc << logm);
+  for (int t = threadIdx.x; t < cc * m; t += blockDim.x) {
+    const int j = t % cc, r = t / cc;
+    const int c = c0 + j;
+    const int rb = bitrev(r, logm);
+    float2 a = make_float2(0.0f, 0.0f), b = make_float2(0.0f, 0.0f);
+    if (r < nodes) {
+      a = rows[(long long)r * m + c];
+      b = rows[(long long)(nodes + r) * m + c];
+    }
+    sbuf[((2 * j) << logm) + rb] = a;
+    sbuf[((2 * j + 1) << logm) + rb] = b;
+    const int kc = c <= half ? c : m - c;
+    const int dy = r < half ? r : m - r;
+    kbuf[(j << logm) + rb] = dy <= nodes - 1 ? krows[(long long)dy * (half + 1) + kc] : make_float2(0.0f, 0.0f);
+  }
+  __syncthreads();
+  fft_dit(sbuf, 3 * cc, logm, tw, false);
+  double zl = 0.0;
+  for (int t = threadIdx.x; t < cc * m; t += blockDim.x) {
+    const int j = t / m, kr = t % m;
+    const float2 kk = kbuf[(j << logm) + kr];
+    float2& a = sbuf[((2 * j) << logm) + kr];
+    float2& b = sbuf[((2 * j + 1) << logm) + kr];
+    zl += ((double)b.x * b.x + (double)b.y * b.y) * (double)kk.x;
+    a.x *= kk.y;
+    a.y *= kk.y;
+    b.x *= kk.y;
+    b.y *= kk.y;
+  }
+  __syncthreads();
+  fft_dif(sbuf, 2 * cc, logm, tw, true);
+  for (int t = threadIdx.x; t < cc * nodes; t += blockDim.x) {
+    const int j = t % cc, r = t / cc;
+    const int c = c0 + j;
+    const int rb = bitrev(r, logm);
+    rows[(long long)r * m + c] = sbuf[((2 * j) << logm) + rb];
+    rows[(long long)(nodes + r) * m + c] = sbuf[((2 * j + 1) << logm) + rb];
+  }
+  zl = warp_sum(zl);
+  if ((threadIdx.x & 31) == 0) s_z[threadIdx.x >> 5] = zl;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double z = 0.0;
+    for (int w = 0; w < (int)(blockDim.x / 32); ++w) z += s_z[w];
+    zpart[blockIdx.x] = z;
+  }
+}
+
+// Inverse row pass -> potentials (phi_q2, phi_x, phi_y) per node; block 0 also finalises
+// Z = sum_k |F_mass|^2 Kq / M^2 - n (the reference's sum_i q_grid(y_i) - n).
+__global__ void __launch_bounds__(kFftThreads)
+rows_inverse_kernel(const float2* __restrict__ rows, int grid, int nodes, int logm, const float2* __restrict__ tw,
+                    const double* __restrict__ zpart, int zblocks, int n, GridState* __restrict__ cur,
+                    float4* __restrict__ potential) {
+  extern __shared__ float2 sbuf[];
+  const int m = 1 << logm;
+  const int r = blockIdx.x;
+  const float2* ina = rows + (long long)r * m;
+  const float2* inb = rows + (long long)(nodes + r) * m;
+  for (int c = threadIdx.x; c < m; c += blockDim.x) {
+    sbuf[c] = ina[c];
+    sbuf[m + c] = inb[c];
+  }
+  __syncthreads();
+  fft_dif(sbuf, 2, logm, tw, true);
+  const float scale = 1.0f / ((float)m * (float)m);
+  float4* out = potential + (long long)r * grid;
+  for (int c = threadIdx.x; c < nodes; c += blockDim.x) {
+    const int cb = bitrev(c, logm);
+    const float2 a = sbuf[cb], b = sbuf[m + cb];
+    out[c] = make_float4(b.x * scale, a.x * scale, a.y * scale, 0.0f);
+  }
+  if (r == 0) {
+    __shared__ double s_z[kFftThreads];
+    double z = 0.0;
+    for (int b = threadIdx.x; b < zblocks; b += blockDim.x) z += zpart[b];
+    s_z[threadIdx.x] = z;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+      if ((int)threadIdx.x < w) s_z[threadIdx.x] += s_z[threadIdx.x + w];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      const double zz = s_z[0] / ((double)m * (double)m) - (double)n;
+      cur->z = zz;
+      cur->inv_z = (float)(1.0 / fmax(zz, (double)FLT_MIN));
+    }
+  }
+}
+
+// ---------------------------------------------------------------- fused step
+template <int TAPS>
+__device__ __forceinline__ float pick(const float (&w)[TAPS], int a) {
+  float v = w[0];
+#pragma unroll
+  for (int t = 1; t < TAPS; ++t) v = a == t ? w[t] : v;
+  return v;
+}
+
+__device__ __forceinline__ int sign3(float v) { return (v > 0.0f) - (v < 0.0f); }
+
+// One warp per CSR row (rows strided over a persistent grid).
+//   attractive: g_i += exag * p_ij * q_ij * (y_i - y_j), q = 1 / (1 + d^2)
+//               (add_sparse_attractive_gradient_f, src/tsne_neighbors.cpp:1061-1088),
+//               compensated (Kahan) per lane on rows longer than 256 entries;
+//   repulsive:  -((y_i - c) phi_q2 - phi_xy) / Z from the interpolated potentials
+//               (src/tsne_neighbors.cpp:1247-1258);
+//   update:     gains / momentum / step clip of apply_open_tsne_update_f
+//               (src/tsne_neighbors.cpp:1297-1336), then the recentring of zero_mean_f
+//               (:1280-1291) folded in by subtracting the previous mean.
+// The epilogue reduces bounding box and mean of the new layout into `next`.
+// DIAG = true writes the two force parts instead of updating.
+template <int TAPS, bool DIAG>
+__global__ void __launch_bounds__(kStepThreads)
+fused_step_kernel(const int* __restrict__ row_ptr, const int* __restrict__ col, const float* __restrict__ val,
+                  const float2* __restrict__ y, float2* __restrict__ ynew, float2* __restrict__ gains,
+                  float2* __restrict__ update, const float4* __restrict__ pot, int grid, int n,
+                  const GridState* __restrict__ cur, GridState* __restrict__ next, StepPartial* __restrict__ part,
+                  unsigned* __restrict__ counter, int mode, float exag, float lr, float mom, float min_gain,
+                  float max_step, float2* __restrict__ out_attr, float2* __restrict__ out_rep) {
+  const GridState g = *cur;
+  const int lane = threadIdx.x & 31;
+  const int warps_total = gridDim.x * (blockDim.x >> 5);
+  const bool clip = isfinite(max_step) && max_step > 0.0f;
+  const float max2 = max_step * max_step;
+  float mnx = FLT_MAX, mxx = -FLT_MAX, mny = FLT_MAX, mxy = -FLT_MAX;
+  double sx = 0.0, sy = 0.0;
+  for (int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps_total) {
+    const int b = row_ptr[i], e = row_ptr[i + 1];
+    const float2 yi = y[i];
+    float ax = 0.0f, ay = 0.0f;
+    if (e - b <= 256) {
+      for (int p = b + lane; p < e; p += 128) {
+        int ci[4];
+        float v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int q = p + 32 * u;
+          ci[u] = q < e ? __ldg(col + q) : i;
+          v[u] = q < e ? __ldg(val + q) : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const float2 yj = y[ci[u]];
+          const float dx = yi.x - yj.x, dy = yi.y - yj.y;
+          const float q = 1.0f / (1.0f + (dx * dx + dy * dy));
+          const float c = exag * v[u] * q;
+          ax += c * dx;
+          ay += c * dy;
+        }
+      }
+    } else {
+      float kx = 0.0f, ky = 0.0f;
+      for (int p = b + lane; p < e; p += 32) {
+        const int j = __ldg(col + p);
+        const float pv = __ldg(val + p);
+        const float2 yj = y[j];
+        const float dx = yi.x - yj.x, dy = yi.y - yj.y;
+        const float q = 1.0f / (1.0f + (dx * dx + dy * dy));
+        const float c = exag * pv * q;
+        const float tx = c * dx - kx, ty = c * dy - ky;
+        const float nx = ax + tx, ny = ay + ty;
+        kx = (nx - ax) - tx;
+        ky = (ny - ay) - ty;
+        ax = nx;
+        ay = ny;
+      }
+    }
+    const Stencil<TAPS> stx = make_stencil<TAPS>(yi.x, g.x0, g.inv_h, g.inv_box, g.nodes);
+    const Stencil<TAPS> sty = make_stencil<TAPS>(yi.y, g.y0, g.inv_h, g.inv_box, g.nodes);
+    float r0 = 0.0f, r1 = 0.0f, r2 = 0.0f;
+    if (lane < TAPS * TAPS) {
+      const int a = lane / TAPS, bb = lane - a * TAPS;
+      const float w = pick<TAPS>(sty.w, a) * pick<TAPS>(stx.w, bb);
+      const float4 f = __ldg(pot + (long long)(sty.base + a) * grid + stx.base + bb);
+      r0 = w * f.x;
+      r1 = w * f.y;
+      r2 = w * f.z;
+    }
+    ax = warp_sum(ax);
+    ay = warp_sum(ay);
+    r0 = warp_sum(r0);
+    r1 = warp_sum(r1);
+    r2 = warp_sum(r2);
+    if (lane == 0) {
+      const float dxc = yi.x - g.cx, dyc = yi.y - g.cy;
+      const float repx = -(dxc * r0 - r1) * g.inv_z;
+      const float repy = -(dyc * r0 - r2) * g.inv_z;
+      if constexpr (DIAG) {
+        out_attr[i] = make_float2(ax, ay);
+        out_rep[i] = make_float2(repx, repy);
+      } else {
+        const float gx = repx + ax, gy = repy + ay;
+        const float2 ga = gains[i], up = update[i];
+        float gnx = sign3(up.x) != sign3(gx) ? ga.x + 0.2f : ga.x * 0.8f + min_gain;
+        float gny = sign3(up.y) != sign3(gy) ? ga.y + 0.2f : ga.y * 0.8f + min_gain;
+        if (gnx < min_gain) gnx = min_gain;
+        if (gny < min_gain) gny = min_gain;
+        float ux = mom * up.x - lr * gnx * gx;
+        float uy = mom * up.y - lr * gny * gy;
+        const float s2 = ux * ux + uy * uy;
+        if (clip && s2 > max2) {
+          const float sc = max_step / sqrtf(fmaxf(s2, FLT_MIN));
+          ux *= sc;
+          uy *= sc;
+        }
+        const float nx = (yi.x - (float)g.mean_x) + ux;
+        const float ny = (yi.y - (float)g.mean_y) + uy;
+        gains[i] = make_float2(gnx, gny);
+        update[i] = make_float2(ux, uy);
+        ynew[i] = make_float2(nx, ny);
+        mnx = fminf(mnx, nx);
+        mxx = fmaxf(mxx, nx);
+        mny = fminf(mny, ny);
+        mxy = fmaxf(mxy, ny);
+        sx += nx;
+        sy += ny;
+      }
+    }
+  }
+  if constexpr (!DIAG) {
+    block_partial(mnx, mxx, mny, mxy, sx, sy, part + blockIdx.x);
+    if (last_block_done(counter)) finish_layout_stats(part, gridDim.x, n, grid, mode, next);
+  }
+}
+
+__global__ void fill_state_kernel(float2* __restrict__ gains, float2* __restrict__ update, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    gains[i] = make_float2(1.0f, 1.0f);
+    update[i] = make_float2(0.0f, 0.0f);
+  }
+}
+
+__global__ void finalize_kernel(const float2* __restrict__ ynew, const GridState* __restrict__ next, int n,
+                                float2* __restrict__ out) {
+  const float mx = (float)next->mean_x, my = (float)next->mean_y;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float2 p = ynew[i];
+    out[i] = make_float2(p.x - mx, p.y - my);
+  }
+}
+
+// ---------------------------------------------------------------- host side
+namespace {
+int point_blocks(int n) { return std::max(1, std::min(ceil_div(n, 256), sm_count() * 8)); }
+
+template <typename K>
+int persistent_blocks(K kernel, int threads, int n_warps_needed) {
+  int per_sm = 0;
+  FE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0));
+  per_sm = std::max(1, per_sm);
+  return std::max(1, std::min(per_sm * sm_count(), ceil_div(n_warps_needed, threads / 32)));
+}
+}  // namespace
+
+void tsne_device_alloc(TsneDevice& d, int n, int grid, int mode) {
+  d.n = n;
+  d.grid = grid;
+  d.fft = 2 * grid;
+  d.log_fft = 0;
+  while ((1 << d.log_fft) < d.fft) ++d.log_fft;
+  d.mode = mode;
+  d.nodes = mode == kInterpBilinear ? grid : 3 * (grid / 3);
+  const int m = d.fft;
+  d.cols_per_block = m >= 512 ? 2 : 1;
+  d.col_blocks = m / d.cols_per_block;
+  d.step_blocks = mode == kInterpBilinear
+                      ? persistent_blocks(fused_step_kernel<2, false>, kStepThreads, n)
+                      : persistent_blocks(fused_step_kernel<3, false>, kStepThreads, n);
+  const int nparts = std::max(d.step_blocks, point_blocks(n));
+  d.arena.release();
+  d.arena.reserve(&d.y, n);
+  d.arena.reserve(&d.ynew, n);
+  d.arena.reserve(&d.gains, n);
+  d.arena.reserve(&d.update, n);
+  d.arena.reserve(&d.charges, (std::size_t)grid * grid);
+  d.arena.reserve(&d.rows, (std::size_t)2 * d.nodes * m);
+  d.arena.reserve(&d.krows, (std::size_t)d.nodes * (m / 2 + 1));
+  d.arena.reserve(&d.potential, (std::size_t)grid * grid);
+  d.arena.reserve(&d.twiddle, m / 2);
+  d.arena.reserve(&d.zpart, d.col_blocks);
+  d.arena.reserve(&d.cur, 1);
+  d.arena.reserve(&d.next, 1);
+  d.arena.reserve(&d.partial, nparts);
+  d.arena.reserve(&d.counter, 1);
+  d.arena.commit("t-SNE optimizer state");
+  std::vector<float2> tw(m / 2);
+  for (int t = 0; t < m / 2; ++t) {
+    const double a = -2.0 * M_PI * (double)t / (double)m;
+    tw[t] = make_float2((float)std::cos(a), (float)std::sin(a));
+  }
+  FE_CUDA(cudaMemcpy(d.twiddle, tw.data(), sizeof(float2) * tw.size(), cudaMemcpyHostToDevice));
+  FE_CUDA(cudaMemset(d.charges, 0, sizeof(float4) * (std::size_t)grid * grid));
+  FE_CUDA(cudaMemset(d.potential, 0, sizeof(float4) * (std::size_t)grid * grid));
+  FE_CUDA(cudaMemset(d.counter, 0, sizeof(unsigned)));
+  FE_CUDA(cudaMemset(d.cur, 0, sizeof(GridState)));
+  const int big = 3 * d.cols_per_block * m * (int)sizeof(float2);
+  FE_CUDA(cudaFuncSetAttribute(columns_convolve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  const int rowb = 2 * m * (int)sizeof(float2);
+  FE_CUDA(cudaFuncSetAttribute(rows_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, rowb));
+  FE_CUDA(cudaFuncSetAttribute(rows_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, rowb));
+}
+
+void tsne_device_init(TsneDevice& d, const float* d_init, cudaStream_t s) {
+  FE_CUDA(cudaMemcpyAsync(d.ynew, d_init, sizeof(float2) * d.n, cudaMemcpyDeviceToDevice, s));
+  fill_state_kernel<<<point_blocks(d.n), 256, 0, s>>>(d.gains, d.update, d.n);
+  FE_LAUNCH("fill_state_kernel");
+  layout_stats_kernel<<<point_blocks(d.n), kStepThreads, 0, s>>>(d.ynew, d.n, d.grid, d.mode, d.partial, d.counter,
+                                                                  d.next);
+  FE_LAUNCH("layout_stats_kernel");
+}
+
+void tsne_grid_stage(TsneDevice& d, cudaStream_t s) {
+  const int m = d.fft;
+  if (d.mode == kInterpBilinear)
+    scatter_kernel<2><<<point_blocks(d.n), 256, 0, s>>>(d.ynew, d.y, d.n, d.grid, d.cur, d.next, d.charges);
+  else
+    scatter_kernel<3><<<point_blocks(d.n), 256, 0, s>>>(d.ynew, d.y, d.n, d.grid, d.cur, d.next, d.charges);
+  FE_LAUNCH("scatter_kernel");
+  rows_forward_kernel<<<2 * d.nodes, kFftThreads, 2 * m * sizeof(float2), s>>>(d.charges, d.grid, d.nodes,
+                                                                                d.log_fft, d.twiddle, d.cur,
+                                                                                d.rows, d.krows);
+  FE_LAUNCH("rows_forward_kernel");
+  columns_convolve_kernel<<<d.col_blocks, kFftThreads, 3 * d.cols_per_block * m * sizeof(float2), s>>>(
+      d.rows, d.krows, d.nodes, d.log_fft, d.cols_per_block, d.twiddle, d.zpart);
+  FE_LAUNCH("columns_convolve_kernel");
+  rows_inverse_kernel<<<d.nodes, kFftThreads, 2 * m * sizeof(float2), s>>>(d.rows, d.grid, d.nodes, d.log_fft,
+                                                                            d.twiddle, d.zpart, d.col_blocks, d.n,
+                                                                            d.cur, d.potential);
+  FE_LAUNCH("rows_inverse_kernel");
+}
+
+void tsne_iteration(TsneDevice& d, const DeviceCsr& P, float exag, float lr, float mom, float min_gain,
+                    float max_step, cudaStream_t s) {
+  tsne_grid_stage(d, s);
+  tsne_step_stage(d, P, exag, lr, mom, min_gain, max_step, s);
+}
+
+void tsne_step_stage(TsneDevice& d, const DeviceCsr& P, float exag, float lr, float mom, float min_gain,
+                     float max_step, cudaStream_t s) {
+  if (d.mode == kInterpBilinear)
+    fused_step_kernel<2, false><<<d.step_blocks, kStepThreads, 0, s>>>(
+        P.row_ptr, P.col, P.val, d.y, d.ynew, d.gains, d.update, d.potential, d.grid, d.n, d.cur, d.next,
+        d.partial, d.counter, d.mode, exag, lr, mom, min_gain, max_step, nullptr, nullptr);
+  else
+    fused_step_kernel<3, false><<<d.step_blocks, kStepThreads, 0, s>>>(
+        P.row_ptr, P.col, P.val, d.y, d.ynew, d.gains, d.update, d.potential, d.grid, d.n, d.cur, d.next,
+        d.partial, d.counter, d.mode, exag, lr, mom, min_gain, max_step, nullptr, nullptr);
+  FE_LAUNCH("fused_step_kernel");
+}
+
+void tsne_forces(TsneDevice& d, const DeviceCsr& P, float exag, float* d_attr, float* d_rep, cudaStream_t s) {
+  tsne_grid_stage(d, s);
+  float2* a = reinterpret_cast<float2*>(d_attr);
+  float2* r = reinterpret_cast<float2*>(d_rep);
+  if (d.mode == kInterpBilinear)
+    fused_step_kernel<2, true><<<d.step_blocks, kStepThreads, 0, s>>>(
+        P.row_ptr, P.col, P.val, d.y, d.ynew, d.gains, d.update, d.potential, d.grid, d.n, d.cur, d.next,
+        d.partial, d.counter, d.mode, exag, 0.0f, 0.0f, 0.0f, 0.0f, a, r);
+  else
+    fused_step_kernel<3, true><<<d.step_blocks, kStepThreads, 0, s>>>(
+        P.row_ptr, P.col, P.val, d.y, d.ynew, d.gains, d.update, d.potential, d.grid, d.n, d.cur, d.next,
+        d.partial, d.counter, d.mode, exag, 0.0f, 0.0f, 0.0f, 0.0f, a, r);
+  FE_LAUNCH("fused_step_kernel(diagnostic)");
+}
+
+void tsne_finalize(TsneDevice& d, float* d_out, cudaStream_t s) {
+  finalize_kernel<<<point_blocks(d.n), 256, 0, s>>>(d.ynew, d.next, d.n, reinterpret_cast<float2*>(d_out));
+  FE_LAUNCH("finalize_kernel");
+}
+
+int tsne_launches_per_iteration() { return 5; }
+
+}  // namespace fe

@@ -1,0 +1,125 @@
+/*
+ * fastEmbedR GB300 embedding optimizer: C ABI.
+ *
+ * Drop-in replacement for the extern "C" layer of fastEmbedR
+ * src/embedding_cuda_kernels.cpp that src/embedding_cuda_impl.cpp calls. Same names,
+ * argument order and meaning; same status convention: every int-returning entry point
+ * returns 0 on success and 1 on failure, and the message of the last failure on the calling
+ * thread is returned by fastembedr_cuda_embedding_last_error().
+ *
+ * Layouts (as in the reference):
+ *   - KNN indices / distances: column-major n x k (element (i, j) at j * n + i), as R stores
+ *     matrices; indices carry `index_offset` (0- or 1-based).
+ *   - init / out layouts: row-major interleaved (x, y) floats, n * 2 values.
+ * Host pointers unless the name says device. Entry points are synchronous: when they return,
+ * outputs are written and all device memory they allocated is released.
+ */
+#ifndef FASTEMBEDR_CUDA_H
+#define FASTEMBEDR_CUDA_H
+
+#include <stdbool.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- runtime */
+
+/* replaces fastembedr_cuda_available, src/embedding_cuda_kernels.cpp:3833-3841 */
+bool fastembedr_cuda_available(void);
+
+/* replaces fastembedr_cuda_embedding_last_error, src/embedding_cuda_kernels.cpp:3829-3831 */
+const char* fastembedr_cuda_embedding_last_error(void);
+
+/* replaces fastembedr_cuda_opentsne_fft_grid_size, src/embedding_cuda_kernels.cpp:5625-5627:
+ * grid nodes per side, 256 (n < 20k) / 512 / 1024 (n >= 100k), FASTEMBEDR_TSNE_FFT_GRID override */
+int fastembedr_cuda_opentsne_fft_grid_size(int n);
+
+/* ---------------------------------------------------------------- t-SNE from KNN */
+
+/* replaces fastembedr_cuda_opentsne_fft_from_knn_float, src/embedding_cuda_kernels.cpp:6207-6234.
+ * Perplexity affinities, symmetrised CSR P, then early_exaggeration_iter + n_iter iterations of
+ * the gains/momentum optimizer with FFT-grid repulsion. learning_rate_auto: lr = n / exaggeration
+ * of each phase. max_step_norm <= 0 or non-finite disables the step clip. has_init = 0 draws a
+ * seeded N(0, 1e-4^2) layout. Repulsion interpolation: FASTEMBEDR_TSNE_INTERPOLATION=bilinear
+ * selects the reference stencil, otherwise 3-node Lagrange boxes. */
+int fastembedr_cuda_opentsne_fft_from_knn_float(const int* indices, const float* distances, const float* init,
+                                                int has_init, int n, int k, int n_components, float perplexity,
+                                                int early_exaggeration_iter, int n_iter, float early_exaggeration,
+                                                float exaggeration, float learning_rate, int learning_rate_auto,
+                                                float initial_momentum, float final_momentum, float min_gain,
+                                                float max_step_norm, unsigned int seed, int index_offset,
+                                                float* out);
+
+/* replaces fastembedr_cuda_opentsne_fft_from_knn (double distances), src/embedding_cuda_kernels.cpp:6178-6205 */
+int fastembedr_cuda_opentsne_fft_from_knn(const int* indices, const double* distances, const float* init,
+                                          int has_init, int n, int k, int n_components, float perplexity,
+                                          int early_exaggeration_iter, int n_iter, float early_exaggeration,
+                                          float exaggeration, float learning_rate, int learning_rate_auto,
+                                          float initial_momentum, float final_momentum, float min_gain,
+                                          float max_step_norm, unsigned int seed, int index_offset, float* out);
+
+/* replaces fastembedr_cuda_opentsne_fft_from_device_knn_float, src/embedding_cuda_kernels.cpp:6236-6263:
+ * indices / distances are device pointers (column-major), init and out are host pointers. */
+int fastembedr_cuda_opentsne_fft_from_device_knn_float(const int* indices, const float* distances,
+                                                       const float* init, int has_init, int n, int k,
+                                                       int n_components, float perplexity,
+                                                       int early_exaggeration_iter, int n_iter,
+                                                       float early_exaggeration, float exaggeration,
+                                                       float learning_rate, int learning_rate_auto,
+                                                       float initial_momentum, float final_momentum,
+                                                       float min_gain, float max_step_norm, unsigned int seed,
+                                                       int index_offset, float* out);
+
+/* ---------------------------------------------------------------- t-SNE diagnostics */
+
+/* GPU twin of the affinity part of opentsne_force_diagnostic_cpp
+ * (src/tsne_neighbors.cpp:1698-1817; build_tsne_probabilities_float :616-724).
+ * Writes the symmetrised CSR (row_ptr n + 1, col / val up to `capacity`), its size in *nnz and
+ * the directed-mass total; p_directed (row-major n x k) and entropy (n) may be NULL. */
+int fastembedr_cuda_tsne_affinities(const int* indices, const float* distances, int n, int k, float perplexity,
+                                    int index_offset, int* row_ptr, int* col, float* val, long long capacity,
+                                    long long* nnz, float* p_directed, double* entropy, double* total_mass);
+
+/* GPU twin of the force part of opentsne_force_diagnostic_cpp (src/tsne_neighbors.cpp:1698-1817):
+ * on `layout` (row-major n x 2) computes the attractive force (exaggeration-scaled), the grid
+ * repulsion with grid_size nodes per side (interpolation 0 = bilinear, 1 = Lagrange; grid_size
+ * <= 0 uses the CUDA policy) and its Z; optionally (repulsive_exact != NULL) the exact
+ * repulsion with the all-pairs Z, and the KL (kl != NULL). */
+int fastembedr_cuda_tsne_force_diagnostic(const int* indices, const float* distances, const float* layout,
+                                          int n, int k, float perplexity, float exaggeration, int grid_size,
+                                          int interpolation, int index_offset, float* attractive,
+                                          float* repulsive, double* z_grid, float* repulsive_exact,
+                                          double* z_exact, double* kl);
+
+/* ---------------------------------------------------------------- resident t-SNE plan
+ * No reference counterpart: the reference rebuilds everything per call. A plan keeps P, the
+ * layout and the optimizer state resident in HBM so iterations can be timed and driven in
+ * chunks (each chunk is one CUDA graph launch). */
+typedef struct fastembedr_tsne_plan fastembedr_tsne_plan;
+
+/* indices / distances: device pointers (column-major n x k); init: host row-major n x 2 or NULL. */
+int fastembedr_tsne_plan_create(const int* indices, const float* distances, const float* init, int n, int k,
+                                float perplexity, int index_offset, int grid_size, int interpolation,
+                                unsigned int seed, fastembedr_tsne_plan** plan);
+/* enqueue `iters` iterations on the plan's stream (CUDA graph when use_graph != 0) */
+int fastembedr_tsne_plan_run(fastembedr_tsne_plan* plan, int iters, float exaggeration, float learning_rate,
+                             float momentum, float min_gain, float max_step_norm, int use_graph);
+/* run `iters` iterations eagerly and report device time: total, and the fused step kernel alone */
+int fastembedr_tsne_plan_profile(fastembedr_tsne_plan* plan, int iters, float exaggeration, float learning_rate,
+                                 float momentum, float min_gain, float max_step_norm, float* ms_total,
+                                 float* ms_step_kernel, float* ms_grid_stage);
+int fastembedr_tsne_plan_synchronize(fastembedr_tsne_plan* plan);
+/* the plan's cudaStream_t, for callers that time with their own events */
+void* fastembedr_tsne_plan_stream(fastembedr_tsne_plan* plan);
+int fastembedr_tsne_plan_layout(fastembedr_tsne_plan* plan, float* out);
+int fastembedr_tsne_plan_info(fastembedr_tsne_plan* plan, long long* nnz, int* grid_size, int* interpolation,
+                              int* launches_per_iteration);
+/* exact KL of the current layout (all-pairs Z on the GPU) */
+int fastembedr_tsne_plan_kl(fastembedr_tsne_plan* plan, double* kl);
+void fastembedr_tsne_plan_destroy(fastembedr_tsne_plan* plan);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,58 @@
+"""CPU-side checks of the boundary: the library loads without a GPU, exports every symbol that
+include/fastembedr_cuda.h declares, and reports the absence of a device through the reference's
+error convention (no compute is attempted without a GPU)."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from fastembedr_gb300 import _lib, api
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    syms = set()
+    for name in os.listdir(os.path.join(ROOT, "include")):
+        if name.endswith(".h"):
+            text = open(os.path.join(ROOT, "include", name)).read()
+            text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+            syms |= set(re.findall(r"\b(fastembedr_\w+)\s*\(", text))
+    return syms
+
+
+def test_header_declares_the_reference_abi():
+    syms = declared_symbols()
+    for ref in ("fastembedr_cuda_available", "fastembedr_cuda_embedding_last_error",
+                "fastembedr_cuda_opentsne_fft_grid_size", "fastembedr_cuda_opentsne_fft_from_knn_float",
+                "fastembedr_cuda_opentsne_fft_from_knn", "fastembedr_cuda_opentsne_fft_from_device_knn_float"):
+        assert ref in syms
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _lib.load()
+    for s in sorted(declared_symbols()):
+        assert hasattr(lib, s), s
+
+
+def test_grid_policy_matches_reference_cuda(monkeypatch):
+    lib = _lib.load()
+    monkeypatch.delenv("FASTEMBEDR_TSNE_FFT_GRID", raising=False)
+    assert [lib.fastembedr_cuda_opentsne_fft_grid_size(n) for n in (1000, 19999, 20000, 99999, 100000, 10**6)] == \
+        [256, 256, 512, 512, 1024, 1024]
+
+
+def test_no_device_is_an_error_not_a_fallback():
+    lib = _lib.load()
+    if lib.fastembedr_cuda_available():
+        pytest.skip("a CUDA device is present")
+    idx = np.array([[2, 3], [1, 3], [1, 2]], np.int32)
+    dist = np.ones((3, 2), np.float32)
+    with pytest.raises(_lib.CudaEmbeddingError):
+        api.tsne_knn(idx, dist, perplexity=0.5, n_iter=1, early_exaggeration_iter=0)
+
+
+def test_index_offset_detection():
+    assert api.knn_index_offset(np.array([[2, 3], [1, 3], [1, 2]])) == 1
+    assert api.knn_index_offset(np.array([[1, 2], [0, 2], [0, 1]])) == 0
