@@ -129,8 +129,8 @@ def tsne_affinities(indices, distances, perplexity, index_offset=None):
     nnz = C.c_longlong()
     tot = C.c_double()
     lib = _lib.require_gpu()
-    st = lib.fastembedr_cuda_tsne_affinities(_colmajor(idx, np.int32).ctypes.data,
-                                             _colmajor(distances, np.float32).ctypes.data, n, k, float(perplexity),
+    idx_cm, dist_cm = _colmajor(idx, np.int32), _colmajor(distances, np.float32)  # kept alive across the call
+    st = lib.fastembedr_cuda_tsne_affinities(idx_cm.ctypes.data, dist_cm.ctypes.data, n, k, float(perplexity),
                                              off, rp.ctypes.data, col.ctypes.data, val.ctypes.data, cap,
                                              C.byref(nnz), p.ctypes.data, h.ctypes.data, C.byref(tot))
     _lib.check(st, "CUDA t-SNE affinities")
@@ -150,8 +150,9 @@ def tsne_force_diagnostic(indices, distances, layout, perplexity, exaggeration=1
     rex = np.zeros((n, 2), np.float32) if exact else None
     zg, ze, kv = C.c_double(), C.c_double(), C.c_double()
     lib = _lib.require_gpu()
+    idx_cm, dist_cm = _colmajor(idx, np.int32), _colmajor(distances, np.float32)  # kept alive across the call
     st = lib.fastembedr_cuda_tsne_force_diagnostic(
-        _colmajor(idx, np.int32).ctypes.data, _colmajor(distances, np.float32).ctypes.data, y.ctypes.data, n, k,
+        idx_cm.ctypes.data, dist_cm.ctypes.data, y.ctypes.data, n, k,
         float(perplexity), float(exaggeration), int(grid_size), int(interpolation), off, att.ctypes.data,
         rep.ctypes.data, C.byref(zg), rex.ctypes.data if exact else None, C.byref(ze) if exact else None,
         C.byref(kv) if kl else None)
@@ -195,7 +196,7 @@ class TsnePlan:
                                                          float(learning_rate), float(momentum), float(min_gain),
                                                          float(max_step_norm), C.byref(tot), C.byref(stp),
                                                          C.byref(grd)), "t-SNE plan profile")
-        return dict(total_ms=tot.value, step_kernel_ms=stp.value, grid_stage_ms=grd.value)
+        return dict(total_ms=tot.value, attractive_kernel_ms=stp.value, grid_stage_ms=grd.value)
 
     def synchronize(self):
         _lib.check(self.lib.fastembedr_tsne_plan_synchronize(self.h), "t-SNE plan synchronize")

@@ -191,8 +191,9 @@ int run_tsne_from_knn(const int* indices, const DistT* distances, bool on_device
       FE_LAUNCH("double_to_float_kernel");
       dist_ptr = d_dist;
     }
-    job->prepare(idx_ptr, dist_ptr, has_init ? init : nullptr, n, k, perplexity, offset, cuda_fft_grid_size(n),
-                 interp_mode_from_env(), seed);
+    const int mode = interp_mode_from_env();
+    job->prepare(idx_ptr, dist_ptr, has_init ? init : nullptr, n, k, perplexity, offset, default_grid_size(n, mode),
+                 mode, seed);
     in.release();
     job->schedule(early_iter, n_iter, early_exag, exag, lr, lr_auto, m0, m1, min_gain, max_step);
     job->layout(out);
@@ -218,7 +219,7 @@ bool fastembedr_cuda_available(void) {
 
 const char* fastembedr_cuda_embedding_last_error(void) { return fe::last_error(); }
 
-int fastembedr_cuda_opentsne_fft_grid_size(int n) { return fe::cuda_fft_grid_size(n); }
+int fastembedr_cuda_opentsne_fft_grid_size(int n) { return fe::default_grid_size(n, fe::interp_mode_from_env()); }
 
 int fastembedr_cuda_opentsne_fft_from_knn_float(const int* indices, const float* distances, const float* init,
                                                 int has_init, int n, int k, int n_components, float perplexity,
@@ -300,7 +301,8 @@ int fastembedr_cuda_tsne_force_diagnostic(const int* indices, const float* dista
       throw fe::Error("invalid CUDA t-SNE diagnostic parameters");
     for (long long t = 0; t < 2LL * n; ++t)
       if (!std::isfinite(layout[t])) throw fe::Error("`layout` must contain only finite coordinates.");
-    const int grid = grid_size > 0 ? grid_size : fe::cuda_fft_grid_size(n);
+    const int mode = interpolation == 0 ? fe::kInterpBilinear : fe::kInterpLagrange3;
+    const int grid = grid_size > 0 ? grid_size : fe::default_grid_size(n, mode);
     if (grid < 8 || grid > 2048 || (grid & (grid - 1)) != 0)
       throw fe::Error("`grid_size` must be a power of two between 8 and 2048.");
     fe::TsneJob job;
@@ -330,8 +332,7 @@ int fastembedr_cuda_tsne_force_diagnostic(const int* indices, const float* dista
     FE_CUDA(cudaMemcpyAsync(d_dist, distances, sizeof(float) * items, cudaMemcpyHostToDevice, s));
     FE_CUDA(cudaMemcpyAsync(d_y, layout, sizeof(float) * 2 * n, cudaMemcpyHostToDevice, s));
     FE_CUDA(cudaStreamSynchronize(s));
-    job.prepare(d_idx, d_dist, layout, n, k, perplexity, index_offset, grid,
-                interpolation == 0 ? fe::kInterpBilinear : fe::kInterpLagrange3, 0u);
+    job.prepare(d_idx, d_dist, layout, n, k, perplexity, index_offset, grid, mode, 0u);
     fe::tsne_forces(job.D, job.P, exaggeration, d_attr, d_rep, s);
     FE_CUDA(cudaMemcpyAsync(attractive, d_attr, sizeof(float) * 2 * n, cudaMemcpyDeviceToHost, s));
     FE_CUDA(cudaMemcpyAsync(repulsive, d_rep, sizeof(float) * 2 * n, cudaMemcpyDeviceToHost, s));
@@ -361,12 +362,12 @@ int fastembedr_tsne_plan_create(const int* indices, const float* distances, cons
   return fe::guarded([&] {
     if (!indices || !distances || !plan) throw fe::Error("null CUDA t-SNE plan pointer");
     if (n < 2 || k < 1 || k > 1024 || !(perplexity > 0.0f)) throw fe::Error("invalid CUDA t-SNE plan parameters");
-    const int grid = grid_size > 0 ? grid_size : fe::cuda_fft_grid_size(n);
+    const int mode = interpolation == 0 ? fe::kInterpBilinear : fe::kInterpLagrange3;
+    const int grid = grid_size > 0 ? grid_size : fe::default_grid_size(n, mode);
     if (grid < 8 || grid > 2048 || (grid & (grid - 1)) != 0)
       throw fe::Error("`grid_size` must be a power of two between 8 and 2048.");
     auto p = std::make_unique<fastembedr_tsne_plan>();
-    p->job.prepare(indices, distances, init, n, k, perplexity, index_offset, grid,
-                   interpolation == 0 ? fe::kInterpBilinear : fe::kInterpLagrange3, seed);
+    p->job.prepare(indices, distances, init, n, k, perplexity, index_offset, grid, mode, seed);
     *plan = p.release();
   });
 }
@@ -386,25 +387,27 @@ int fastembedr_tsne_plan_profile(fastembedr_tsne_plan* plan, int iters, float ex
     if (!plan || iters < 1) throw fe::Error("invalid CUDA t-SNE profile request");
     fe::TsneJob& J = plan->job;
     cudaStream_t s = J.stream.s;
-    std::vector<cudaEvent_t> ev(3 * (std::size_t)iters);
+    std::vector<cudaEvent_t> ev(4 * (std::size_t)iters);
     for (auto& e : ev) FE_CUDA(cudaEventCreate(&e));
     for (int it = 0; it < iters; ++it) {
-      FE_CUDA(cudaEventRecord(ev[3 * it], s));
+      FE_CUDA(cudaEventRecord(ev[4 * it], s));
+      fe::tsne_attractive_stage(J.D, J.P, exag, s);
+      FE_CUDA(cudaEventRecord(ev[4 * it + 1], s));
       fe::tsne_grid_stage(J.D, s);
-      FE_CUDA(cudaEventRecord(ev[3 * it + 1], s));
-      fe::tsne_step_stage(J.D, J.P, exag, lr, mom, min_gain, max_step, s);
-      FE_CUDA(cudaEventRecord(ev[3 * it + 2], s));
+      FE_CUDA(cudaEventRecord(ev[4 * it + 2], s));
+      fe::tsne_update_stage(J.D, lr, mom, min_gain, max_step, s);
+      FE_CUDA(cudaEventRecord(ev[4 * it + 3], s));
     }
     FE_CUDA(cudaStreamSynchronize(s));
     float tot = 0.0f, stp = 0.0f, grd = 0.0f;
     for (int it = 0; it < iters; ++it) {
       float a = 0.0f, b = 0.0f;
-      FE_CUDA(cudaEventElapsedTime(&a, ev[3 * it], ev[3 * it + 1]));
-      FE_CUDA(cudaEventElapsedTime(&b, ev[3 * it + 1], ev[3 * it + 2]));
-      grd += a;
-      stp += b;
+      FE_CUDA(cudaEventElapsedTime(&a, ev[4 * it], ev[4 * it + 1]));
+      FE_CUDA(cudaEventElapsedTime(&b, ev[4 * it + 1], ev[4 * it + 2]));
+      stp += a;
+      grd += b;
     }
-    FE_CUDA(cudaEventElapsedTime(&tot, ev[0], ev[3 * (std::size_t)iters - 1]));
+    FE_CUDA(cudaEventElapsedTime(&tot, ev[0], ev[4 * (std::size_t)iters - 1]));
     for (auto& e : ev) cudaEventDestroy(e);
     if (ms_total) *ms_total = tot;
     if (ms_step_kernel) *ms_step_kernel = stp;

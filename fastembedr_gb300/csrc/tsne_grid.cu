@@ -6,15 +6,17 @@
 // q = 1/(1 + d^2) and q^2 by FFT on the zero-padded 2G x 2G torus, interpolate the potentials
 // back, combine with the sparse attractive term and apply the gains/momentum update.
 //
-// GB300 layout of one iteration (5 launches):
-//   1. scatter_kernel            points -> float4 charges (vector red to L2-resident grid)
-//   2. rows_forward_kernel       row FFTs of the charges (2 packed planes) and of the kernel
-//   3. columns_convolve_kernel   column FFT of kernel + charges, Z by Parseval, multiply,
-//                                inverse column FFT, all in shared memory
-//   4. rows_inverse_kernel       inverse row FFTs -> float4 potentials, Z finalised
-//   5. fused_step_kernel         warp-per-row CSR attractive force + potential gather +
-//                                gains/momentum/step clip + recentring; epilogue reduces the
-//                                new bounding box / mean into the next iteration's grid
+// GB300 layout of one iteration (6 launches, two streams, captured in a CUDA graph):
+//   side stream:  attractive_kernel        warp-per-row CSR attractive force (HBM stream of P)
+//   main stream:  scatter_kernel           points -> float4 charges (vector red, L2-resident grid)
+//                 rows_forward_kernel      row FFTs of the charges (2 packed planes) and kernel
+//                 columns_convolve_kernel  column FFTs of kernel + charges, Z by Parseval,
+//                                          multiply, inverse column FFT, all in shared memory
+//                 rows_inverse_kernel      inverse row FFTs -> float4 potentials, Z finalised
+//   join:         update_kernel            potential gather + gains/momentum/step clip +
+//                                          recentring; epilogue reduces the new bounding box and
+//                                          mean into the next iteration's grid
+// The attractive pass (bandwidth-bound) overlaps the grid stage (latency/shared-memory bound).
 // Interpolation: the reference bilinear splat on G shared nodes, or (default) 3 equispaced
 // Lagrange nodes per box over floor(G / 3) boxes, as in FIt-SNE-style interpolation.
 #include <cfloat>
@@ -189,17 +191,16 @@ layout_stats_kernel(const float2* __restrict__ ynew, int n, int grid, int mode, 
 }
 
 // ---------------------------------------------------------------- scatter
-// Each point adds (w, w*(x - cx), w*(y - cy)) to its TAPS x TAPS stencil nodes. The layout the
-// gradient reads (y) is refreshed from the update's output (ynew) on the way.
+// Each point adds (w, w*(x - cx), w*(y - cy)) to its TAPS x TAPS stencil nodes; block 0 also
+// promotes the grid computed by the previous update (`next`) to `cur`.
 template <int TAPS>
 __global__ void __launch_bounds__(256)
-scatter_kernel(const float2* __restrict__ ynew, float2* __restrict__ y, int n, int grid,
-               GridState* __restrict__ cur, const GridState* __restrict__ next, float4* __restrict__ charges) {
+scatter_kernel(const float2* __restrict__ y, int n, int grid, GridState* __restrict__ cur,
+               const GridState* __restrict__ next, float4* __restrict__ charges) {
   const GridState g = *next;
   if (blockIdx.x == 0 && threadIdx.x == 0) *cur = g;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const float2 p = ynew[i];
-    y[i] = p;
+    const float2 p = y[i];
     const Stencil<TAPS> sx = make_stencil<TAPS>(p.x, g.x0, g.inv_h, g.inv_box, g.nodes);
     const Stencil<TAPS> sy = make_stencil<TAPS>(p.y, g.y0, g.inv_h, g.inv_box, g.nodes);
     const float dx = p.x - g.cx, dy = p.y - g.cy;
@@ -221,52 +222,104 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
 }
 __device__ __forceinline__ int bitrev(int i, int logm) { return (int)(__brev((unsigned)i) >> (32 - logm)); }
 
-// Radix-2 decimation in time over `count` sequences of length 2^logm at buf + s * 2^logm:
-// input in bit-reversed order, output in natural order. tw[t] = exp(-2 pi i t / 2^logm).
-__device__ void fft_dit(float2* buf, int count, int logm, const float2* __restrict__ tw, bool inverse) {
-  const int halfm = 1 << (logm - 1);
-  const int work = count * halfm;
-  for (int s = 0; s < logm; ++s) {
-    const int half = 1 << s;
-    const int shift = logm - 1 - s;
-    for (int t = threadIdx.x; t < work; t += blockDim.x) {
-      const int seq = t >> (logm - 1);
-      const int b = t & (halfm - 1);
-      const int j = b & (half - 1);
-      const int i0 = ((b >> s) << (s + 1)) + j;
-      float2* a = buf + (seq << logm);
-      float2 w = tw[j << shift];
-      if (inverse) w.y = -w.y;
-      const float2 u = a[i0];
-      const float2 v = cmul(a[i0 + half], w);
-      a[i0] = make_float2(u.x + v.x, u.y + v.y);
-      a[i0 + half] = make_float2(u.x - v.x, u.y - v.y);
+// Radix-2 FFTs over `count` sequences of length M = 2^logm stored at buf + seq * M, with R
+// consecutive radix-2 stages fused per shared-memory pass (R <= 3): each work item keeps the
+// 2^R elements i0 + t * 2^s of one butterfly group in registers. tw[t] = exp(-2 pi i t / M).
+__device__ __forceinline__ float2 twiddle(const float2* __restrict__ tw, int x, int shift, bool inverse) {
+  float2 w = tw[x << shift];
+  if (inverse) w.y = -w.y;
+  return w;
+}
+
+// Decimation in time: stages s .. s + R - 1 (input of the FFT in bit-reversed order).
+template <int R>
+__device__ __forceinline__ void dit_pass(float2* buf, int count, int logm, int s, const float2* __restrict__ tw,
+                                         bool inverse) {
+  constexpr int E = 1 << R;
+  const int h = 1 << s;
+  const int items = count << (logm - R);
+  for (int t = threadIdx.x; t < items; t += blockDim.x) {
+    const int seq = t >> (logm - R);
+    const int rem = t & ((1 << (logm - R)) - 1);
+    const int j = rem & (h - 1);
+    const int i0 = ((rem >> s) << (s + R)) + j;
+    float2* a = buf + (seq << logm) + i0;
+    float2 v[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) v[e] = a[e * h];
+#pragma unroll
+    for (int st = 0; st < R; ++st) {
+      const int span = 1 << st;            // partner distance in units of h
+      const int shift = logm - 1 - (s + st);  // twiddle stride for block length 2^(s+st+1)
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        if (e & span) continue;
+        const float2 w = twiddle(tw, j + (e & (span - 1)) * h, shift, inverse);
+        const float2 x = cmul(v[e + span], w);
+        const float2 u = v[e];
+        v[e] = make_float2(u.x + x.x, u.y + x.y);
+        v[e + span] = make_float2(u.x - x.x, u.y - x.y);
+      }
     }
-    __syncthreads();
+#pragma unroll
+    for (int e = 0; e < E; ++e) a[e * h] = v[e];
   }
 }
 
-// Radix-2 decimation in frequency: natural-order input, bit-reversed output.
-__device__ void fft_dif(float2* buf, int count, int logm, const float2* __restrict__ tw, bool inverse) {
-  const int halfm = 1 << (logm - 1);
-  const int work = count * halfm;
-  for (int s = logm - 1; s >= 0; --s) {
-    const int half = 1 << s;
-    const int shift = logm - 1 - s;
-    for (int t = threadIdx.x; t < work; t += blockDim.x) {
-      const int seq = t >> (logm - 1);
-      const int b = t & (halfm - 1);
-      const int j = b & (half - 1);
-      const int i0 = ((b >> s) << (s + 1)) + j;
-      float2* a = buf + (seq << logm);
-      float2 w = tw[j << shift];
-      if (inverse) w.y = -w.y;
-      const float2 u = a[i0];
-      const float2 v = a[i0 + half];
-      a[i0] = make_float2(u.x + v.x, u.y + v.y);
-      a[i0 + half] = cmul(make_float2(u.x - v.x, u.y - v.y), w);
+// Decimation in frequency: stages s + R - 1 down to s (output in bit-reversed order).
+template <int R>
+__device__ __forceinline__ void dif_pass(float2* buf, int count, int logm, int s, const float2* __restrict__ tw,
+                                         bool inverse) {
+  constexpr int E = 1 << R;
+  const int h = 1 << s;
+  const int items = count << (logm - R);
+  for (int t = threadIdx.x; t < items; t += blockDim.x) {
+    const int seq = t >> (logm - R);
+    const int rem = t & ((1 << (logm - R)) - 1);
+    const int j = rem & (h - 1);
+    const int i0 = ((rem >> s) << (s + R)) + j;
+    float2* a = buf + (seq << logm) + i0;
+    float2 v[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) v[e] = a[e * h];
+#pragma unroll
+    for (int st = R - 1; st >= 0; --st) {
+      const int span = 1 << st;
+      const int shift = logm - 1 - (s + st);
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        if (e & span) continue;
+        const float2 w = twiddle(tw, j + (e & (span - 1)) * h, shift, inverse);
+        const float2 u = v[e], x = v[e + span];
+        v[e] = make_float2(u.x + x.x, u.y + x.y);
+        v[e + span] = cmul(make_float2(u.x - x.x, u.y - x.y), w);
+      }
     }
+#pragma unroll
+    for (int e = 0; e < E; ++e) a[e * h] = v[e];
+  }
+}
+
+__device__ void fft_dit(float2* buf, int count, int logm, const float2* __restrict__ tw, bool inverse) {
+  for (int s = 0; s < logm;) {
+    const int r = min(3, logm - s);
+    if (r == 3) dit_pass<3>(buf, count, logm, s, tw, inverse);
+    else if (r == 2) dit_pass<2>(buf, count, logm, s, tw, inverse);
+    else dit_pass<1>(buf, count, logm, s, tw, inverse);
     __syncthreads();
+    s += r;
+  }
+}
+
+__device__ void fft_dif(float2* buf, int count, int logm, const float2* __restrict__ tw, bool inverse) {
+  for (int top = logm - 1; top >= 0;) {
+    const int r = min(3, top + 1);
+    const int s = top - r + 1;
+    if (r == 3) dif_pass<3>(buf, count, logm, s, tw, inverse);
+    else if (r == 2) dif_pass<2>(buf, count, logm, s, tw, inverse);
+    else dif_pass<1>(buf, count, logm, s, tw, inverse);
+    __syncthreads();
+    top = s - 1;
   }
 }
 
@@ -427,46 +480,22 @@ rows_inverse_kernel(const float2* __restrict__ rows, int grid, int nodes, int lo
   }
 }
 
-// ---------------------------------------------------------------- fused step
-template <int TAPS>
-__device__ __forceinline__ float pick(const float (&w)[TAPS], int a) {
-  float v = w[0];
-#pragma unroll
-  for (int t = 1; t < TAPS; ++t) v = a == t ? w[t] : v;
-  return v;
-}
+// ---------------------------------------------------------------- attractive pass
+// One warp per CSR row, rows strided over a persistent grid:
+//   a_i = exag * sum_j p_ij q_ij (y_i - y_j), q = 1 / (1 + d^2)
+// (add_sparse_attractive_gradient_f, src/tsne_neighbors.cpp:1061-1088). Column / value loads
+// are streaming (coalesced, not kept in L1); the y gathers hit the L2-resident layout. Rows
+// longer than 256 entries accumulate with per-lane compensated (Kahan) sums.
+constexpr int kAttrThreads = 256;
 
-__device__ __forceinline__ int sign3(float v) { return (v > 0.0f) - (v < 0.0f); }
-
-// One warp per CSR row (rows strided over a persistent grid).
-//   attractive: g_i += exag * p_ij * q_ij * (y_i - y_j), q = 1 / (1 + d^2)
-//               (add_sparse_attractive_gradient_f, src/tsne_neighbors.cpp:1061-1088),
-//               compensated (Kahan) per lane on rows longer than 256 entries;
-//   repulsive:  -((y_i - c) phi_q2 - phi_xy) / Z from the interpolated potentials
-//               (src/tsne_neighbors.cpp:1247-1258);
-//   update:     gains / momentum / step clip of apply_open_tsne_update_f
-//               (src/tsne_neighbors.cpp:1297-1336), then the recentring of zero_mean_f
-//               (:1280-1291) folded in by subtracting the previous mean.
-// The epilogue reduces bounding box and mean of the new layout into `next`.
-// DIAG = true writes the two force parts instead of updating.
-template <int TAPS, bool DIAG>
-__global__ void __launch_bounds__(kStepThreads)
-fused_step_kernel(const int* __restrict__ row_ptr, const int* __restrict__ col, const float* __restrict__ val,
-                  const float2* __restrict__ y, float2* __restrict__ ynew, float2* __restrict__ gains,
-                  float2* __restrict__ update, const float4* __restrict__ pot, int grid, int n,
-                  const GridState* __restrict__ cur, GridState* __restrict__ next, StepPartial* __restrict__ part,
-                  unsigned* __restrict__ counter, int mode, float exag, float lr, float mom, float min_gain,
-                  float max_step, float2* __restrict__ out_attr, float2* __restrict__ out_rep) {
-  const GridState g = *cur;
+__global__ void __launch_bounds__(kAttrThreads)
+attractive_kernel(const int* __restrict__ row_ptr, const int* __restrict__ col, const float* __restrict__ val,
+                  const float2* __restrict__ y, int n, float exag, float2* __restrict__ attr) {
   const int lane = threadIdx.x & 31;
   const int warps_total = gridDim.x * (blockDim.x >> 5);
-  const bool clip = isfinite(max_step) && max_step > 0.0f;
-  const float max2 = max_step * max_step;
-  float mnx = FLT_MAX, mxx = -FLT_MAX, mny = FLT_MAX, mxy = -FLT_MAX;
-  double sx = 0.0, sy = 0.0;
   for (int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps_total) {
-    const int b = row_ptr[i], e = row_ptr[i + 1];
-    const float2 yi = y[i];
+    const int b = __ldg(row_ptr + i), e = __ldg(row_ptr + i + 1);
+    const float2 yi = __ldg(y + i);
     float ax = 0.0f, ay = 0.0f;
     if (e - b <= 256) {
       for (int p = b + lane; p < e; p += 128) {
@@ -475,12 +504,12 @@ fused_step_kernel(const int* __restrict__ row_ptr, const int* __restrict__ col, 
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
           const int q = p + 32 * u;
-          ci[u] = q < e ? __ldg(col + q) : i;
-          v[u] = q < e ? __ldg(val + q) : 0.0f;
+          ci[u] = q < e ? __ldcs(col + q) : i;
+          v[u] = q < e ? __ldcs(val + q) : 0.0f;
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-          const float2 yj = y[ci[u]];
+          const float2 yj = __ldg(y + ci[u]);
           const float dx = yi.x - yj.x, dy = yi.y - yj.y;
           const float q = 1.0f / (1.0f + (dx * dx + dy * dy));
           const float c = exag * v[u] * q;
@@ -491,9 +520,9 @@ fused_step_kernel(const int* __restrict__ row_ptr, const int* __restrict__ col, 
     } else {
       float kx = 0.0f, ky = 0.0f;
       for (int p = b + lane; p < e; p += 32) {
-        const int j = __ldg(col + p);
-        const float pv = __ldg(val + p);
-        const float2 yj = y[j];
+        const int j = __ldcs(col + p);
+        const float pv = __ldcs(val + p);
+        const float2 yj = __ldg(y + j);
         const float dx = yi.x - yj.x, dy = yi.y - yj.y;
         const float q = 1.0f / (1.0f + (dx * dx + dy * dy));
         const float c = exag * pv * q;
@@ -505,56 +534,89 @@ fused_step_kernel(const int* __restrict__ row_ptr, const int* __restrict__ col, 
         ay = ny;
       }
     }
-    const Stencil<TAPS> stx = make_stencil<TAPS>(yi.x, g.x0, g.inv_h, g.inv_box, g.nodes);
-    const Stencil<TAPS> sty = make_stencil<TAPS>(yi.y, g.y0, g.inv_h, g.inv_box, g.nodes);
-    float r0 = 0.0f, r1 = 0.0f, r2 = 0.0f;
-    if (lane < TAPS * TAPS) {
-      const int a = lane / TAPS, bb = lane - a * TAPS;
-      const float w = pick<TAPS>(sty.w, a) * pick<TAPS>(stx.w, bb);
-      const float4 f = __ldg(pot + (long long)(sty.base + a) * grid + stx.base + bb);
-      r0 = w * f.x;
-      r1 = w * f.y;
-      r2 = w * f.z;
-    }
     ax = warp_sum(ax);
     ay = warp_sum(ay);
-    r0 = warp_sum(r0);
-    r1 = warp_sum(r1);
-    r2 = warp_sum(r2);
-    if (lane == 0) {
-      const float dxc = yi.x - g.cx, dyc = yi.y - g.cy;
-      const float repx = -(dxc * r0 - r1) * g.inv_z;
-      const float repy = -(dyc * r0 - r2) * g.inv_z;
-      if constexpr (DIAG) {
-        out_attr[i] = make_float2(ax, ay);
-        out_rep[i] = make_float2(repx, repy);
-      } else {
-        const float gx = repx + ax, gy = repy + ay;
-        const float2 ga = gains[i], up = update[i];
-        float gnx = sign3(up.x) != sign3(gx) ? ga.x + 0.2f : ga.x * 0.8f + min_gain;
-        float gny = sign3(up.y) != sign3(gy) ? ga.y + 0.2f : ga.y * 0.8f + min_gain;
-        if (gnx < min_gain) gnx = min_gain;
-        if (gny < min_gain) gny = min_gain;
-        float ux = mom * up.x - lr * gnx * gx;
-        float uy = mom * up.y - lr * gny * gy;
-        const float s2 = ux * ux + uy * uy;
-        if (clip && s2 > max2) {
-          const float sc = max_step / sqrtf(fmaxf(s2, FLT_MIN));
-          ux *= sc;
-          uy *= sc;
-        }
-        const float nx = (yi.x - (float)g.mean_x) + ux;
-        const float ny = (yi.y - (float)g.mean_y) + uy;
-        gains[i] = make_float2(gnx, gny);
-        update[i] = make_float2(ux, uy);
-        ynew[i] = make_float2(nx, ny);
-        mnx = fminf(mnx, nx);
-        mxx = fmaxf(mxx, nx);
-        mny = fminf(mny, ny);
-        mxy = fmaxf(mxy, ny);
-        sx += nx;
-        sy += ny;
+    if (lane == 0) attr[i] = make_float2(ax, ay);
+  }
+}
+
+// ---------------------------------------------------------------- update
+template <int TAPS>
+__device__ __forceinline__ float pick(const float (&w)[TAPS], int a) {
+  float v = w[0];
+#pragma unroll
+  for (int t = 1; t < TAPS; ++t) v = a == t ? w[t] : v;
+  return v;
+}
+
+__device__ __forceinline__ int sign3(float v) { return (v > 0.0f) - (v < 0.0f); }
+
+// One thread per point: interpolate the potentials, form the gradient
+//   g_i = a_i - ((y_i - c) phi_q2 - phi_xy) / Z     (src/tsne_neighbors.cpp:1247-1259)
+// and apply gains / momentum / step clip (apply_open_tsne_update_f, :1297-1336) with the
+// recentring of zero_mean_f (:1280-1291) folded in by subtracting the previous mean. The
+// epilogue reduces bounding box and mean of the new layout into `next`. DIAG writes the
+// repulsive force instead of updating.
+template <int TAPS, bool DIAG>
+__global__ void __launch_bounds__(kStepThreads)
+update_kernel(float2* __restrict__ y, const float2* __restrict__ attr, float2* __restrict__ gains,
+              float2* __restrict__ update, const float4* __restrict__ pot, int grid, int n,
+              const GridState* __restrict__ cur, GridState* __restrict__ next, StepPartial* __restrict__ part,
+              unsigned* __restrict__ counter, int mode, float lr, float mom, float min_gain, float max_step,
+              float2* __restrict__ out_rep) {
+  const GridState g = *cur;
+  const bool clip = isfinite(max_step) && max_step > 0.0f;
+  const float max2 = max_step * max_step;
+  float mnx = FLT_MAX, mxx = -FLT_MAX, mny = FLT_MAX, mxy = -FLT_MAX;
+  double sx = 0.0, sy = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float2 p = y[i];
+    const Stencil<TAPS> stx = make_stencil<TAPS>(p.x, g.x0, g.inv_h, g.inv_box, g.nodes);
+    const Stencil<TAPS> sty = make_stencil<TAPS>(p.y, g.y0, g.inv_h, g.inv_box, g.nodes);
+    float r0 = 0.0f, r1 = 0.0f, r2 = 0.0f;
+#pragma unroll
+    for (int a = 0; a < TAPS; ++a) {
+      const float4* row = pot + (long long)(sty.base + a) * grid + stx.base;
+#pragma unroll
+      for (int b = 0; b < TAPS; ++b) {
+        const float w = sty.w[a] * stx.w[b];
+        const float4 f = __ldg(row + b);
+        r0 += w * f.x;
+        r1 += w * f.y;
+        r2 += w * f.z;
       }
+    }
+    const float repx = -((p.x - g.cx) * r0 - r1) * g.inv_z;
+    const float repy = -((p.y - g.cy) * r0 - r2) * g.inv_z;
+    if constexpr (DIAG) {
+      out_rep[i] = make_float2(repx, repy);
+    } else {
+      const float2 a = attr[i];
+      const float gx = repx + a.x, gy = repy + a.y;
+      const float2 ga = gains[i], up = update[i];
+      float gnx = sign3(up.x) != sign3(gx) ? ga.x + 0.2f : ga.x * 0.8f + min_gain;
+      float gny = sign3(up.y) != sign3(gy) ? ga.y + 0.2f : ga.y * 0.8f + min_gain;
+      if (gnx < min_gain) gnx = min_gain;
+      if (gny < min_gain) gny = min_gain;
+      float ux = mom * up.x - lr * gnx * gx;
+      float uy = mom * up.y - lr * gny * gy;
+      const float s2 = ux * ux + uy * uy;
+      if (clip && s2 > max2) {
+        const float sc = max_step / sqrtf(fmaxf(s2, FLT_MIN));
+        ux *= sc;
+        uy *= sc;
+      }
+      const float nx = (p.x - (float)g.mean_x) + ux;
+      const float ny = (p.y - (float)g.mean_y) + uy;
+      gains[i] = make_float2(gnx, gny);
+      update[i] = make_float2(ux, uy);
+      y[i] = make_float2(nx, ny);
+      mnx = fminf(mnx, nx);
+      mxx = fmaxf(mxx, nx);
+      mny = fminf(mny, ny);
+      mxy = fmaxf(mxy, ny);
+      sx += nx;
+      sy += ny;
     }
   }
   if constexpr (!DIAG) {
@@ -570,11 +632,11 @@ __global__ void fill_state_kernel(float2* __restrict__ gains, float2* __restrict
   }
 }
 
-__global__ void finalize_kernel(const float2* __restrict__ ynew, const GridState* __restrict__ next, int n,
+__global__ void finalize_kernel(const float2* __restrict__ y, const GridState* __restrict__ next, int n,
                                 float2* __restrict__ out) {
   const float mx = (float)next->mean_x, my = (float)next->mean_y;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const float2 p = ynew[i];
+    const float2 p = y[i];
     out[i] = make_float2(p.x - mx, p.y - my);
   }
 }
@@ -584,13 +646,27 @@ namespace {
 int point_blocks(int n) { return std::max(1, std::min(ceil_div(n, 256), sm_count() * 8)); }
 
 template <typename K>
-int persistent_blocks(K kernel, int threads, int n_warps_needed) {
+int persistent_blocks(K kernel, int threads, long long warps_needed) {
   int per_sm = 0;
   FE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0));
   per_sm = std::max(1, per_sm);
-  return std::max(1, std::min(per_sm * sm_count(), ceil_div(n_warps_needed, threads / 32)));
+  return std::max(1, (int)std::min<long long>((long long)per_sm * sm_count(), (warps_needed + threads / 32 - 1) /
+                                                                                   (threads / 32)));
 }
 }  // namespace
+
+TsneDevice::~TsneDevice() {
+  if (fork) cudaEventDestroy(fork);
+  if (join) cudaEventDestroy(join);
+  if (side) cudaStreamDestroy(side);
+}
+
+int default_grid_size(int n, int mode) {
+  const char* env = std::getenv("FASTEMBEDR_TSNE_FFT_GRID");
+  const int g = cuda_fft_grid_size(n);
+  if (env && env[0]) return g;
+  return mode == kInterpLagrange3 ? std::max(64, g / 2) : g;
+}
 
 void tsne_device_alloc(TsneDevice& d, int n, int grid, int mode) {
   d.n = n;
@@ -603,13 +679,14 @@ void tsne_device_alloc(TsneDevice& d, int n, int grid, int mode) {
   const int m = d.fft;
   d.cols_per_block = m >= 512 ? 2 : 1;
   d.col_blocks = m / d.cols_per_block;
-  d.step_blocks = mode == kInterpBilinear
-                      ? persistent_blocks(fused_step_kernel<2, false>, kStepThreads, n)
-                      : persistent_blocks(fused_step_kernel<3, false>, kStepThreads, n);
-  const int nparts = std::max(d.step_blocks, point_blocks(n));
+  d.attr_blocks = persistent_blocks(attractive_kernel, kAttrThreads, n);
+  d.update_blocks = mode == kInterpBilinear
+                        ? persistent_blocks(update_kernel<2, false>, kStepThreads, ceil_div(n, 32))
+                        : persistent_blocks(update_kernel<3, false>, kStepThreads, ceil_div(n, 32));
+  const int nparts = std::max(d.update_blocks, point_blocks(n));
   d.arena.release();
   d.arena.reserve(&d.y, n);
-  d.arena.reserve(&d.ynew, n);
+  d.arena.reserve(&d.attr, n);
   d.arena.reserve(&d.gains, n);
   d.arena.reserve(&d.update, n);
   d.arena.reserve(&d.charges, (std::size_t)grid * grid);
@@ -633,6 +710,9 @@ void tsne_device_alloc(TsneDevice& d, int n, int grid, int mode) {
   FE_CUDA(cudaMemset(d.potential, 0, sizeof(float4) * (std::size_t)grid * grid));
   FE_CUDA(cudaMemset(d.counter, 0, sizeof(unsigned)));
   FE_CUDA(cudaMemset(d.cur, 0, sizeof(GridState)));
+  if (!d.side) FE_CUDA(cudaStreamCreateWithFlags(&d.side, cudaStreamNonBlocking));
+  if (!d.fork) FE_CUDA(cudaEventCreateWithFlags(&d.fork, cudaEventDisableTiming));
+  if (!d.join) FE_CUDA(cudaEventCreateWithFlags(&d.join, cudaEventDisableTiming));
   const int big = 3 * d.cols_per_block * m * (int)sizeof(float2);
   FE_CUDA(cudaFuncSetAttribute(columns_convolve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   const int rowb = 2 * m * (int)sizeof(float2);
@@ -641,10 +721,10 @@ void tsne_device_alloc(TsneDevice& d, int n, int grid, int mode) {
 }
 
 void tsne_device_init(TsneDevice& d, const float* d_init, cudaStream_t s) {
-  FE_CUDA(cudaMemcpyAsync(d.ynew, d_init, sizeof(float2) * d.n, cudaMemcpyDeviceToDevice, s));
+  FE_CUDA(cudaMemcpyAsync(d.y, d_init, sizeof(float2) * d.n, cudaMemcpyDeviceToDevice, s));
   fill_state_kernel<<<point_blocks(d.n), 256, 0, s>>>(d.gains, d.update, d.n);
   FE_LAUNCH("fill_state_kernel");
-  layout_stats_kernel<<<point_blocks(d.n), kStepThreads, 0, s>>>(d.ynew, d.n, d.grid, d.mode, d.partial, d.counter,
+  layout_stats_kernel<<<point_blocks(d.n), kStepThreads, 0, s>>>(d.y, d.n, d.grid, d.mode, d.partial, d.counter,
                                                                   d.next);
   FE_LAUNCH("layout_stats_kernel");
 }
@@ -652,9 +732,9 @@ void tsne_device_init(TsneDevice& d, const float* d_init, cudaStream_t s) {
 void tsne_grid_stage(TsneDevice& d, cudaStream_t s) {
   const int m = d.fft;
   if (d.mode == kInterpBilinear)
-    scatter_kernel<2><<<point_blocks(d.n), 256, 0, s>>>(d.ynew, d.y, d.n, d.grid, d.cur, d.next, d.charges);
+    scatter_kernel<2><<<point_blocks(d.n), 256, 0, s>>>(d.y, d.n, d.grid, d.cur, d.next, d.charges);
   else
-    scatter_kernel<3><<<point_blocks(d.n), 256, 0, s>>>(d.ynew, d.y, d.n, d.grid, d.cur, d.next, d.charges);
+    scatter_kernel<3><<<point_blocks(d.n), 256, 0, s>>>(d.y, d.n, d.grid, d.cur, d.next, d.charges);
   FE_LAUNCH("scatter_kernel");
   rows_forward_kernel<<<2 * d.nodes, kFftThreads, 2 * m * sizeof(float2), s>>>(d.charges, d.grid, d.nodes,
                                                                                 d.log_fft, d.twiddle, d.cur,
@@ -669,45 +749,55 @@ void tsne_grid_stage(TsneDevice& d, cudaStream_t s) {
   FE_LAUNCH("rows_inverse_kernel");
 }
 
-void tsne_iteration(TsneDevice& d, const DeviceCsr& P, float exag, float lr, float mom, float min_gain,
-                    float max_step, cudaStream_t s) {
-  tsne_grid_stage(d, s);
-  tsne_step_stage(d, P, exag, lr, mom, min_gain, max_step, s);
+void tsne_attractive_stage(TsneDevice& d, const DeviceCsr& P, float exag, cudaStream_t s) {
+  attractive_kernel<<<d.attr_blocks, kAttrThreads, 0, s>>>(P.row_ptr, P.col, P.val, d.y, d.n, exag, d.attr);
+  FE_LAUNCH("attractive_kernel");
 }
 
-void tsne_step_stage(TsneDevice& d, const DeviceCsr& P, float exag, float lr, float mom, float min_gain,
-                     float max_step, cudaStream_t s) {
+void tsne_update_stage(TsneDevice& d, float lr, float mom, float min_gain, float max_step, cudaStream_t s) {
   if (d.mode == kInterpBilinear)
-    fused_step_kernel<2, false><<<d.step_blocks, kStepThreads, 0, s>>>(
-        P.row_ptr, P.col, P.val, d.y, d.ynew, d.gains, d.update, d.potential, d.grid, d.n, d.cur, d.next,
-        d.partial, d.counter, d.mode, exag, lr, mom, min_gain, max_step, nullptr, nullptr);
+    update_kernel<2, false><<<d.update_blocks, kStepThreads, 0, s>>>(
+        d.y, d.attr, d.gains, d.update, d.potential, d.grid, d.n, d.cur, d.next, d.partial, d.counter, d.mode, lr,
+        mom, min_gain, max_step, nullptr);
   else
-    fused_step_kernel<3, false><<<d.step_blocks, kStepThreads, 0, s>>>(
-        P.row_ptr, P.col, P.val, d.y, d.ynew, d.gains, d.update, d.potential, d.grid, d.n, d.cur, d.next,
-        d.partial, d.counter, d.mode, exag, lr, mom, min_gain, max_step, nullptr, nullptr);
-  FE_LAUNCH("fused_step_kernel");
+    update_kernel<3, false><<<d.update_blocks, kStepThreads, 0, s>>>(
+        d.y, d.attr, d.gains, d.update, d.potential, d.grid, d.n, d.cur, d.next, d.partial, d.counter, d.mode, lr,
+        mom, min_gain, max_step, nullptr);
+  FE_LAUNCH("update_kernel");
+}
+
+void tsne_iteration(TsneDevice& d, const DeviceCsr& P, float exag, float lr, float mom, float min_gain,
+                    float max_step, cudaStream_t s) {
+  FE_CUDA(cudaEventRecord(d.fork, s));
+  FE_CUDA(cudaStreamWaitEvent(d.side, d.fork, 0));
+  tsne_attractive_stage(d, P, exag, d.side);
+  FE_CUDA(cudaEventRecord(d.join, d.side));
+  tsne_grid_stage(d, s);
+  FE_CUDA(cudaStreamWaitEvent(s, d.join, 0));
+  tsne_update_stage(d, lr, mom, min_gain, max_step, s);
 }
 
 void tsne_forces(TsneDevice& d, const DeviceCsr& P, float exag, float* d_attr, float* d_rep, cudaStream_t s) {
+  tsne_attractive_stage(d, P, exag, s);
   tsne_grid_stage(d, s);
-  float2* a = reinterpret_cast<float2*>(d_attr);
+  FE_CUDA(cudaMemcpyAsync(d_attr, d.attr, sizeof(float2) * d.n, cudaMemcpyDeviceToDevice, s));
   float2* r = reinterpret_cast<float2*>(d_rep);
   if (d.mode == kInterpBilinear)
-    fused_step_kernel<2, true><<<d.step_blocks, kStepThreads, 0, s>>>(
-        P.row_ptr, P.col, P.val, d.y, d.ynew, d.gains, d.update, d.potential, d.grid, d.n, d.cur, d.next,
-        d.partial, d.counter, d.mode, exag, 0.0f, 0.0f, 0.0f, 0.0f, a, r);
+    update_kernel<2, true><<<d.update_blocks, kStepThreads, 0, s>>>(
+        d.y, d.attr, d.gains, d.update, d.potential, d.grid, d.n, d.cur, d.next, d.partial, d.counter, d.mode, 0.0f,
+        0.0f, 0.0f, 0.0f, r);
   else
-    fused_step_kernel<3, true><<<d.step_blocks, kStepThreads, 0, s>>>(
-        P.row_ptr, P.col, P.val, d.y, d.ynew, d.gains, d.update, d.potential, d.grid, d.n, d.cur, d.next,
-        d.partial, d.counter, d.mode, exag, 0.0f, 0.0f, 0.0f, 0.0f, a, r);
-  FE_LAUNCH("fused_step_kernel(diagnostic)");
+    update_kernel<3, true><<<d.update_blocks, kStepThreads, 0, s>>>(
+        d.y, d.attr, d.gains, d.update, d.potential, d.grid, d.n, d.cur, d.next, d.partial, d.counter, d.mode, 0.0f,
+        0.0f, 0.0f, 0.0f, r);
+  FE_LAUNCH("update_kernel(diagnostic)");
 }
 
 void tsne_finalize(TsneDevice& d, float* d_out, cudaStream_t s) {
-  finalize_kernel<<<point_blocks(d.n), 256, 0, s>>>(d.ynew, d.next, d.n, reinterpret_cast<float2*>(d_out));
+  finalize_kernel<<<point_blocks(d.n), 256, 0, s>>>(d.y, d.next, d.n, reinterpret_cast<float2*>(d_out));
   FE_LAUNCH("finalize_kernel");
 }
 
-int tsne_launches_per_iteration() { return 5; }
+int tsne_launches_per_iteration() { return 6; }
 
 }  // namespace fe

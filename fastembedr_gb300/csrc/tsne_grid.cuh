@@ -24,7 +24,8 @@ struct StepPartial {
   double sum_x, sum_y;
 };
 
-// Device buffers of one t-SNE instance (all inside one arena).
+// Device buffers of one t-SNE instance (all inside one arena) and the side stream that runs
+// the attractive pass concurrently with the grid stage.
 struct TsneDevice {
   int n = 0;
   int grid = 0;     // G: nodes per side of the charge grid
@@ -32,8 +33,8 @@ struct TsneDevice {
   int log_fft = 0;
   int mode = kInterpLagrange3;
   int nodes = 0;
-  float2* y = nullptr;      // layout read by the gradient (stored, not recentred)
-  float2* ynew = nullptr;   // layout written by the update
+  float2* y = nullptr;        // layout (stored, recentred lazily by the update)
+  float2* attr = nullptr;     // attractive force of the current iteration
   float2* gains = nullptr;
   float2* update = nullptr;
   float4* charges = nullptr;  // G x G (mass, mass*dx, mass*dy, 0)
@@ -46,29 +47,40 @@ struct TsneDevice {
   GridState* next = nullptr;
   StepPartial* partial = nullptr;
   unsigned* counter = nullptr;
-  int step_blocks = 0;
+  int attr_blocks = 0;
+  int update_blocks = 0;
   int col_blocks = 0;
   int cols_per_block = 0;
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
   Arena arena;
+  TsneDevice() = default;
+  TsneDevice(const TsneDevice&) = delete;
+  TsneDevice& operator=(const TsneDevice&) = delete;
+  ~TsneDevice();
 };
 
+// Lagrange runs at half the reference's node count per side: its O(h^3) interpolation error at
+// G / 2 stays below the bilinear O(h^2) error at G (checked by the GPU tests).
+int default_grid_size(int n, int mode);
+
 void tsne_device_alloc(TsneDevice& d, int n, int grid, int mode);
-// Copy a row-major float2 init into ynew, zero gains/update state and compute `next`.
+// Copy a row-major float2 init into the layout, reset gains/update and compute `next`.
 void tsne_device_init(TsneDevice& d, const float* d_init, cudaStream_t s);
-// One optimizer iteration (scatter, FFT convolution, fused attractive + update).
+// One optimizer iteration: grid stage on `s` concurrently with the attractive pass on the side
+// stream, then the update (6 launches).
 void tsne_iteration(TsneDevice& d, const DeviceCsr& P, float exaggeration, float learning_rate, float momentum,
                     float min_gain, float max_step_norm, cudaStream_t s);
-// The two halves of an iteration: scatter + FFT convolution (4 launches), fused step (1).
+// Stages, for profiling: scatter + FFT convolution (4 launches), attractive (1), update (1).
 void tsne_grid_stage(TsneDevice& d, cudaStream_t s);
-void tsne_step_stage(TsneDevice& d, const DeviceCsr& P, float exaggeration, float learning_rate, float momentum,
-                     float min_gain, float max_step_norm, cudaStream_t s);
-// out = ynew - mean(ynew), row-major float2.
+void tsne_attractive_stage(TsneDevice& d, const DeviceCsr& P, float exaggeration, cudaStream_t s);
+void tsne_update_stage(TsneDevice& d, float learning_rate, float momentum, float min_gain, float max_step_norm,
+                       cudaStream_t s);
+// out = y - mean(y), row-major float2.
 void tsne_finalize(TsneDevice& d, float* d_out, cudaStream_t s);
-// Forces on the current layout without updating it (diagnostics): attractive and repulsive
-// parts separately, plus the grid Z.
+// Forces on the current layout without updating it (diagnostics).
 void tsne_forces(TsneDevice& d, const DeviceCsr& P, float exaggeration, float* d_attr, float* d_rep,
                  cudaStream_t s);
-// Kernel launch counts per iteration (for launch accounting).
 int tsne_launches_per_iteration();
 
 }  // namespace fe

@@ -32,14 +32,16 @@ bool fastembedr_cuda_available(void);
 const char* fastembedr_cuda_embedding_last_error(void);
 
 /* replaces fastembedr_cuda_opentsne_fft_grid_size, src/embedding_cuda_kernels.cpp:5625-5627:
- * grid nodes per side, 256 (n < 20k) / 512 / 1024 (n >= 100k), FASTEMBEDR_TSNE_FFT_GRID override */
+ * grid nodes per side. Reference bilinear stencil: 256 (n < 20k) / 512 / 1024 (n >= 100k);
+ * the default 3-node Lagrange stencil uses half of that; FASTEMBEDR_TSNE_FFT_GRID overrides both. */
 int fastembedr_cuda_opentsne_fft_grid_size(int n);
 
 /* ---------------------------------------------------------------- t-SNE from KNN */
 
 /* replaces fastembedr_cuda_opentsne_fft_from_knn_float, src/embedding_cuda_kernels.cpp:6207-6234.
  * Perplexity affinities, symmetrised CSR P, then early_exaggeration_iter + n_iter iterations of
- * the gains/momentum optimizer with FFT-grid repulsion. learning_rate_auto: lr = n / exaggeration
+ * the gains/momentum optimizer with FFT-grid repulsion (grid nodes per side from
+ * fastembedr_cuda_opentsne_fft_grid_size). learning_rate_auto: lr = n / exaggeration
  * of each phase. max_step_norm <= 0 or non-finite disables the step clip. has_init = 0 draws a
  * seeded N(0, 1e-4^2) layout. Repulsion interpolation: FASTEMBEDR_TSNE_INTERPOLATION=bilinear
  * selects the reference stencil, otherwise 3-node Lagrange boxes. */
@@ -105,10 +107,12 @@ int fastembedr_tsne_plan_create(const int* indices, const float* distances, cons
 /* enqueue `iters` iterations on the plan's stream (CUDA graph when use_graph != 0) */
 int fastembedr_tsne_plan_run(fastembedr_tsne_plan* plan, int iters, float exaggeration, float learning_rate,
                              float momentum, float min_gain, float max_step_norm, int use_graph);
-/* run `iters` iterations eagerly and report device time: total, and the fused step kernel alone */
+/* run `iters` iterations eagerly, one stage after the other, and report device time (CUDA
+ * events on the plan's stream): total, the attractive CSR kernel alone, and the grid stage
+ * (scatter + FFT convolution) */
 int fastembedr_tsne_plan_profile(fastembedr_tsne_plan* plan, int iters, float exaggeration, float learning_rate,
                                  float momentum, float min_gain, float max_step_norm, float* ms_total,
-                                 float* ms_step_kernel, float* ms_grid_stage);
+                                 float* ms_attractive_kernel, float* ms_grid_stage);
 int fastembedr_tsne_plan_synchronize(fastembedr_tsne_plan* plan);
 /* the plan's cudaStream_t, for callers that time with their own events */
 void* fastembedr_tsne_plan_stream(fastembedr_tsne_plan* plan);

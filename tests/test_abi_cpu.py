@@ -39,8 +39,13 @@ def test_library_exports_every_declared_symbol():
 def test_grid_policy_matches_reference_cuda(monkeypatch):
     lib = _lib.load()
     monkeypatch.delenv("FASTEMBEDR_TSNE_FFT_GRID", raising=False)
-    assert [lib.fastembedr_cuda_opentsne_fft_grid_size(n) for n in (1000, 19999, 20000, 99999, 100000, 10**6)] == \
-        [256, 256, 512, 512, 1024, 1024]
+    sizes = (1000, 19999, 20000, 99999, 100000, 10**6)
+    monkeypatch.setenv("FASTEMBEDR_TSNE_INTERPOLATION", "bilinear")
+    assert [lib.fastembedr_cuda_opentsne_fft_grid_size(n) for n in sizes] == [256, 256, 512, 512, 1024, 1024]
+    monkeypatch.setenv("FASTEMBEDR_TSNE_INTERPOLATION", "lagrange")
+    assert [lib.fastembedr_cuda_opentsne_fft_grid_size(n) for n in sizes] == [128, 128, 256, 256, 512, 512]
+    monkeypatch.setenv("FASTEMBEDR_TSNE_FFT_GRID", "64")
+    assert lib.fastembedr_cuda_opentsne_fft_grid_size(10**6) == 64
 
 
 def test_no_device_is_an_error_not_a_fallback():
