@@ -32,6 +32,21 @@ void row_probabilities(const int* d_idx, const float* d_dist, int n, int k, floa
 void symmetrise(const int* d_idx, const float* d_p, int n, int k, int offset, DeviceCsr& out,
                 cudaStream_t s);
 
+// Device-wide exclusive scan of n int32 counts into n + 1 int64 offsets (out[n] = total);
+// tmp holds ceil(n / 1024) int64 values.
+void exclusive_scan(const int* in, long long* out, int n, long long* tmp, cudaStream_t s);
+
+// Stable LSD radix sort of (key, value) pairs on the low `bits` key bits. Buffers of n items
+// each plus the histogram workspace sized by radix_sort_workspace().
+struct RadixWorkspace {
+  int* hist = nullptr;          // 256 x blocks
+  long long* offs = nullptr;    // 256 x blocks + 1
+  long long* scan_tmp = nullptr;
+};
+int radix_sort_blocks(int n);
+void radix_sort_pairs(unsigned* keys, int* vals, unsigned* keys_tmp, int* vals_tmp, int n, int bits,
+                      const RadixWorkspace& ws, cudaStream_t s);
+
 // Grid policy of the reference CUDA path (src/embedding_cuda_kernels.cpp:5610-5623), including
 // the FASTEMBEDR_TSNE_FFT_GRID override.
 int cuda_fft_grid_size(int n);

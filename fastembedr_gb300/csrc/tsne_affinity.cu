@@ -74,20 +74,22 @@ row_probabilities_kernel(const float* __restrict__ dist, int n, int k, int rows,
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int rr = warp; rr < nrows; rr += kBisectWarps) {
     const float* d = tile + rr * k;
-    double min_d2 = DBL_MAX, max_d2 = 0.0;
+    // zero-spread test in float arithmetic, as compute_row_probabilities_float does it
+    float min_f = FLT_MAX, max_f = 0.0f;
+    double min_d2 = DBL_MAX;
     for (int j = lane; j < k; j += 32) {
+      const float df = d[j] * d[j];
+      min_f = fminf(min_f, df);
+      max_f = fmaxf(max_f, df);
       const double dj = d[j];
-      const double d2 = dj * dj;  // exact: a float squared fits in a double
-      min_d2 = fmin(min_d2, d2);
-      max_d2 = fmax(max_d2, d2);
+      min_d2 = fmin(min_d2, dj * dj);  // exact: a float squared fits in a double
     }
+    min_f = warp_min(min_f);
+    max_f = warp_max(max_f);
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      min_d2 = fmin(min_d2, __shfl_xor_sync(0xffffffffu, min_d2, o));
-      max_d2 = fmax(max_d2, __shfl_xor_sync(0xffffffffu, max_d2, o));
-    }
+    for (int o = 16; o > 0; o >>= 1) min_d2 = fmin(min_d2, __shfl_xor_sync(0xffffffffu, min_d2, o));
     float* prow = p_out + (long long)(r0 + rr) * k;
-    if (max_d2 - min_d2 <= DBL_EPSILON * fmax(1.0, max_d2)) {
+    if (max_f - min_f <= FLT_EPSILON * fmaxf(1.0f, max_f)) {
       const float u = 1.0f / (float)k;
       for (int j = lane; j < k; j += 32) prow[j] = u;
       if (entropy_out && lane == 0) entropy_out[r0 + rr] = log((double)k);
@@ -95,6 +97,7 @@ row_probabilities_kernel(const float* __restrict__ dist, int n, int k, int rows,
     }
     double beta = 1.0, beta_min = -DBL_MAX, beta_max = DBL_MAX;
     double beta_eval = beta, sum_eval = 1.0, entropy_eval = 0.0;
+    bool exact_eval = false;
     for (int it = 0; it < 200; ++it) {
       double sp = 0.0, sw = 0.0;
       for (int j = lane; j < k; j += 32) {
@@ -106,11 +109,30 @@ row_probabilities_kernel(const float* __restrict__ dist, int n, int k, int rows,
       }
       sp = warp_sum(sp);
       sw = warp_sum(sw);
-      const double entropy = beta * sw / sp + log(sp);
+      double entropy = beta * sw / sp + log(sp);
+      double diff = entropy - log_perplexity;
+      exact_eval = false;
+      // The stop test is the only decision FP32 exp can flip: re-evaluate near its boundary
+      // with FP64 exp so the bisection follows the FP64 path.
+      if (fabs(fabs(diff) - 1e-5) < 1e-6) {
+        sp = 0.0;
+        sw = 0.0;
+        for (int j = lane; j < k; j += 32) {
+          const double dj = d[j];
+          const double s = dj * dj - min_d2;
+          const double p = exp(-beta * s);
+          sp += p;
+          sw += s * p;
+        }
+        sp = warp_sum(sp);
+        sw = warp_sum(sw);
+        entropy = beta * sw / sp + log(sp);
+        diff = entropy - log_perplexity;
+        exact_eval = true;
+      }
       beta_eval = beta;
       sum_eval = sp;
       entropy_eval = entropy;
-      const double diff = entropy - log_perplexity;
       if (fabs(diff) < 1e-5) break;
       if (diff > 0.0) {
         beta_min = beta;
@@ -125,7 +147,8 @@ row_probabilities_kernel(const float* __restrict__ dist, int n, int k, int rows,
     for (int j = lane; j < k; j += 32) {
       const double dj = d[j];
       const double s = dj * dj - min_d2;
-      prow[j] = (float)((double)expf((float)(-beta_eval * s)) * inv);
+      const double p = exact_eval ? exp(-beta_eval * s) : (double)expf((float)(-beta_eval * s));
+      prow[j] = (float)(p * inv);
     }
     if (entropy_out && lane == 0) entropy_out[r0 + rr] = entropy_eval;
   }
@@ -220,7 +243,7 @@ __global__ void scan_add_kernel(long long* out, int n, const long long* sums) {
 }
 
 // out must hold n + 1 values; out[n] = total. tmp must hold ceil(n / 1024) values.
-static void exclusive_scan(const int* in, long long* out, int n, long long* tmp, cudaStream_t s) {
+void exclusive_scan(const int* in, long long* out, int n, long long* tmp, cudaStream_t s) {
   const int nb = std::max(1, ceil_div(n, kScanBlock));
   scan_blocks_kernel<<<nb, kScanBlock, 0, s>>>(in, out, n, tmp);
   FE_LAUNCH("scan_blocks_kernel");

@@ -35,6 +35,11 @@ __global__ void double_to_float_kernel(const double* __restrict__ in, float* __r
     out[t] = (float)in[t];
 }
 
+bool reorder_enabled() {
+  const char* env = std::getenv("FASTEMBEDR_TSNE_REORDER");
+  return !(env && env[0] == '0');
+}
+
 bool graph_capture_enabled() {
   const char* env = std::getenv("FASTEMBEDR_CUDA_GRAPH_CAPTURE");
   if (!env || !env[0]) return true;
@@ -85,17 +90,23 @@ struct TsneJob {
     FE_CUDA(cudaStreamSynchronize(s));
   }
 
+  // Iterations in chunks of 25; each chunk starts with a spatial reorder of the points and
+  // is one CUDA graph launch (two streams inside).
   void run(int iters, float exag, float lr, float mom, float min_gain, float max_step, bool use_graph) {
     cudaStream_t s = stream.s;
     if (iters <= 0) return;
-    if (!use_graph || !graph_capture_enabled()) {
-      for (int it = 0; it < iters; ++it) tsne_iteration(D, P, exag, lr, mom, min_gain, max_step, s);
-      return;
-    }
-    constexpr int kChunk = 25;  // iterations per graph, as the reference's graph chunks
+    constexpr int kChunk = 25;
+    const bool reorder = reorder_enabled();
+    const bool graph = use_graph && graph_capture_enabled();
     int left = iters;
     while (left > 0) {
       const int c = std::min(kChunk, left);
+      if (!graph) {
+        if (reorder) tsne_reorder(D, P, s);
+        for (int r = 0; r < c; ++r) tsne_iteration(D, P, exag, lr, mom, min_gain, max_step, s);
+        left -= c;
+        continue;
+      }
       const Key key{c, exag, lr, mom, min_gain, max_step};
       auto it = graphs.find(key);
       if (it == graphs.end()) {
@@ -103,6 +114,7 @@ struct TsneJob {
         cudaGraphExec_t ge = nullptr;
         FE_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         try {
+          if (reorder) tsne_reorder(D, P, s);
           for (int r = 0; r < c; ++r) tsne_iteration(D, P, exag, lr, mom, min_gain, max_step, s);
         } catch (...) {
           cudaStreamEndCapture(s, &g);
@@ -349,7 +361,7 @@ int fastembedr_cuda_tsne_force_diagnostic(const int* indices, const float* dista
       if (z_exact) *z_exact = zt;
     }
     if (kl) {
-      fe::exact_kl(job.P, d_y, d_zrow, d_work, d_sc + 2, s);
+      fe::exact_kl(job.P, d_y, nullptr, d_zrow, d_work, d_sc + 2, s);
       FE_CUDA(cudaMemcpyAsync(kl, d_sc + 3, sizeof(double), cudaMemcpyDeviceToHost, s));
     }
     FE_CUDA(cudaStreamSynchronize(s));
@@ -460,8 +472,7 @@ int fastembedr_tsne_plan_kl(fastembedr_tsne_plan* plan, double* kl) {
     a.reserve(&d_work, n);
     a.reserve(&d_sc, 2);
     a.commit("t-SNE KL");
-    fe::tsne_finalize(J.D, d_y, s);
-    fe::exact_kl(J.P, d_y, d_zrow, d_work, d_sc, s);
+    fe::exact_kl(J.P, reinterpret_cast<const float*>(J.D.y), J.D.inv, d_zrow, d_work, d_sc, s);
     FE_CUDA(cudaMemcpyAsync(kl, d_sc + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
     FE_CUDA(cudaStreamSynchronize(s));
   });

@@ -81,13 +81,15 @@ __global__ void reduce_double_kernel(const double* __restrict__ v, int n, double
 }
 
 // KL = sum_CSR p log((p + 1e-9) / (q / Z + 1e-9)); Z rounded to float as the reference keeps it.
+// Row i of P belongs to the point at y[inv[i]] (inv = nullptr: y is in row order); columns index y.
 __global__ void __launch_bounds__(256)
 kl_rows_kernel(const int* __restrict__ row_ptr, const int* __restrict__ col, const float* __restrict__ val,
-               const float2* __restrict__ y, int n, const double* __restrict__ zsum, double* __restrict__ out) {
+               const float2* __restrict__ y, const int* __restrict__ inv, int n, const double* __restrict__ zsum,
+               double* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double z = (double)(float)fmax(*zsum, (double)FLT_MIN);
-  const float2 yi = y[i];
+  const float2 yi = y[inv ? inv[i] : i];
   double acc = 0.0;
   for (int p = row_ptr[i]; p < row_ptr[i + 1]; ++p) {
     const float2 yj = y[col[p]];
@@ -109,15 +111,15 @@ void exact_repulsion(const float* d_y, int n, double* d_rep, double* d_zrow, dou
   FE_LAUNCH("reduce_double_kernel");
 }
 
-void exact_kl(const DeviceCsr& P, const float* d_y, double* d_zrow, double* d_work, double* d_scalars,
-              cudaStream_t s) {
+void exact_kl(const DeviceCsr& P, const float* d_y, const int* d_inv, double* d_zrow, double* d_work,
+              double* d_scalars, cudaStream_t s) {
   const int n = P.n;
   const float2* y = reinterpret_cast<const float2*>(d_y);
   sum_q_rows_kernel<<<ceil_div(n, 256), 256, 0, s>>>(y, n, d_zrow);
   FE_LAUNCH("sum_q_rows_kernel");
   reduce_double_kernel<<<1, 1024, 0, s>>>(d_zrow, n, d_scalars);
   FE_LAUNCH("reduce_double_kernel");
-  kl_rows_kernel<<<ceil_div(n, 256), 256, 0, s>>>(P.row_ptr, P.col, P.val, y, n, d_scalars, d_work);
+  kl_rows_kernel<<<ceil_div(n, 256), 256, 0, s>>>(P.row_ptr, P.col, P.val, y, d_inv, n, d_scalars, d_work);
   FE_LAUNCH("kl_rows_kernel");
   reduce_double_kernel<<<1, 1024, 0, s>>>(d_work, n, d_scalars + 1);
   FE_LAUNCH("reduce_double_kernel");

@@ -9,8 +9,9 @@ namespace fe {
 // d_ztotal: sum over all ordered pairs i != j.
 void exact_repulsion(const float* d_y, int n, double* d_rep, double* d_zrow, double* d_ztotal, cudaStream_t s);
 
-// d_scalars[0] = all-pairs Z, d_scalars[1] = KL. d_zrow, d_work: n doubles each.
-void exact_kl(const DeviceCsr& P, const float* d_y, double* d_zrow, double* d_work, double* d_scalars,
-              cudaStream_t s);
+// d_scalars[0] = all-pairs Z, d_scalars[1] = KL. d_zrow, d_work: n doubles each. Row i of P is
+// the point y[d_inv[i]] (d_inv may be null for row order); P's columns index d_y.
+void exact_kl(const DeviceCsr& P, const float* d_y, const int* d_inv, double* d_zrow, double* d_work,
+              double* d_scalars, cudaStream_t s);
 
 }  // namespace fe

@@ -192,25 +192,61 @@ layout_stats_kernel(const float2* __restrict__ ynew, int n, int grid, int mode, 
 
 // ---------------------------------------------------------------- scatter
 // Each point adds (w, w*(x - cx), w*(y - cy)) to its TAPS x TAPS stencil nodes; block 0 also
-// promotes the grid computed by the previous update (`next`) to `cur`.
+// promotes the grid computed by the previous update (`next`) to `cur`. Points are stored in
+// spatial order, so lanes of a warp often share a stencil anchor: runs of equal anchors are
+// summed with a segmented warp reduction and only the run head issues the vector atomics,
+// which removes the hot-node contention when clusters collapse onto a few grid cells.
 template <int TAPS>
 __global__ void __launch_bounds__(256)
 scatter_kernel(const float2* __restrict__ y, int n, int grid, GridState* __restrict__ cur,
                const GridState* __restrict__ next, float4* __restrict__ charges) {
+  constexpr int NV = TAPS * TAPS * 3;
   const GridState g = *next;
   if (blockIdx.x == 0 && threadIdx.x == 0) *cur = g;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const float2 p = y[i];
+  const int lane = threadIdx.x & 31;
+  for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n; base += gridDim.x * blockDim.x) {
+    const int i = base + lane;
+    const bool valid = i < n;
+    const float2 p = valid ? y[i] : make_float2(g.cx, g.cy);
     const Stencil<TAPS> sx = make_stencil<TAPS>(p.x, g.x0, g.inv_h, g.inv_box, g.nodes);
     const Stencil<TAPS> sy = make_stencil<TAPS>(p.y, g.y0, g.inv_h, g.inv_box, g.nodes);
     const float dx = p.x - g.cx, dy = p.y - g.cy;
+    float v[NV];
 #pragma unroll
-    for (int a = 0; a < TAPS; ++a) {
-      float4* row = charges + (long long)(sy.base + a) * grid + sx.base;
+    for (int a = 0; a < TAPS; ++a)
 #pragma unroll
       for (int b = 0; b < TAPS; ++b) {
-        const float w = sy.w[a] * sx.w[b];
-        atomicAdd(row + b, make_float4(w, w * dx, w * dy, 0.0f));
+        const float w = valid ? sy.w[a] * sx.w[b] : 0.0f;
+        v[(a * TAPS + b) * 3 + 0] = w;
+        v[(a * TAPS + b) * 3 + 1] = w * dx;
+        v[(a * TAPS + b) * 3 + 2] = w * dy;
+      }
+    const int key = valid ? sy.base * grid + sx.base : -1 - lane;
+    const int prev = __shfl_up_sync(0xffffffffu, key, 1);
+    const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || prev != key);
+    if (heads != 0xffffffffu) {
+      // suffix sums restricted to contiguous runs [lane, next head)
+      const unsigned above = heads & ~((2u << lane) - 1u);
+      const int run_end = above ? __ffs(above) - 1 : 32;
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        const bool take = lane + off < run_end;
+#pragma unroll
+        for (int c = 0; c < NV; ++c) {
+          const float o = __shfl_down_sync(0xffffffffu, v[c], off);
+          if (take) v[c] += o;
+        }
+      }
+    }
+    if (valid && ((heads >> lane) & 1u)) {
+#pragma unroll
+      for (int a = 0; a < TAPS; ++a) {
+        float4* row = charges + (long long)(sy.base + a) * grid + sx.base;
+#pragma unroll
+        for (int b = 0; b < TAPS; ++b) {
+          const int c = (a * TAPS + b) * 3;
+          atomicAdd(row + b, make_float4(v[c], v[c + 1], v[c + 2], 0.0f));
+        }
       }
     }
   }
@@ -481,7 +517,7 @@ rows_inverse_kernel(const float2* __restrict__ rows, int grid, int nodes, int lo
 }
 
 // ---------------------------------------------------------------- attractive pass
-// One warp per CSR row, rows strided over a persistent grid:
+// One warp per point (storage slot i visits CSR row perm[i]), strided over a persistent grid:
 //   a_i = exag * sum_j p_ij q_ij (y_i - y_j), q = 1 / (1 + d^2)
 // (add_sparse_attractive_gradient_f, src/tsne_neighbors.cpp:1061-1088). Column / value loads
 // are streaming (coalesced, not kept in L1); the y gathers hit the L2-resident layout. Rows
@@ -490,11 +526,13 @@ constexpr int kAttrThreads = 256;
 
 __global__ void __launch_bounds__(kAttrThreads)
 attractive_kernel(const int* __restrict__ row_ptr, const int* __restrict__ col, const float* __restrict__ val,
-                  const float2* __restrict__ y, int n, float exag, float2* __restrict__ attr) {
+                  const float2* __restrict__ y, const int* __restrict__ perm, int n, float exag,
+                  float2* __restrict__ attr) {
   const int lane = threadIdx.x & 31;
   const int warps_total = gridDim.x * (blockDim.x >> 5);
   for (int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps_total) {
-    const int b = __ldg(row_ptr + i), e = __ldg(row_ptr + i + 1);
+    const int row = perm ? __ldg(perm + i) : i;
+    const int b = __ldg(row_ptr + row), e = __ldg(row_ptr + row + 1);
     const float2 yi = __ldg(y + i);
     float ax = 0.0f, ay = 0.0f;
     if (e - b <= 256) {
@@ -633,11 +671,73 @@ __global__ void fill_state_kernel(float2* __restrict__ gains, float2* __restrict
 }
 
 __global__ void finalize_kernel(const float2* __restrict__ y, const GridState* __restrict__ next, int n,
-                                float2* __restrict__ out) {
+                                const int* __restrict__ perm, float2* __restrict__ out) {
   const float mx = (float)next->mean_x, my = (float)next->mean_y;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float2 p = y[i];
-    out[i] = make_float2(p.x - mx, p.y - my);
+    out[perm ? perm[i] : i] = make_float2(p.x - mx, p.y - my);
+  }
+}
+
+// ---------------------------------------------------------------- spatial reorder
+__device__ __forceinline__ unsigned spread_bits(unsigned v) {
+  v &= 0xffffu;
+  v = (v | (v << 8)) & 0x00ff00ffu;
+  v = (v | (v << 4)) & 0x0f0f0f0fu;
+  v = (v | (v << 2)) & 0x33333333u;
+  v = (v | (v << 1)) & 0x55555555u;
+  return v;
+}
+
+template <int TAPS>
+__global__ void anchor_keys_kernel(const float2* __restrict__ y, int n, const GridState* __restrict__ next,
+                                   unsigned* __restrict__ keys, int* __restrict__ order) {
+  const GridState g = *next;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float2 p = y[i];
+    const int bx = make_stencil<TAPS>(p.x, g.x0, g.inv_h, g.inv_box, g.nodes).base;
+    const int by = make_stencil<TAPS>(p.y, g.y0, g.inv_h, g.inv_box, g.nodes).base;
+    keys[i] = spread_bits((unsigned)bx) | (spread_bits((unsigned)by) << 1);
+    order[i] = i;
+  }
+}
+
+__global__ void gather_points_kernel(const int* __restrict__ order, int n, const float2* __restrict__ y,
+                                     const float2* __restrict__ gains, const float2* __restrict__ update,
+                                     const int* __restrict__ perm, float2* __restrict__ scratch,
+                                     int* __restrict__ perm_tmp, int* __restrict__ delta) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    const int o = order[r];
+    scratch[r] = y[o];
+    scratch[n + r] = gains[o];
+    scratch[2 * (long long)n + r] = update[o];
+    perm_tmp[r] = perm[o];
+    delta[o] = r;
+  }
+}
+
+__global__ void scatter_points_kernel(const float2* __restrict__ scratch, const int* __restrict__ perm_tmp, int n,
+                                      float2* __restrict__ y, float2* __restrict__ gains,
+                                      float2* __restrict__ update, int* __restrict__ perm, int* __restrict__ inv) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    y[r] = scratch[r];
+    gains[r] = scratch[n + r];
+    update[r] = scratch[2 * (long long)n + r];
+    const int o = perm_tmp[r];
+    perm[r] = o;
+    inv[o] = r;
+  }
+}
+
+__global__ void relabel_cols_kernel(int* __restrict__ col, long long nnz, const int* __restrict__ delta) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < nnz; p += (long long)gridDim.x * blockDim.x)
+    col[p] = __ldg(delta + __ldcs(col + p));
+}
+
+__global__ void identity_kernel(int* __restrict__ perm, int* __restrict__ inv, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    perm[i] = i;
+    inv[i] = i;
   }
 }
 
@@ -661,12 +761,7 @@ TsneDevice::~TsneDevice() {
   if (side) cudaStreamDestroy(side);
 }
 
-int default_grid_size(int n, int mode) {
-  const char* env = std::getenv("FASTEMBEDR_TSNE_FFT_GRID");
-  const int g = cuda_fft_grid_size(n);
-  if (env && env[0]) return g;
-  return mode == kInterpLagrange3 ? std::max(64, g / 2) : g;
-}
+int default_grid_size(int n, int /*mode*/) { return cuda_fft_grid_size(n); }
 
 void tsne_device_alloc(TsneDevice& d, int n, int grid, int mode) {
   d.n = n;
@@ -699,7 +794,21 @@ void tsne_device_alloc(TsneDevice& d, int n, int grid, int mode) {
   d.arena.reserve(&d.next, 1);
   d.arena.reserve(&d.partial, nparts);
   d.arena.reserve(&d.counter, 1);
+  const int nb = radix_sort_blocks(n);
+  d.arena.reserve(&d.perm, n);
+  d.arena.reserve(&d.inv, n);
+  d.arena.reserve(&d.keys, n);
+  d.arena.reserve(&d.keys_tmp, n);
+  d.arena.reserve(&d.order, n);
+  d.arena.reserve(&d.order_tmp, n);
+  d.arena.reserve(&d.delta, n);
+  d.arena.reserve(&d.perm_tmp, n);
+  d.arena.reserve(&d.scratch, 3 * (std::size_t)n);
+  d.arena.reserve(&d.radix.hist, 256 * (std::size_t)nb);
+  d.arena.reserve(&d.radix.offs, 256 * (std::size_t)nb + 1);
+  d.arena.reserve(&d.radix.scan_tmp, ceil_div(256LL * nb, 1024));
   d.arena.commit("t-SNE optimizer state");
+  d.reordered = false;
   std::vector<float2> tw(m / 2);
   for (int t = 0; t < m / 2; ++t) {
     const double a = -2.0 * M_PI * (double)t / (double)m;
@@ -718,10 +827,15 @@ void tsne_device_alloc(TsneDevice& d, int n, int grid, int mode) {
   const int rowb = 2 * m * (int)sizeof(float2);
   FE_CUDA(cudaFuncSetAttribute(rows_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, rowb));
   FE_CUDA(cudaFuncSetAttribute(rows_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, rowb));
+  // the synchronous setup above ran on the legacy stream, which the job's non-blocking streams
+  // do not wait for
+  FE_CUDA(cudaDeviceSynchronize());
 }
 
 void tsne_device_init(TsneDevice& d, const float* d_init, cudaStream_t s) {
   FE_CUDA(cudaMemcpyAsync(d.y, d_init, sizeof(float2) * d.n, cudaMemcpyDeviceToDevice, s));
+  identity_kernel<<<point_blocks(d.n), 256, 0, s>>>(d.perm, d.inv, d.n);
+  FE_LAUNCH("identity_kernel");
   fill_state_kernel<<<point_blocks(d.n), 256, 0, s>>>(d.gains, d.update, d.n);
   FE_LAUNCH("fill_state_kernel");
   layout_stats_kernel<<<point_blocks(d.n), kStepThreads, 0, s>>>(d.y, d.n, d.grid, d.mode, d.partial, d.counter,
@@ -750,7 +864,8 @@ void tsne_grid_stage(TsneDevice& d, cudaStream_t s) {
 }
 
 void tsne_attractive_stage(TsneDevice& d, const DeviceCsr& P, float exag, cudaStream_t s) {
-  attractive_kernel<<<d.attr_blocks, kAttrThreads, 0, s>>>(P.row_ptr, P.col, P.val, d.y, d.n, exag, d.attr);
+  attractive_kernel<<<d.attr_blocks, kAttrThreads, 0, s>>>(P.row_ptr, P.col, P.val, d.y, d.perm, d.n, exag,
+                                                           d.attr);
   FE_LAUNCH("attractive_kernel");
 }
 
@@ -794,8 +909,35 @@ void tsne_forces(TsneDevice& d, const DeviceCsr& P, float exag, float* d_attr, f
 }
 
 void tsne_finalize(TsneDevice& d, float* d_out, cudaStream_t s) {
-  finalize_kernel<<<point_blocks(d.n), 256, 0, s>>>(d.y, d.next, d.n, reinterpret_cast<float2*>(d_out));
+  finalize_kernel<<<point_blocks(d.n), 256, 0, s>>>(d.y, d.next, d.n, d.perm, reinterpret_cast<float2*>(d_out));
   FE_LAUNCH("finalize_kernel");
+}
+
+void tsne_reorder(TsneDevice& d, DeviceCsr& P, cudaStream_t s) {
+  const int n = d.n;
+  int bits = 0;
+  while ((1 << bits) < d.grid) ++bits;
+  if (d.mode == kInterpBilinear)
+    anchor_keys_kernel<2><<<point_blocks(n), 256, 0, s>>>(d.y, n, d.next, d.keys, d.order);
+  else
+    anchor_keys_kernel<3><<<point_blocks(n), 256, 0, s>>>(d.y, n, d.next, d.keys, d.order);
+  FE_LAUNCH("anchor_keys_kernel");
+  radix_sort_pairs(d.keys, d.order, d.keys_tmp, d.order_tmp, n, 2 * bits, d.radix, s);
+  gather_points_kernel<<<point_blocks(n), 256, 0, s>>>(d.order, n, d.y, d.gains, d.update, d.perm, d.scratch,
+                                                       d.perm_tmp, d.delta);
+  FE_LAUNCH("gather_points_kernel");
+  scatter_points_kernel<<<point_blocks(n), 256, 0, s>>>(d.scratch, d.perm_tmp, n, d.y, d.gains, d.update, d.perm,
+                                                        d.inv);
+  FE_LAUNCH("scatter_points_kernel");
+  relabel_cols_kernel<<<std::max(1, std::min(ceil_div(P.nnz, 256), sm_count() * 16)), 256, 0, s>>>(P.col, P.nnz,
+                                                                                                   d.delta);
+  FE_LAUNCH("relabel_cols_kernel");
+  d.reordered = true;
+}
+
+int tsne_reorder_launches() {
+  // keys, 3 radix passes x (histogram + 3-kernel scan + scatter), gather, scatter, relabel
+  return 1 + 3 * 5 + 3;
 }
 
 int tsne_launches_per_iteration() { return 6; }

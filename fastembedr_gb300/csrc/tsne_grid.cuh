@@ -33,7 +33,7 @@ struct TsneDevice {
   int log_fft = 0;
   int mode = kInterpLagrange3;
   int nodes = 0;
-  float2* y = nullptr;        // layout (stored, recentred lazily by the update)
+  float2* y = nullptr;        // layout in storage order (recentred lazily by the update)
   float2* attr = nullptr;     // attractive force of the current iteration
   float2* gains = nullptr;
   float2* update = nullptr;
@@ -47,6 +47,19 @@ struct TsneDevice {
   GridState* next = nullptr;
   StepPartial* partial = nullptr;
   unsigned* counter = nullptr;
+  // spatial order: storage slot t holds original point perm[t]; inv is the inverse. CSR rows stay
+  // in original order; CSR columns hold storage slots (relabelled at every reorder).
+  int* perm = nullptr;
+  int* inv = nullptr;
+  unsigned* keys = nullptr;
+  unsigned* keys_tmp = nullptr;
+  int* order = nullptr;
+  int* order_tmp = nullptr;
+  int* delta = nullptr;
+  float2* scratch = nullptr;  // 3 x n: y, gains, update while permuting
+  int* perm_tmp = nullptr;
+  RadixWorkspace radix;
+  bool reordered = false;
   int attr_blocks = 0;
   int update_blocks = 0;
   int col_blocks = 0;
@@ -60,8 +73,7 @@ struct TsneDevice {
   ~TsneDevice();
 };
 
-// Lagrange runs at half the reference's node count per side: its O(h^3) interpolation error at
-// G / 2 stays below the bilinear O(h^2) error at G (checked by the GPU tests).
+// Nodes per side used for a given size (the reference CUDA policy for either stencil).
 int default_grid_size(int n, int mode);
 
 void tsne_device_alloc(TsneDevice& d, int n, int grid, int mode);
@@ -76,7 +88,11 @@ void tsne_grid_stage(TsneDevice& d, cudaStream_t s);
 void tsne_attractive_stage(TsneDevice& d, const DeviceCsr& P, float exaggeration, cudaStream_t s);
 void tsne_update_stage(TsneDevice& d, float learning_rate, float momentum, float min_gain, float max_step_norm,
                        cudaStream_t s);
-// out = y - mean(y), row-major float2.
+// Sort points by the Morton code of their stencil anchor on the current grid and permute the
+// point state (storage order) and the CSR column labels accordingly.
+void tsne_reorder(TsneDevice& d, DeviceCsr& P, cudaStream_t s);
+int tsne_reorder_launches();
+// out[original id] = y - mean(y), row-major float2.
 void tsne_finalize(TsneDevice& d, float* d_out, cudaStream_t s);
 // Forces on the current layout without updating it (diagnostics).
 void tsne_forces(TsneDevice& d, const DeviceCsr& P, float exaggeration, float* d_attr, float* d_rep,

@@ -32,8 +32,7 @@ bool fastembedr_cuda_available(void);
 const char* fastembedr_cuda_embedding_last_error(void);
 
 /* replaces fastembedr_cuda_opentsne_fft_grid_size, src/embedding_cuda_kernels.cpp:5625-5627:
- * grid nodes per side. Reference bilinear stencil: 256 (n < 20k) / 512 / 1024 (n >= 100k);
- * the default 3-node Lagrange stencil uses half of that; FASTEMBEDR_TSNE_FFT_GRID overrides both. */
+ * grid nodes per side, 256 (n < 20k) / 512 / 1024 (n >= 100k), FASTEMBEDR_TSNE_FFT_GRID override */
 int fastembedr_cuda_opentsne_fft_grid_size(int n);
 
 /* ---------------------------------------------------------------- t-SNE from KNN */

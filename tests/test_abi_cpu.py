@@ -43,7 +43,7 @@ def test_grid_policy_matches_reference_cuda(monkeypatch):
     monkeypatch.setenv("FASTEMBEDR_TSNE_INTERPOLATION", "bilinear")
     assert [lib.fastembedr_cuda_opentsne_fft_grid_size(n) for n in sizes] == [256, 256, 512, 512, 1024, 1024]
     monkeypatch.setenv("FASTEMBEDR_TSNE_INTERPOLATION", "lagrange")
-    assert [lib.fastembedr_cuda_opentsne_fft_grid_size(n) for n in sizes] == [128, 128, 256, 256, 512, 512]
+    assert [lib.fastembedr_cuda_opentsne_fft_grid_size(n) for n in sizes] == [256, 256, 512, 512, 1024, 1024]
     monkeypatch.setenv("FASTEMBEDR_TSNE_FFT_GRID", "64")
     assert lib.fastembedr_cuda_opentsne_fft_grid_size(10**6) == 64
 
