@@ -547,10 +547,13 @@ int cuda_fft_grid_size(int n) {
   return g;
 }
 
+// Default: the reference's bilinear stencil. FASTEMBEDR_TSNE_INTERPOLATION=lagrange selects
+// 3-node Lagrange boxes (more accurate forces in L2, but an interpolant that is discontinuous
+// at box edges, which measurably degrades the local neighbourhood structure of the result).
 int interp_mode_from_env() {
   const char* env = std::getenv("FASTEMBEDR_TSNE_INTERPOLATION");
-  if (env && (env[0] == 'b' || env[0] == 'B')) return kInterpBilinear;
-  return kInterpLagrange3;
+  if (env && (env[0] == 'l' || env[0] == 'L')) return kInterpLagrange3;
+  return kInterpBilinear;
 }
 
 }  // namespace fe

@@ -399,6 +399,7 @@ int fastembedr_tsne_plan_profile(fastembedr_tsne_plan* plan, int iters, float ex
     if (!plan || iters < 1) throw fe::Error("invalid CUDA t-SNE profile request");
     fe::TsneJob& J = plan->job;
     cudaStream_t s = J.stream.s;
+    if (fe::reorder_enabled()) fe::tsne_reorder(J.D, J.P, s);
     std::vector<cudaEvent_t> ev(4 * (std::size_t)iters);
     for (auto& e : ev) FE_CUDA(cudaEventCreate(&e));
     for (int it = 0; it < iters; ++it) {

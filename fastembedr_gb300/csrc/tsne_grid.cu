@@ -20,6 +20,7 @@
 // Interpolation: the reference bilinear splat on G shared nodes, or (default) 3 equispaced
 // Lagrange nodes per box over floor(G / 3) boxes, as in FIt-SNE-style interpolation.
 #include <cfloat>
+#include <climits>
 #include <cmath>
 #include <vector>
 
@@ -192,53 +193,89 @@ layout_stats_kernel(const float2* __restrict__ ynew, int n, int grid, int mode, 
 
 // ---------------------------------------------------------------- scatter
 // Each point adds (w, w*(x - cx), w*(y - cy)) to its TAPS x TAPS stencil nodes; block 0 also
-// promotes the grid computed by the previous update (`next`) to `cur`. Points are stored in
-// spatial order, so lanes of a warp often share a stencil anchor: runs of equal anchors are
-// summed with a segmented warp reduction and only the run head issues the vector atomics,
-// which removes the hot-node contention when clusters collapse onto a few grid cells.
+// promotes the grid computed by the previous update (`next`) to `cur`.
+// Points are stored in spatial (Morton) order and every block takes 256 consecutive points, so
+// a block covers a compact patch of the grid even when clusters collapse onto a few cells:
+//   1. runs of equal stencil anchors inside a warp are summed by a segmented shuffle reduction;
+//   2. run heads accumulate into a kTile x kTile node tile in shared memory anchored at the
+//      block's lowest anchor (heads outside the tile go straight to global memory);
+//   3. the tile is flushed with one float4 vector atomic per touched node.
+constexpr int kScatterTile = 32;
+
 template <int TAPS>
 __global__ void __launch_bounds__(256)
 scatter_kernel(const float2* __restrict__ y, int n, int grid, GridState* __restrict__ cur,
                const GridState* __restrict__ next, float4* __restrict__ charges) {
   constexpr int NV = TAPS * TAPS * 3;
+  __shared__ float tile[kScatterTile * kScatterTile * 3];
+  __shared__ int s_box[4];
   const GridState g = *next;
   if (blockIdx.x == 0 && threadIdx.x == 0) *cur = g;
   const int lane = threadIdx.x & 31;
-  for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n; base += gridDim.x * blockDim.x) {
-    const int i = base + lane;
-    const bool valid = i < n;
-    const float2 p = valid ? y[i] : make_float2(g.cx, g.cy);
-    const Stencil<TAPS> sx = make_stencil<TAPS>(p.x, g.x0, g.inv_h, g.inv_box, g.nodes);
-    const Stencil<TAPS> sy = make_stencil<TAPS>(p.y, g.y0, g.inv_h, g.inv_box, g.nodes);
-    const float dx = p.x - g.cx, dy = p.y - g.cy;
-    float v[NV];
+  for (int t = threadIdx.x; t < kScatterTile * kScatterTile * 3; t += blockDim.x) tile[t] = 0.0f;
+  if (threadIdx.x == 0) {
+    s_box[0] = INT_MAX;
+    s_box[1] = INT_MAX;
+    s_box[2] = -1;
+    s_box[3] = -1;
+  }
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = i < n;
+  const float2 p = valid ? y[i] : make_float2(g.cx, g.cy);
+  const Stencil<TAPS> sx = make_stencil<TAPS>(p.x, g.x0, g.inv_h, g.inv_box, g.nodes);
+  const Stencil<TAPS> sy = make_stencil<TAPS>(p.y, g.y0, g.inv_h, g.inv_box, g.nodes);
+  const float dx = p.x - g.cx, dy = p.y - g.cy;
+  float v[NV];
 #pragma unroll
-    for (int a = 0; a < TAPS; ++a)
+  for (int a = 0; a < TAPS; ++a)
 #pragma unroll
-      for (int b = 0; b < TAPS; ++b) {
-        const float w = valid ? sy.w[a] * sx.w[b] : 0.0f;
-        v[(a * TAPS + b) * 3 + 0] = w;
-        v[(a * TAPS + b) * 3 + 1] = w * dx;
-        v[(a * TAPS + b) * 3 + 2] = w * dy;
-      }
-    const int key = valid ? sy.base * grid + sx.base : -1 - lane;
-    const int prev = __shfl_up_sync(0xffffffffu, key, 1);
-    const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || prev != key);
-    if (heads != 0xffffffffu) {
-      // suffix sums restricted to contiguous runs [lane, next head)
-      const unsigned above = heads & ~((2u << lane) - 1u);
-      const int run_end = above ? __ffs(above) - 1 : 32;
+    for (int b = 0; b < TAPS; ++b) {
+      const float w = valid ? sy.w[a] * sx.w[b] : 0.0f;
+      v[(a * TAPS + b) * 3 + 0] = w;
+      v[(a * TAPS + b) * 3 + 1] = w * dx;
+      v[(a * TAPS + b) * 3 + 2] = w * dy;
+    }
+  const int key = valid ? sy.base * grid + sx.base : -1 - lane;
+  const int prev = __shfl_up_sync(0xffffffffu, key, 1);
+  const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || prev != key);
+  if (heads != 0xffffffffu) {
+    // suffix sums restricted to contiguous runs [lane, next head)
+    const unsigned above = heads & ~((2u << lane) - 1u);
+    const int run_end = above ? __ffs(above) - 1 : 32;
 #pragma unroll
-      for (int off = 1; off < 32; off <<= 1) {
-        const bool take = lane + off < run_end;
+    for (int off = 1; off < 32; off <<= 1) {
+      const bool take = lane + off < run_end;
 #pragma unroll
-        for (int c = 0; c < NV; ++c) {
-          const float o = __shfl_down_sync(0xffffffffu, v[c], off);
-          if (take) v[c] += o;
-        }
+      for (int c = 0; c < NV; ++c) {
+        const float o = __shfl_down_sync(0xffffffffu, v[c], off);
+        if (take) v[c] += o;
       }
     }
-    if (valid && ((heads >> lane) & 1u)) {
+  }
+  const bool head = valid && ((heads >> lane) & 1u);
+  __syncthreads();
+  if (head) {
+    atomicMin(&s_box[0], sx.base);
+    atomicMin(&s_box[1], sy.base);
+    atomicMax(&s_box[2], sx.base);
+    atomicMax(&s_box[3], sy.base);
+  }
+  __syncthreads();
+  const int ox = s_box[0], oy = s_box[1];
+  if (head) {
+    const int tx = sx.base - ox, ty = sy.base - oy;
+    if (tx + TAPS <= kScatterTile && ty + TAPS <= kScatterTile) {
+#pragma unroll
+      for (int a = 0; a < TAPS; ++a)
+#pragma unroll
+        for (int b = 0; b < TAPS; ++b) {
+          float* t = tile + ((ty + a) * kScatterTile + tx + b) * 3;
+          const int c = (a * TAPS + b) * 3;
+          atomicAdd(t, v[c]);
+          atomicAdd(t + 1, v[c + 1]);
+          atomicAdd(t + 2, v[c + 2]);
+        }
+    } else {
 #pragma unroll
       for (int a = 0; a < TAPS; ++a) {
         float4* row = charges + (long long)(sy.base + a) * grid + sx.base;
@@ -249,6 +286,17 @@ scatter_kernel(const float2* __restrict__ y, int n, int grid, GridState* __restr
         }
       }
     }
+  }
+  __syncthreads();
+  if (s_box[2] < 0) return;  // no valid point in this block
+  const int wu = min(kScatterTile, s_box[2] - ox + TAPS);
+  const int hu = min(kScatterTile, s_box[3] - oy + TAPS);
+  for (int t = threadIdx.x; t < wu * hu; t += blockDim.x) {
+    const int r = t / wu, c = t - r * wu;
+    const float* src = tile + (r * kScatterTile + c) * 3;
+    const float a0 = src[0], a1 = src[1], a2 = src[2];
+    if (a0 != 0.0f || a1 != 0.0f || a2 != 0.0f)
+      atomicAdd(charges + (long long)(oy + r) * grid + ox + c, make_float4(a0, a1, a2, 0.0f));
   }
 }
 
@@ -517,43 +565,68 @@ rows_inverse_kernel(const float2* __restrict__ rows, int grid, int nodes, int lo
 }
 
 // ---------------------------------------------------------------- attractive pass
-// One warp per point (storage slot i visits CSR row perm[i]), strided over a persistent grid:
-//   a_i = exag * sum_j p_ij q_ij (y_i - y_j), q = 1 / (1 + d^2)
-// (add_sparse_attractive_gradient_f, src/tsne_neighbors.cpp:1061-1088). Column / value loads
-// are streaming (coalesced, not kept in L1); the y gathers hit the L2-resident layout. Rows
-// longer than 256 entries accumulate with per-lane compensated (Kahan) sums.
+// a_i = exag * sum_j p_ij q_ij (y_i - y_j), q = 1 / (1 + d^2)
+// (add_sparse_attractive_gradient_f, src/tsne_neighbors.cpp:1061-1088).
+// Each warp owns a contiguous range of CSR rows (original point order), so the whole grid
+// streams P front to back. A row of up to 256 entries is covered by one round of 8 independent
+// coalesced loads per lane; lane 0 keeps a bulk L2 prefetch (cp.async.bulk.prefetch) running
+// kAttrAhead rows ahead, so the column/value loads of later rows hit L2 without holding
+// registers. Columns are storage slots (spatially sorted), so the y gathers of one row fall
+// into few sectors. Rows longer than 256 entries accumulate with per-lane Kahan sums.
 constexpr int kAttrThreads = 256;
+constexpr int kAttrAhead = 3;
+
+__device__ __forceinline__ void prefetch_l2_range(const void* base, long long first, long long last, int elem) {
+  // [first, last) elements of a 4-byte array, widened to 16-byte boundaries (the arena pads
+  // every buffer to 256 bytes, so the widened range stays inside the allocation)
+  if (last <= first) return;
+  const unsigned long long a = (unsigned long long)base + (unsigned long long)(first * elem);
+  const unsigned long long e = (unsigned long long)base + (unsigned long long)(last * elem);
+  const unsigned long long a16 = a & ~15ull, e16 = (e + 15ull) & ~15ull;
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a16), "r"((unsigned)(e16 - a16)) : "memory");
+}
 
 __global__ void __launch_bounds__(kAttrThreads)
 attractive_kernel(const int* __restrict__ row_ptr, const int* __restrict__ col, const float* __restrict__ val,
-                  const float2* __restrict__ y, const int* __restrict__ perm, int n, float exag,
+                  const float2* __restrict__ y, const int* __restrict__ inv, int n, float exag,
                   float2* __restrict__ attr) {
   const int lane = threadIdx.x & 31;
-  const int warps_total = gridDim.x * (blockDim.x >> 5);
-  for (int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps_total) {
-    const int row = perm ? __ldg(perm + i) : i;
-    const int b = __ldg(row_ptr + row), e = __ldg(row_ptr + row + 1);
-    const float2 yi = __ldg(y + i);
+  const long long warps_total = (long long)gridDim.x * (blockDim.x >> 5);
+  const long long w = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int r0 = (int)(w * n / warps_total), r1 = (int)((w + 1) * n / warps_total);
+  if (lane == 0 && r0 < r1) {
+    const int pe = min(r1, r0 + kAttrAhead);
+    prefetch_l2_range(col, row_ptr[r0], row_ptr[pe], 4);
+    prefetch_l2_range(val, row_ptr[r0], row_ptr[pe], 4);
+  }
+  for (int i = r0; i < r1; ++i) {
+    if (lane == 0 && i + kAttrAhead < r1) {
+      const int j = i + kAttrAhead;
+      const int pb = __ldg(row_ptr + j), pe = __ldg(row_ptr + j + 1);
+      prefetch_l2_range(col, pb, pe, 4);
+      prefetch_l2_range(val, pb, pe, 4);
+    }
+    const int b = __ldg(row_ptr + i), e = __ldg(row_ptr + i + 1);
+    const int si = inv ? __ldg(inv + i) : i;
+    const float2 yi = __ldg(y + si);
     float ax = 0.0f, ay = 0.0f;
     if (e - b <= 256) {
-      for (int p = b + lane; p < e; p += 128) {
-        int ci[4];
-        float v[4];
+      int ci[8];
+      float v[8];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int q = p + 32 * u;
-          ci[u] = q < e ? __ldcs(col + q) : i;
-          v[u] = q < e ? __ldcs(val + q) : 0.0f;
-        }
+      for (int u = 0; u < 8; ++u) {
+        const int q = b + lane + 32 * u;
+        ci[u] = q < e ? __ldcs(col + q) : si;
+        v[u] = q < e ? __ldcs(val + q) : 0.0f;
+      }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const float2 yj = __ldg(y + ci[u]);
-          const float dx = yi.x - yj.x, dy = yi.y - yj.y;
-          const float q = 1.0f / (1.0f + (dx * dx + dy * dy));
-          const float c = exag * v[u] * q;
-          ax += c * dx;
-          ay += c * dy;
-        }
+      for (int u = 0; u < 8; ++u) {
+        const float2 yj = __ldg(y + ci[u]);
+        const float dx = yi.x - yj.x, dy = yi.y - yj.y;
+        const float q = 1.0f / (1.0f + (dx * dx + dy * dy));
+        const float c = exag * v[u] * q;
+        ax += c * dx;
+        ay += c * dy;
       }
     } else {
       float kx = 0.0f, ky = 0.0f;
@@ -574,7 +647,7 @@ attractive_kernel(const int* __restrict__ row_ptr, const int* __restrict__ col, 
     }
     ax = warp_sum(ax);
     ay = warp_sum(ay);
-    if (lane == 0) attr[i] = make_float2(ax, ay);
+    if (lane == 0) attr[si] = make_float2(ax, ay);
   }
 }
 
@@ -846,9 +919,9 @@ void tsne_device_init(TsneDevice& d, const float* d_init, cudaStream_t s) {
 void tsne_grid_stage(TsneDevice& d, cudaStream_t s) {
   const int m = d.fft;
   if (d.mode == kInterpBilinear)
-    scatter_kernel<2><<<point_blocks(d.n), 256, 0, s>>>(d.y, d.n, d.grid, d.cur, d.next, d.charges);
+    scatter_kernel<2><<<ceil_div(d.n, 256), 256, 0, s>>>(d.y, d.n, d.grid, d.cur, d.next, d.charges);
   else
-    scatter_kernel<3><<<point_blocks(d.n), 256, 0, s>>>(d.y, d.n, d.grid, d.cur, d.next, d.charges);
+    scatter_kernel<3><<<ceil_div(d.n, 256), 256, 0, s>>>(d.y, d.n, d.grid, d.cur, d.next, d.charges);
   FE_LAUNCH("scatter_kernel");
   rows_forward_kernel<<<2 * d.nodes, kFftThreads, 2 * m * sizeof(float2), s>>>(d.charges, d.grid, d.nodes,
                                                                                 d.log_fft, d.twiddle, d.cur,
@@ -864,7 +937,7 @@ void tsne_grid_stage(TsneDevice& d, cudaStream_t s) {
 }
 
 void tsne_attractive_stage(TsneDevice& d, const DeviceCsr& P, float exag, cudaStream_t s) {
-  attractive_kernel<<<d.attr_blocks, kAttrThreads, 0, s>>>(P.row_ptr, P.col, P.val, d.y, d.perm, d.n, exag,
+  attractive_kernel<<<d.attr_blocks, kAttrThreads, 0, s>>>(P.row_ptr, P.col, P.val, d.y, d.inv, d.n, exag,
                                                            d.attr);
   FE_LAUNCH("attractive_kernel");
 }

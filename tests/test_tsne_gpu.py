@@ -161,21 +161,34 @@ def test_invalid_inputs_are_rejected(golden):
         api.tsne_force_diagnostic(g["idx"], g["dist"], layout, 2.0)
 
 
-def test_end_to_end_plain_10k_kl_and_preservation(c1):
-    """(d): full 250 + 750 iteration run vs the reference CPU run (oracle, bit-identical to it)."""
+def test_end_to_end_plain_10k_kl_and_preservation(c1, monkeypatch):
+    """(d): full 250 + 750 iteration run vs the reference CPU run (the oracle, bit-identical to it).
+
+    At the reference CPU's own grid (bilinear, 128 nodes for n < 50k) the GPU run must match it
+    two-sided: KL within 1 %, 15-NN preservation within 0.01. With the default CUDA grid policy
+    (256 nodes, as the reference CUDA backend) the GPU run may only be better: KL at most 1 %
+    above, preservation at most 0.01 below."""
     idx, dist, _ = c1
     n = idx.shape[0]
     init = synthetic.tsne_init(n, 7)
-    fit = api.tsne_knn(idx, dist, perplexity=30, Y_init=init, early_exaggeration_iter=250, n_iter=750)
     cpu = O.tsne_run(idx, dist, init, perplexity=30, early_iter=250, n_iter=750, learning_rate=n / 12.0)
     rp, col, val, _ = O.tsne_csr(idx, dist, 30.0)
-    kl_gpu = O.kl(rp, col, val, fit.layout)
-    kl_cpu = O.kl(rp, col, val, cpu)
-    assert abs(kl_gpu - kl_cpu) / kl_cpu < 0.01, (kl_gpu, kl_cpu)
     keep = np.arange(0, n, 5, dtype=np.int32)
-    pg = O.knn_preservation(fit.layout, idx, keep=keep, preserve_k=15)
+    kl_cpu = O.kl(rp, col, val, cpu)
     pc = O.knn_preservation(cpu, idx, keep=keep, preserve_k=15)
+    monkeypatch.setenv("FASTEMBEDR_TSNE_FFT_GRID", "128")
+    fit = api.tsne_knn(idx, dist, perplexity=30, Y_init=init, early_exaggeration_iter=250, n_iter=750)
+    kl_gpu = O.kl(rp, col, val, fit.layout)
+    pg = O.knn_preservation(fit.layout, idx, keep=keep, preserve_k=15)
+    assert abs(kl_gpu - kl_cpu) / kl_cpu < 0.01, (kl_gpu, kl_cpu)
     assert abs(pg - pc) < 0.01, (pg, pc)
+    monkeypatch.delenv("FASTEMBEDR_TSNE_FFT_GRID")
+    fit = api.tsne_knn(idx, dist, perplexity=30, Y_init=init, early_exaggeration_iter=250, n_iter=750)
+    assert fit.config["fft_grid_size"] == 256
+    kl_d = O.kl(rp, col, val, fit.layout)
+    pd = O.knn_preservation(fit.layout, idx, keep=keep, preserve_k=15)
+    assert kl_d < kl_cpu * 1.01, (kl_d, kl_cpu)
+    assert pd > pc - 0.01, (pd, pc)
 
 
 def test_plan_graph_and_eager_paths_agree(small):
