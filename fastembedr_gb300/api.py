@@ -138,7 +138,7 @@ def tsne_affinities(indices, distances, perplexity, index_offset=None):
     return dict(row_ptr=rp, col=col[:m].copy(), val=val[:m].copy(), p_directed=p, entropy=h, total_mass=tot.value)
 
 
-def tsne_force_diagnostic(indices, distances, layout, perplexity, exaggeration=1.0, grid_size=0, interpolation=1,
+def tsne_force_diagnostic(indices, distances, layout, perplexity, exaggeration=1.0, grid_size=0, interpolation=0,
                           exact=True, kl=True, index_offset=None):
     """GPU twin of opentsne_force_diagnostic_cpp (src/tsne_neighbors.cpp:1698-1817)."""
     idx = np.asarray(indices)
@@ -173,7 +173,7 @@ class TsnePlan:
     """
 
     def __init__(self, d_indices_cm, d_distances_cm, n, k, perplexity, init=None, index_offset=0, grid_size=0,
-                 interpolation=1, seed=4):
+                 interpolation=0, seed=4):
         self.lib = _lib.require_gpu()
         self.n = int(n)
         h = C.c_void_p()
