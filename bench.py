@@ -233,7 +233,8 @@ def run_gpu(args):
 
     if args.no_e2e:
         if rank == 0:
-            print(json.dumps({"metric": "tsne_iterations_per_s", "n": n, "value": value, "ms_per_step": ms / args.steps,
+            print(json.dumps({"metric": "tsne_iterations_per_s", "n": n, "nnz": info["nnz"], "value": value,
+                              "ms_per_step": ms / args.steps,
                               "stage_ms_per_step": {k_: v / args.steps for k_, v in prof.items()}}))
         return 0
     # end to end through the reference C ABI with pinned host buffers, full 1000-iteration job
