@@ -34,6 +34,9 @@ SIGNATURES = {
     "fastembedr_cuda_tsne_affinities": (I, [vp, vp, I, I, F, I, vp, vp, vp, L, C.POINTER(L), vp, vp, C.POINTER(D)]),
     "fastembedr_cuda_tsne_force_diagnostic": (I, [vp, vp, vp, I, I, F, F, I, I, I, vp, vp, C.POINTER(D), vp,
                                                   C.POINTER(D), C.POINTER(D)]),
+    "fastembedr_cuda_umap_optimize_coo": (I, [vp, vp, vp, vp, vp, I, I, I, I, F, F, F, F, U, I, vp]),
+    "fastembedr_cuda_umap_graph_from_knn": (I, [vp, vp, I, I, I, vp, vp, vp, vp, L, C.POINTER(L), C.POINTER(F)]),
+    "fastembedr_cuda_umap_from_knn": (I, [vp, vp, vp, I, I, I, I, I, F, F, F, U, vp]),
     "fastembedr_cuda_tsne_exact_repulsion_noalloc": (I, [vp, I, vp, vp, vp]),
     "fastembedr_tsne_plan_create": (I, [vp, vp, vp, I, I, F, I, I, I, U, C.POINTER(vp)]),
     "fastembedr_tsne_plan_run": (I, [vp, I, F, F, F, F, F, I]),

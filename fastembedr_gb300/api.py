@@ -231,3 +231,81 @@ class TsnePlan:
             self.close()
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------------------- UMAP
+@dataclass
+class UmapFit:
+    layout: np.ndarray
+    config: dict = field(default_factory=dict)
+
+
+def umap_graph(indices, distances, index_offset=None):
+    """Default fuzzy graph on the GPU (umap_graph_csr_float_cpp, src/fast_knn_umap.cpp:3996)."""
+    idx = np.asarray(indices)
+    n, k = idx.shape
+    off = knn_index_offset(idx) if index_offset is None else int(index_offset)
+    cap = 2 * n * k
+    offsets = np.zeros(n + 1, np.int32)
+    nb = np.zeros(cap, np.int32)
+    w = np.zeros(cap, np.float32)
+    e = np.zeros(cap, np.float32)
+    nnz, mw = C.c_longlong(), C.c_float()
+    lib = _lib.require_gpu()
+    idx_cm, dist_cm = _colmajor(idx, np.int32), _colmajor(distances, np.float32)
+    st = lib.fastembedr_cuda_umap_graph_from_knn(idx_cm.ctypes.data, dist_cm.ctypes.data, n, k, off,
+                                                 offsets.ctypes.data, nb.ctypes.data, w.ctypes.data, e.ctypes.data,
+                                                 cap, C.byref(nnz), C.byref(mw))
+    _lib.check(st, "CUDA UMAP graph")
+    m = nnz.value
+    return dict(offsets=offsets, neighbors=nb[:m].copy(), weights=w[:m].copy(), epochs_per_sample=e[:m].copy(),
+                max_weight=mw.value)
+
+
+def umap_optimize_coo(heads, tails, weights, epochs_per_sample, init, n_epochs, a, b, negative_sample_rate=5,
+                      learning_rate=1.0, repulsion_strength=1.0, seed=42):
+    """The reference C ABI entry fastembedr_cuda_umap_optimize_coo on host arrays."""
+    h = np.ascontiguousarray(heads, np.int32)
+    t = np.ascontiguousarray(tails, np.int32)
+    w = np.ascontiguousarray(weights, np.float32)
+    e = np.ascontiguousarray(epochs_per_sample, np.float32)
+    y0 = np.ascontiguousarray(init, np.float32)
+    out = np.zeros_like(y0)
+    lib = _lib.require_gpu()
+    st = lib.fastembedr_cuda_umap_optimize_coo(h.ctypes.data, t.ctypes.data, w.ctypes.data, e.ctypes.data,
+                                               y0.ctypes.data, y0.shape[0], h.size, int(n_epochs),
+                                               int(negative_sample_rate), float(learning_rate), float(a), float(b),
+                                               float(repulsion_strength), int(seed) & 0xFFFFFFFF, 0, out.ctypes.data)
+    _lib.check(st, "CUDA COO UMAP optimizer")
+    return out
+
+
+def umap_knn(indices, distances, init, n_components=2, seed=42, n_epochs=None, min_dist=0.01,
+             negative_sample_rate=5, learning_rate=1.0, repulsion_strength=1.0, backend="cuda") -> UmapFit:
+    """UMAP from a supplied KNN graph (R/fast_knn_umap.R:1444-1462 with the package policy of
+    fast_knn_umap_config, :1008-1032: 200 epochs at n >= 10k else 500, min_dist 0.01, negative
+    rate 5, lr 1, repulsion 1). The initial layout is supplied by the caller (the reference feeds
+    the same CPU spectral initialisation to every backend)."""
+    if backend != "cuda":
+        raise ValueError("fastembedr_gb300 implements backend = 'cuda' only")
+    if int(n_components) != 2:
+        raise ValueError("CUDA UMAP requires a two-dimensional initialization.")
+    idx = np.asarray(indices)
+    n, k = idx.shape
+    epochs = (200 if n >= 10000 else 500) if n_epochs is None else int(n_epochs)
+    y0 = np.ascontiguousarray(init, np.float32)
+    if y0.shape != (n, 2):
+        raise ValueError("init row count must match the KNN graph")
+    out = np.zeros((n, 2), np.float32)
+    lib = _lib.require_gpu()
+    idx_cm, dist_cm = _colmajor(idx, np.int32), _colmajor(distances, np.float32)
+    st = lib.fastembedr_cuda_umap_from_knn(idx_cm.ctypes.data, dist_cm.ctypes.data, y0.ctypes.data, n, k,
+                                           knn_index_offset(idx), epochs, int(negative_sample_rate),
+                                           float(learning_rate), float(min_dist), float(repulsion_strength),
+                                           int(seed) & 0xFFFFFFFF, out.ctypes.data)
+    _lib.check(st, "CUDA UMAP")
+    config = dict(method="umap", backend="cuda", n=n, k=k, n_epochs=epochs, min_dist=float(min_dist),
+                  negative_sample_rate=int(negative_sample_rate), learning_rate=float(learning_rate),
+                  repulsion_strength=float(repulsion_strength), graph_mode="native_csr_graph",
+                  graph_prep_backend="cuda_fuzzy_csr", optimizer_math="coo_atomic_edge_sampler_philox", seed=int(seed))
+    return UmapFit(out, config)

@@ -19,6 +19,7 @@
 #include <cmath>
 #include <cstdlib>
 
+#include "sort.cuh"
 #include "tsne.cuh"
 
 namespace fe {
@@ -289,42 +290,6 @@ __global__ void fill_buckets_kernel(const int* __restrict__ idx, const float* __
 
 constexpr int kSortThreads = 256;
 constexpr int kSortCap = 8192;  // entries of a row sorted in shared memory
-
-// Always-ascending bitonic network over `pw` (power of two) slots; compare(i, j) keeps the
-// minimum at i. Slots at or beyond `len` hold +inf (explicitly in shared memory, virtually
-// in global memory), which this formulation never moves below a real key.
-template <bool kGlobal>
-__device__ void bitonic_sort(unsigned long long* a, int len, int pw) {
-  for (int size = 2; size <= pw; size <<= 1) {
-    const int half = size >> 1;
-    for (int t = threadIdx.x; t < pw / 2; t += blockDim.x) {
-      const int blk = t / half, off = t % half;
-      const int i = blk * size + off, j = blk * size + size - 1 - off;
-      if (!kGlobal || j < len) {
-        const unsigned long long x = a[i], y = a[j];
-        if (y < x) {
-          a[i] = y;
-          a[j] = x;
-        }
-      }
-    }
-    __syncthreads();
-    for (int stride = half >> 1; stride > 0; stride >>= 1) {
-      for (int t = threadIdx.x; t < pw / 2; t += blockDim.x) {
-        const int blk = t / stride, off = t % stride;
-        const int i = blk * 2 * stride + off, j = i + stride;
-        if (!kGlobal || j < len) {
-          const unsigned long long x = a[i], y = a[j];
-          if (y < x) {
-            a[i] = y;
-            a[j] = x;
-          }
-        }
-      }
-      __syncthreads();
-    }
-  }
-}
 
 // Sort each row bucket by (column, p bits); rows above kSortCap are queued for the
 // global-memory path. Then collapse runs of equal columns: the compacted (column, float(sum))

@@ -1,0 +1,698 @@
+// UMAP on the GPU: the fuzzy-union graph built from a supplied KNN graph and the SGD epochs.
+//
+// Reference behaviour followed (fastEmbedR):
+//   - smooth_knn_dist, src/fast_knn_umap.cpp:876-1003 (rho = smallest positive distance,
+//     sigma bisection to log2(k), best-diff kept, sigma floor 1e-3 * mean distance);
+//   - build_graph_csr_native_direct_values, :1562-1780 with compact_directed_rows_inplace
+//     (:1284-1365) and attach_csr_epoch_schedule (:1264-1282): directed weights
+//     exp(-(d - rho) / sigma), duplicates kept at their maximum, union f + r - f r, entries
+//     <= 1e-6 dropped, epochs_per_sample = max_w / max(w, 1e-6);
+//   - the COO epoch of fastembedr_cuda_umap_optimize_coo, src/embedding_cuda_kernels.cpp:5483-5608
+//     (positive/negative schedules :3044-3084, attractive/repulsive coefficients with the
+//     Schraudolph power :364-407, gradient clip 4, linear learning-rate decay, clamp to +-16
+//     after each epoch, epoch 0 inactive).
+// GB300 layout: the graph is built by the same row-bucket + bitonic sort machinery as the
+// t-SNE P; the epoch is one persistent grid-stride kernel over head-sorted COO edges with float2
+// vector atomics, negative samples drawn from per-(edge, epoch) Philox4x32-10 streams, and the
+// epoch counter lives on the device so a captured CUDA graph of 25 epochs replays unchanged.
+#include <cfloat>
+#include <climits>
+#include <cmath>
+#include <map>
+#include <memory>
+
+#include "../../include/fastembedr_cuda.h"
+#include "philox.cuh"
+#include "sort.cuh"
+#include "tsne.cuh"
+
+namespace fe {
+
+// ---------------------------------------------------------------- smooth kNN
+__global__ void umap_distance_sum_kernel(const float* __restrict__ dist, long long total, double* __restrict__ acc) {
+  double s = 0.0;
+  unsigned long long c = 0;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+    const float d = dist[t];
+    if (isfinite(d) && d >= 0.0f) {
+      s += (double)d;
+      ++c;
+    }
+  }
+  s = warp_sum(s);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(acc, s);
+    atomicAdd(reinterpret_cast<unsigned long long*>(acc + 1), c);
+  }
+}
+
+// One warp per row; distances column-major n x k.
+__global__ void umap_smooth_knn_kernel(const float* __restrict__ dist, int n, int k, const double* __restrict__ acc,
+                                       float* __restrict__ sigmas, float* __restrict__ rhos) {
+  const int lane = threadIdx.x & 31;
+  const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (row >= n) return;
+  const unsigned long long cnt = reinterpret_cast<const unsigned long long*>(acc)[1];
+  const double global_mean = cnt > 0 ? acc[0] / (double)cnt : 1.0;
+  const double target = log2((double)k);
+  double rho = INFINITY, row_sum = 0.0;
+  int row_count = 0;
+  for (int j = lane; j < k; j += 32) {
+    const float d = dist[(long long)j * n + row];
+    if (!isfinite(d)) continue;
+    if (d >= 0.0f) {
+      row_sum += (double)d;
+      ++row_count;
+    }
+    if (d > 0.0f && (double)d < rho) rho = (double)d;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    rho = fmin(rho, __shfl_xor_sync(0xffffffffu, rho, o));
+    row_sum += __shfl_xor_sync(0xffffffffu, row_sum, o);
+    row_count += __shfl_xor_sync(0xffffffffu, row_count, o);
+  }
+  if (!isfinite(rho)) rho = 0.0;
+  double sigma = 1.0, sigma_best = 1.0, best_diff = DBL_MAX, lo = 0.0, hi = DBL_MAX;
+  for (int it = 0; it < 64; ++it) {
+    const double safe = fmax(sigma, 1.0e-12);
+    double psum = 0.0;
+    for (int j = lane; j < k; j += 32) {
+      const float raw = dist[(long long)j * n + row];
+      if (!isfinite(raw)) continue;
+      const double d = (double)raw - rho;
+      psum += d <= 0.0 ? 1.0 : exp(-d / safe);
+    }
+    psum = warp_sum(psum);
+    const double diff = fabs(psum - target);
+    if (diff < best_diff) {
+      best_diff = diff;
+      sigma_best = sigma;
+    }
+    if (psum > target) {
+      hi = sigma;
+      sigma = 0.5 * (lo + hi);
+    } else {
+      lo = sigma;
+      sigma = hi == DBL_MAX ? sigma * 2.0 : 0.5 * (lo + hi);
+    }
+    if (diff < 1.0e-5) break;
+  }
+  if (lane == 0) {
+    const double row_mean = row_count > 0 ? row_sum / (double)row_count : global_mean;
+    const double floor_s = 1.0e-3 * (rho > 0.0 ? row_mean : global_mean);
+    sigma_best = fmax(sigma_best, floor_s);
+    rhos[row] = (float)rho;
+    sigmas[row] = (float)fmax(sigma_best, 1.0e-12);
+  }
+}
+
+// ---------------------------------------------------------------- fuzzy union graph
+__device__ __forceinline__ bool directed_weight(const int* __restrict__ idx, const float* __restrict__ dist,
+                                                const float* __restrict__ sig, const float* __restrict__ rho,
+                                                int n, int offset, long long t, int& i, int& nb, float& w) {
+  i = (int)(t % n);
+  nb = idx[t] - offset;
+  const float d = dist[t];
+  if (nb < 0 || nb >= n || nb == i || !isfinite(d)) return false;
+  w = d <= rho[i] ? 1.0f : expf(-(d - rho[i]) / sig[i]);
+  return isfinite(w) && w > 0.0f;
+}
+
+__global__ void umap_count_kernel(const int* __restrict__ idx, const float* __restrict__ dist,
+                                  const float* __restrict__ sig, const float* __restrict__ rho, int n, int k, int offset,
+                                  int* __restrict__ counts) {
+  const long long total = (long long)n * k;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+    int i, nb;
+    float w;
+    if (!directed_weight(idx, dist, sig, rho, n, offset, t, i, nb, w)) continue;
+    atomicAdd(counts + i, 1);
+    atomicAdd(counts + nb, 1);
+  }
+}
+
+// bucket key: column (high word), direction bit 31 (0 = i -> col, 1 = col -> i), weight bits
+__global__ void umap_fill_kernel(const int* __restrict__ idx, const float* __restrict__ dist,
+                                 const float* __restrict__ sig, const float* __restrict__ rho, int n, int k, int offset,
+                                 unsigned long long* __restrict__ cursor, unsigned long long* __restrict__ bucket) {
+  const long long total = (long long)n * k;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+    int i, nb;
+    float w;
+    if (!directed_weight(idx, dist, sig, rho, n, offset, t, i, nb, w)) continue;
+    const unsigned long long wb = (unsigned long long)__float_as_uint(w);
+    bucket[atomicAdd(cursor + i, 1ull)] = ((unsigned long long)(unsigned)nb << 32) | wb;
+    bucket[atomicAdd(cursor + nb, 1ull)] = ((unsigned long long)(unsigned)i << 32) | 0x80000000ull | wb;
+  }
+}
+
+// Forward / reverse weights of one column run [t, end): the maximum per direction (duplicates
+// of a directed edge keep their maximum), then the fuzzy union.
+__device__ __forceinline__ float union_weight(const unsigned long long* a, int t, int len, unsigned col, int* end) {
+  float f = 0.0f, r = 0.0f;
+  int u = t;
+  for (; u < len && (unsigned)(a[u] >> 32) == col; ++u) {
+    const unsigned lo = (unsigned)a[u];
+    const float w = __uint_as_float(lo & 0x7fffffffu);
+    if (lo & 0x80000000u) r = fmaxf(r, w);
+    else f = fmaxf(f, w);
+  }
+  *end = u;
+  return f + r - f * r;
+}
+
+constexpr int kUmapSortThreads = 256;
+constexpr int kUmapSortCap = 4096;
+
+__global__ void __launch_bounds__(kUmapSortThreads)
+umap_union_rows_kernel(unsigned long long* __restrict__ bucket, const long long* __restrict__ offs, int n,
+                       int* __restrict__ ucount, float* __restrict__ row_max, int* __restrict__ big_rows,
+                       int* __restrict__ big_count) {
+  extern __shared__ unsigned long long sm[];
+  __shared__ int warp_cnt[kUmapSortThreads / 32];
+  __shared__ float s_wmax[kUmapSortThreads / 32];
+  for (int row = blockIdx.x; row < n; row += gridDim.x) {
+    const long long b = offs[row];
+    const int len = (int)(offs[row + 1] - b);
+    if (len > kUmapSortCap) {
+      if (threadIdx.x == 0) big_rows[atomicAdd(big_count, 1)] = row;
+      continue;
+    }
+    int pw = 1;
+    while (pw < len) pw <<= 1;
+    for (int t = threadIdx.x; t < pw; t += blockDim.x) sm[t] = t < len ? bucket[b + t] : ~0ull;
+    __syncthreads();
+    if (len > 1) bitonic_sort<false>(sm, len, pw);
+    int kept_before = 0;
+    float mymax = 0.0f;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int base = 0; base < len; base += blockDim.x) {
+      const int t = base + threadIdx.x;
+      bool keep = false;
+      float w = 0.0f;
+      unsigned col = 0u;
+      if (t < len && (t == 0 || (sm[t] >> 32) != (sm[t - 1] >> 32))) {
+        col = (unsigned)(sm[t] >> 32);
+        int end;
+        w = union_weight(sm, t, len, col, &end);
+        keep = isfinite(w) && w > 1.0e-6f;
+      }
+      const unsigned ballot = __ballot_sync(0xffffffffu, keep);
+      if (lane == 0) warp_cnt[warp] = __popc(ballot);
+      __syncthreads();
+      int before = 0, total = 0;
+      for (int wi = 0; wi < (int)(blockDim.x / 32); ++wi) {
+        if (wi < warp) before += warp_cnt[wi];
+        total += warp_cnt[wi];
+      }
+      if (keep) {
+        const int pos = kept_before + before + __popc(ballot & ((1u << lane) - 1u));
+        bucket[b + pos] = ((unsigned long long)col << 32) | (unsigned long long)__float_as_uint(w);
+        mymax = fmaxf(mymax, w);
+      }
+      kept_before += total;
+      __syncthreads();
+    }
+    const float m = warp_max(mymax);
+    if (lane == 0) s_wmax[warp] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float mm = 0.0f;
+      for (int wi = 0; wi < (int)(blockDim.x / 32); ++wi) mm = fmaxf(mm, s_wmax[wi]);
+      row_max[row] = mm;
+      ucount[row] = kept_before;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(1024)
+umap_union_big_rows_kernel(unsigned long long* __restrict__ bucket, const long long* __restrict__ offs,
+                           const int* __restrict__ big_rows, const int* __restrict__ big_count,
+                           int* __restrict__ ucount, float* __restrict__ row_max) {
+  const int count = *big_count;
+  for (int r = blockIdx.x; r < count; r += gridDim.x) {
+    const int row = big_rows[r];
+    const long long b = offs[row];
+    const int len = (int)(offs[row + 1] - b);
+    int pw = 1;
+    while (pw < len) pw <<= 1;
+    bitonic_sort<true>(bucket + b, len, pw);
+    if (threadIdx.x == 0) {
+      int w_out = 0;
+      float mm = 0.0f;
+      for (int t = 0; t < len;) {
+        const unsigned col = (unsigned)(bucket[b + t] >> 32);
+        int end;
+        const float w = union_weight(bucket + b, t, len, col, &end);
+        t = end;
+        if (isfinite(w) && w > 1.0e-6f) {
+          bucket[b + w_out++] = ((unsigned long long)col << 32) | (unsigned long long)__float_as_uint(w);
+          mm = fmaxf(mm, w);
+        }
+      }
+      ucount[row] = w_out;
+      row_max[row] = mm;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void umap_max_kernel(const float* __restrict__ row_max, int n, float* __restrict__ out) {
+  __shared__ float part[1024];
+  float m = 0.0f;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) m = fmaxf(m, row_max[i]);
+  part[threadIdx.x] = m;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) part[threadIdx.x] = fmaxf(part[threadIdx.x], part[threadIdx.x + w]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = part[0];
+}
+
+__global__ void umap_fill_csr_kernel(const unsigned long long* __restrict__ bucket, const long long* __restrict__ offs,
+                                     const long long* __restrict__ out64, int n, const float* __restrict__ max_w,
+                                     int* __restrict__ offsets, int* __restrict__ heads, int* __restrict__ neighbors,
+                                     float* __restrict__ weights, float* __restrict__ eps) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp > n) return;
+  if (lane == 0) offsets[warp] = (int)out64[warp];
+  if (warp == n) return;
+  const float mw = *max_w;
+  const long long src = offs[warp], dst = out64[warp];
+  const int cnt = (int)(out64[warp + 1] - dst);
+  for (int t = lane; t < cnt; t += 32) {
+    const unsigned long long e = bucket[src + t];
+    const float w = __uint_as_float((unsigned)e);
+    if (heads) heads[dst + t] = warp;
+    neighbors[dst + t] = (int)(e >> 32);
+    weights[dst + t] = w;
+    eps[dst + t] = mw > 0.0f ? mw / fmaxf(w, 1.0e-6f) : INFINITY;
+  }
+}
+
+// Device fuzzy graph (CSR, ascending neighbours, plus the COO heads used by the epoch kernel).
+struct UmapGraph {
+  int n = 0;
+  long long nnz = 0;
+  float max_weight = 0.0f;
+  int* offsets = nullptr;
+  int* heads = nullptr;
+  int* neighbors = nullptr;
+  float* weights = nullptr;
+  float* eps = nullptr;
+  Arena arena;
+};
+
+void umap_build_graph(const int* d_idx, const float* d_dist, int n, int k, int offset, UmapGraph& g, cudaStream_t s) {
+  const long long directed = (long long)n * k;
+  const int nscan = std::max(1, ceil_div(n, 1024));
+  float *sig = nullptr, *rho = nullptr, *row_max = nullptr, *d_max = nullptr;
+  double* acc = nullptr;
+  int *counts = nullptr, *ucount = nullptr, *big_rows = nullptr, *big_count = nullptr;
+  long long *offs = nullptr, *scan_tmp = nullptr, *out64 = nullptr;
+  unsigned long long *cursor = nullptr, *bucket = nullptr;
+  Arena w;
+  w.reserve(&sig, n);
+  w.reserve(&rho, n);
+  w.reserve(&row_max, n);
+  w.reserve(&d_max, 1);
+  w.reserve(&acc, 2);
+  w.reserve(&counts, n);
+  w.reserve(&ucount, n);
+  w.reserve(&big_rows, n);
+  w.reserve(&big_count, 1);
+  w.reserve(&offs, n + 1);
+  w.reserve(&scan_tmp, nscan);
+  w.reserve(&out64, n + 1);
+  w.reserve(&cursor, n);
+  w.reserve(&bucket, 2 * directed);
+  w.commit("UMAP graph workspace");
+  const int grid = std::max(1, std::min(ceil_div(directed, 256), sm_count() * 16));
+  FE_CUDA(cudaMemsetAsync(acc, 0, 2 * sizeof(double), s));
+  FE_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * n, s));
+  FE_CUDA(cudaMemsetAsync(big_count, 0, sizeof(int), s));
+  umap_distance_sum_kernel<<<grid, 256, 0, s>>>(d_dist, directed, acc);
+  FE_LAUNCH("umap_distance_sum_kernel");
+  umap_smooth_knn_kernel<<<ceil_div((long long)n * 32, 256), 256, 0, s>>>(d_dist, n, k, acc, sig, rho);
+  FE_LAUNCH("umap_smooth_knn_kernel");
+  umap_count_kernel<<<grid, 256, 0, s>>>(d_idx, d_dist, sig, rho, n, k, offset, counts);
+  FE_LAUNCH("umap_count_kernel");
+  exclusive_scan(counts, offs, n, scan_tmp, s);
+  FE_CUDA(cudaMemcpyAsync(cursor, offs, sizeof(long long) * n, cudaMemcpyDeviceToDevice, s));
+  umap_fill_kernel<<<grid, 256, 0, s>>>(d_idx, d_dist, sig, rho, n, k, offset, cursor, bucket);
+  FE_LAUNCH("umap_fill_kernel");
+  const std::size_t smem = kUmapSortCap * sizeof(unsigned long long);
+  FE_CUDA(cudaFuncSetAttribute(umap_union_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  umap_union_rows_kernel<<<std::min(n, sm_count() * 8), kUmapSortThreads, smem, s>>>(bucket, offs, n, ucount, row_max,
+                                                                                     big_rows, big_count);
+  FE_LAUNCH("umap_union_rows_kernel");
+  umap_union_big_rows_kernel<<<sm_count(), 1024, 0, s>>>(bucket, offs, big_rows, big_count, ucount, row_max);
+  FE_LAUNCH("umap_union_big_rows_kernel");
+  exclusive_scan(ucount, out64, n, scan_tmp, s);
+  umap_max_kernel<<<1, 1024, 0, s>>>(row_max, n, d_max);
+  FE_LAUNCH("umap_max_kernel");
+  long long nnz = 0;
+  float mw = 0.0f;
+  FE_CUDA(cudaMemcpyAsync(&nnz, out64 + n, sizeof(long long), cudaMemcpyDeviceToHost, s));
+  FE_CUDA(cudaMemcpyAsync(&mw, d_max, sizeof(float), cudaMemcpyDeviceToHost, s));
+  FE_CUDA(cudaStreamSynchronize(s));
+  if (nnz <= 0 || !(mw > 0.0f)) throw Error("The CSR graph has no usable UMAP edges.");
+  if (nnz > INT_MAX) throw Error("UMAP graph exceeds 2^31 - 1 entries.");
+  g.n = n;
+  g.nnz = nnz;
+  g.max_weight = mw;
+  g.arena.release();
+  g.arena.reserve(&g.offsets, n + 1);
+  g.arena.reserve(&g.heads, nnz);
+  g.arena.reserve(&g.neighbors, nnz);
+  g.arena.reserve(&g.weights, nnz);
+  g.arena.reserve(&g.eps, nnz);
+  g.arena.commit("UMAP graph");
+  umap_fill_csr_kernel<<<ceil_div((long long)(n + 1) * 32, 256), 256, 0, s>>>(bucket, offs, out64, n, d_max, g.offsets,
+                                                                              g.heads, g.neighbors, g.weights, g.eps);
+  FE_LAUNCH("umap_fill_csr_kernel");
+  FE_CUDA(cudaStreamSynchronize(s));
+}
+
+// ---------------------------------------------------------------- SGD epoch
+struct UmapParams {
+  int n, n_epochs, negative_sample_rate;
+  unsigned seed;
+  float learning_rate, a, b, repulsion_strength;
+};
+
+// Positive-base power by IEEE-754 exponent interpolation (Schraudolph 1999), the approximation
+// the reference uses in its UMAP force terms (src/embedding_cuda_kernels.cpp:364-383).
+__device__ __forceinline__ float schraudolph_pow(float x, float b) {
+  if (x <= 0.0f) return 0.0f;
+  const float bias = 1064866805.0f;
+  const int whole = (int)b;
+  const float frac = b - (float)whole;
+  const float fp = __uint_as_float((unsigned)(frac * ((float)__float_as_uint(x) - bias) + bias));
+  float ip = 1.0f, base = x;
+  for (int e = whole; e > 0; e >>= 1) {
+    if (e & 1) ip *= base;
+    base *= base;
+  }
+  return ip * fp;
+}
+
+__device__ __forceinline__ float clip4(float x) { return fminf(4.0f, fmaxf(-4.0f, x)); }
+
+__device__ __forceinline__ int umap_positive_samples(float period, unsigned epoch) {
+  if (period <= 0.0f || !isfinite(period) || epoch == 0u) return 0;
+  const int s = (int)floorf((float)epoch / period) - (int)floorf((float)(epoch - 1u) / period);
+  return s > 0 ? s : 0;
+}
+
+__device__ __forceinline__ int umap_negative_samples(float period, int rate, unsigned epoch) {
+  if (rate <= 0 || period <= 0.0f || !isfinite(period) || epoch == 0u) return 0;
+  const float now = (float)epoch, prev = (float)(epoch - 1u);
+  const int cur = (int)floorf(now / period), pre = (int)floorf(prev / period);
+  if (cur <= pre) return 0;
+  const float np = period / (float)rate;
+  if (np <= 0.0f || !isfinite(np)) return 0;
+  const int ct = (int)floorf((now - np) / np);
+  int pt = 0;
+  if (cur > 1) pt = (int)floorf((ceilf((float)(cur - 1) * period) - np) / np);
+  const int s = ct - pt;
+  return s > 0 ? s : 0;
+}
+
+// Grid-stride over COO edges (sorted by head). The epoch number is read from device memory so
+// a captured graph of several epochs replays without re-capture.
+__global__ void __launch_bounds__(256)
+umap_epoch_kernel(float2* __restrict__ y, const int* __restrict__ heads, const int* __restrict__ tails,
+                  const float* __restrict__ eps, long long n_edges, UmapParams p, const unsigned* __restrict__ epoch_ptr) {
+  const unsigned epoch = *epoch_ptr;
+  const float alpha = p.learning_rate * (1.0f - (float)epoch / fmaxf(1.0f, (float)p.n_epochs));
+  const float fe = 1.1920928955078125e-7f;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n_edges; e += (long long)gridDim.x * blockDim.x) {
+    const float period = __ldg(eps + e);
+    const int ps = umap_positive_samples(period, epoch);
+    if (ps <= 0) continue;
+    const int h = __ldg(heads + e), t = __ldg(tails + e);
+    if (h < 0 || h >= p.n || t < 0 || t >= p.n || h == t) continue;
+    for (int s = 0; s < ps; ++s) {
+      const float2 yh = y[h], yt = y[t];
+      const float dx = yh.x - yt.x, dy = yh.y - yt.y;
+      const float d2 = fmaxf(fe, dx * dx + dy * dy);
+      const float d2b = schraudolph_pow(d2, p.b);
+      const float c = -2.0f * p.a * p.b * (d2b / d2) / (p.a * d2b + 1.0f);
+      const float gx = clip4(c * dx) * alpha, gy = clip4(c * dy) * alpha;
+      atomicAdd(y + h, make_float2(gx, gy));
+      atomicAdd(y + t, make_float2(-gx, -gy));
+    }
+    const int ns = umap_negative_samples(period, p.negative_sample_rate, epoch);
+    uint4 r = make_uint4(0u, 0u, 0u, 0u);
+    for (int s = 0; s < ns; ++s) {
+      if ((s & 3) == 0)
+        r = philox4x32_10(make_uint4((unsigned)e, (unsigned)(e >> 32), epoch, (unsigned)(s >> 2)),
+                          make_uint2(p.seed, 0x5eed0f0cu));
+      const unsigned draw = (s & 3) == 0 ? r.x : ((s & 3) == 1 ? r.y : ((s & 3) == 2 ? r.z : r.w));
+      const int neg = (int)bounded(draw, (unsigned)p.n);
+      if (neg == h || neg == t) continue;
+      const float2 yh = y[h], yn = y[neg];
+      const float dx = yh.x - yn.x, dy = yh.y - yn.y;
+      const float d2 = fmaxf(fe, dx * dx + dy * dy);
+      const float d2b = schraudolph_pow(d2, p.b);
+      const float rc = p.repulsion_strength * 2.0f * p.b / ((0.001f + d2) * (p.a * d2b + 1.0f));
+      atomicAdd(y + h, make_float2(clip4(rc * dx) * alpha, clip4(rc * dy) * alpha));
+    }
+  }
+}
+
+// NaN -> 0 and clamp to +-16 (umap_sanitize_layout_kernel, :3244-3258); thread 0 advances the
+// device epoch counter.
+__global__ void umap_sanitize_kernel(float2* __restrict__ y, int n, unsigned* __restrict__ epoch_ptr) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float2 v = y[i];
+    if (!isfinite(v.x)) v.x = 0.0f;
+    if (!isfinite(v.y)) v.y = 0.0f;
+    y[i] = make_float2(fminf(16.0f, fmaxf(-16.0f, v.x)), fminf(16.0f, fmaxf(-16.0f, v.y)));
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *epoch_ptr += 1u;
+}
+
+// find_ab_params CPU policy (src/fast_knn_umap.cpp:437-497): hard-coded values for the package's
+// spreads/min_dists, otherwise the grid search + gradient refinement of that function.
+void umap_ab_params(double spread, double min_dist, double* a, double* b) {
+  if (std::fabs(spread - 1.0) < 1e-12 && std::fabs(min_dist - 0.01) < 1e-12) {
+    *a = 1.895605865596314;
+    *b = 0.8006377738365004;
+    return;
+  }
+  if (std::fabs(spread - 1.0) < 1e-12 && std::fabs(min_dist - 0.1) < 1e-12) {
+    *a = 1.5769434601962196;
+    *b = 0.8950608781227859;
+    return;
+  }
+  if (std::fabs(spread - 1.0) < 1e-12 && std::fabs(min_dist - 0.5) < 1e-12) {
+    *a = 0.5830300199018228;
+    *b = 1.3341669931033755;
+    return;
+  }
+  double xs[300], ys[300];
+  for (int i = 0; i < 300; ++i) {
+    xs[i] = (spread * 3.0) * (double)i / 299.0;
+    ys[i] = xs[i] < min_dist ? 1.0 : std::exp(-(xs[i] - min_dist) / spread);
+  }
+  double ba = 1.5769434601962196, bb = 0.8950608781227859, best = INFINITY;
+  for (double la = -4.0; la <= 4.0001; la += 0.2)
+    for (double bv = 0.25; bv <= 2.0001; bv += 0.05) {
+      const double av = std::exp(la);
+      double loss = 0.0;
+      for (int i = 0; i < 300; ++i) {
+        const double e = 1.0 / (1.0 + av * std::pow(xs[i], 2.0 * bv)) - ys[i];
+        loss += e * e;
+      }
+      if (loss < best) {
+        best = loss;
+        ba = av;
+        bb = bv;
+      }
+    }
+  for (int it = 0; it < 80; ++it) {
+    double ga = 0.0, gb = 0.0;
+    for (int i = 0; i < 300; ++i) {
+      const double x = std::max(xs[i], 1e-6);
+      const double x2b = std::pow(x, 2.0 * bb);
+      const double den = 1.0 + ba * x2b;
+      const double e = 1.0 / den - ys[i];
+      ga += e * (-x2b / (den * den));
+      gb += e * (-(ba * x2b * 2.0 * std::log(x)) / (den * den));
+    }
+    ba = std::max(1e-4, ba - 0.01 * ga);
+    bb = std::max(0.1, bb - 0.01 * gb);
+  }
+  *a = ba;
+  *b = bb;
+}
+
+// Optimizer state of one UMAP instance.
+struct UmapJob {
+  Stream stream;
+  Arena arena;
+  float2* y = nullptr;
+  unsigned* epoch = nullptr;
+  std::map<int, std::pair<cudaGraph_t, cudaGraphExec_t>> graphs;
+  ~UmapJob() {
+    for (auto& kv : graphs) {
+      if (kv.second.second) cudaGraphExecDestroy(kv.second.second);
+      if (kv.second.first) cudaGraphDestroy(kv.second.first);
+    }
+  }
+  void alloc(int n) {
+    arena.reserve(&y, n);
+    arena.reserve(&epoch, 1);
+    arena.commit("UMAP layout");
+  }
+  void run(const int* heads, const int* tails, const float* eps, long long n_edges, const UmapParams& p) {
+    cudaStream_t s = stream.s;
+    FE_CUDA(cudaMemsetAsync(epoch, 0, sizeof(unsigned), s));
+    const int eblocks = std::max(1, std::min(ceil_div(n_edges, 256), sm_count() * 8));
+    const int pblocks = std::max(1, std::min(ceil_div(p.n, 256), sm_count() * 4));
+    auto one_epoch = [&]() {
+      umap_epoch_kernel<<<eblocks, 256, 0, s>>>(y, heads, tails, eps, n_edges, p, epoch);
+      FE_LAUNCH("umap_epoch_kernel");
+      umap_sanitize_kernel<<<pblocks, 256, 0, s>>>(y, p.n, epoch);
+      FE_LAUNCH("umap_sanitize_kernel");
+    };
+    constexpr int kChunk = 25;
+    int left = p.n_epochs;
+    while (left > 0) {
+      const int c = std::min(kChunk, left);
+      auto it = graphs.find(c);
+      if (it == graphs.end()) {
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t ge = nullptr;
+        FE_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        try {
+          for (int r = 0; r < c; ++r) one_epoch();
+        } catch (...) {
+          cudaStreamEndCapture(s, &g);
+          if (g) cudaGraphDestroy(g);
+          throw;
+        }
+        FE_CUDA(cudaStreamEndCapture(s, &g));
+        FE_CUDA(cudaGraphInstantiate(&ge, g, 0));
+        it = graphs.emplace(c, std::make_pair(g, ge)).first;
+      }
+      FE_CUDA(cudaGraphLaunch(it->second.second, s));
+      left -= c;
+    }
+  }
+};
+
+void check_umap_params(int n, long long n_edges, int n_epochs, int nsr, float lr, float rep) {
+  if (n < 2 || n_edges < 1 || n_epochs < 1 || nsr < 0 || !(lr > 0.0f) || !(rep > 0.0f))
+    throw Error("invalid CUDA COO UMAP optimization parameters");
+}
+
+}  // namespace fe
+
+extern "C" {
+
+int fastembedr_cuda_umap_optimize_coo(const int* heads, const int* tails, const float* weights,
+                                      const float* epochs_per_sample, const float* init, int n, int n_edges_capacity,
+                                      int n_epochs, int negative_sample_rate, float learning_rate, float a, float b,
+                                      float repulsion_strength, unsigned int seed, int optimizer_mode, float* out) {
+  return fe::guarded([&] {
+    if (!heads || !tails || !weights || !epochs_per_sample || !init || !out) throw fe::Error("null host pointer");
+    fe::check_umap_params(n, n_edges_capacity, n_epochs, negative_sample_rate, learning_rate, repulsion_strength);
+    if (optimizer_mode != 0)
+      throw fe::Error("optimizer_mode 1 (batched delta) is not provided; the package policy uses mode 0");
+    fe::UmapJob job;
+    job.alloc(n);
+    cudaStream_t s = job.stream.s;
+    int *d_h = nullptr, *d_t = nullptr;
+    float* d_e = nullptr;
+    fe::Arena in;
+    in.reserve(&d_h, n_edges_capacity);
+    in.reserve(&d_t, n_edges_capacity);
+    in.reserve(&d_e, n_edges_capacity);
+    in.commit("CUDA COO UMAP edges");
+    FE_CUDA(cudaMemcpyAsync(d_h, heads, sizeof(int) * n_edges_capacity, cudaMemcpyHostToDevice, s));
+    FE_CUDA(cudaMemcpyAsync(d_t, tails, sizeof(int) * n_edges_capacity, cudaMemcpyHostToDevice, s));
+    FE_CUDA(cudaMemcpyAsync(d_e, epochs_per_sample, sizeof(float) * n_edges_capacity, cudaMemcpyHostToDevice, s));
+    FE_CUDA(cudaMemcpyAsync(job.y, init, sizeof(float) * 2 * n, cudaMemcpyHostToDevice, s));
+    const fe::UmapParams p{n, n_epochs, negative_sample_rate, seed, learning_rate, a, b, repulsion_strength};
+    job.run(d_h, d_t, d_e, n_edges_capacity, p);
+    FE_CUDA(cudaMemcpyAsync(out, job.y, sizeof(float) * 2 * n, cudaMemcpyDeviceToHost, s));
+    FE_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int fastembedr_cuda_umap_graph_from_knn(const int* indices, const float* distances, int n, int k, int index_offset,
+                                        int* offsets, int* neighbors, float* weights, float* epochs_per_sample,
+                                        long long capacity, long long* nnz, float* max_weight) {
+  return fe::guarded([&] {
+    if (!indices || !distances || !offsets || !nnz) throw fe::Error("null UMAP graph pointer");
+    if (n < 2 || k < 1) throw fe::Error("invalid UMAP graph dimensions");
+    fe::Stream st;
+    const std::size_t items = (std::size_t)n * k;
+    int* d_idx = nullptr;
+    float* d_dist = nullptr;
+    fe::Arena a;
+    a.reserve(&d_idx, items);
+    a.reserve(&d_dist, items);
+    a.commit("UMAP graph input");
+    FE_CUDA(cudaMemcpyAsync(d_idx, indices, sizeof(int) * items, cudaMemcpyHostToDevice, st.s));
+    FE_CUDA(cudaMemcpyAsync(d_dist, distances, sizeof(float) * items, cudaMemcpyHostToDevice, st.s));
+    fe::validate_knn(d_idx, d_dist, n, k, index_offset, st.s);
+    fe::UmapGraph g;
+    fe::umap_build_graph(d_idx, d_dist, n, k, index_offset, g, st.s);
+    *nnz = g.nnz;
+    if (max_weight) *max_weight = g.max_weight;
+    FE_CUDA(cudaMemcpyAsync(offsets, g.offsets, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, st.s));
+    if (neighbors && weights && epochs_per_sample && g.nnz <= capacity) {
+      FE_CUDA(cudaMemcpyAsync(neighbors, g.neighbors, sizeof(int) * g.nnz, cudaMemcpyDeviceToHost, st.s));
+      FE_CUDA(cudaMemcpyAsync(weights, g.weights, sizeof(float) * g.nnz, cudaMemcpyDeviceToHost, st.s));
+      FE_CUDA(cudaMemcpyAsync(epochs_per_sample, g.eps, sizeof(float) * g.nnz, cudaMemcpyDeviceToHost, st.s));
+    }
+    FE_CUDA(cudaStreamSynchronize(st.s));
+  });
+}
+
+int fastembedr_cuda_umap_from_knn(const int* indices, const float* distances, const float* init, int n, int k,
+                                  int index_offset, int n_epochs, int negative_sample_rate, float learning_rate,
+                                  float min_dist, float repulsion_strength, unsigned int seed, float* out) {
+  return fe::guarded([&] {
+    if (!indices || !distances || !init || !out) throw fe::Error("null UMAP input pointer");
+    if (n < 2 || k < 1 || n_epochs < 1 || negative_sample_rate < 0 || !(learning_rate > 0.0f) || min_dist < 0.0f ||
+        !(repulsion_strength > 0.0f))
+      throw fe::Error("invalid CUDA UMAP parameters");
+    fe::UmapJob job;
+    job.alloc(n);
+    cudaStream_t s = job.stream.s;
+    const std::size_t items = (std::size_t)n * k;
+    int* d_idx = nullptr;
+    float* d_dist = nullptr;
+    fe::Arena a;
+    a.reserve(&d_idx, items);
+    a.reserve(&d_dist, items);
+    a.commit("UMAP input");
+    FE_CUDA(cudaMemcpyAsync(d_idx, indices, sizeof(int) * items, cudaMemcpyHostToDevice, s));
+    FE_CUDA(cudaMemcpyAsync(d_dist, distances, sizeof(float) * items, cudaMemcpyHostToDevice, s));
+    FE_CUDA(cudaMemcpyAsync(job.y, init, sizeof(float) * 2 * n, cudaMemcpyHostToDevice, s));
+    fe::validate_knn(d_idx, d_dist, n, k, index_offset, s);
+    fe::UmapGraph g;
+    fe::umap_build_graph(d_idx, d_dist, n, k, index_offset, g, s);
+    a.release();
+    double av = 0.0, bv = 0.0;
+    fe::umap_ab_params(1.0, min_dist, &av, &bv);
+    const fe::UmapParams p{n, n_epochs, negative_sample_rate, seed, learning_rate, (float)av, (float)bv,
+                           repulsion_strength};
+    job.run(g.heads, g.neighbors, g.eps, g.nnz, p);
+    FE_CUDA(cudaMemcpyAsync(out, job.y, sizeof(float) * 2 * n, cudaMemcpyDeviceToHost, s));
+    FE_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+}  // extern "C"

@@ -72,6 +72,33 @@ int fastembedr_cuda_opentsne_fft_from_device_knn_float(const int* indices, const
                                                        float min_gain, float max_step_norm, unsigned int seed,
                                                        int index_offset, float* out);
 
+/* ---------------------------------------------------------------- UMAP */
+
+/* replaces fastembedr_cuda_umap_optimize_coo, src/embedding_cuda_kernels.cpp:5483-5608.
+ * COO graph (heads, tails, weights, epochs_per_sample; n_edges_capacity entries, as
+ * umap_cuda_optimize_csr_cpp expands the CSR, src/embedding_cuda_bridge.cpp:346-378) and a
+ * row-major n x 2 init; n_epochs SGD epochs with the reference schedule (epoch 0 inactive,
+ * linear learning-rate decay, gradient clip 4, clamp to +-16 after every epoch). Negative
+ * samples come from counter-based Philox streams keyed by (seed, edge, epoch). Only
+ * optimizer_mode 0 (the package policy) is provided. */
+int fastembedr_cuda_umap_optimize_coo(const int* heads, const int* tails, const float* weights,
+                                      const float* epochs_per_sample, const float* init, int n, int n_edges_capacity,
+                                      int n_epochs, int negative_sample_rate, float learning_rate, float a, float b,
+                                      float repulsion_strength, unsigned int seed, int optimizer_mode, float* out);
+
+/* GPU twin of umap_graph_csr_float_cpp (src/fast_knn_umap.cpp:3996-4052): the default fuzzy
+ * graph from column-major KNN (offsets n + 1; neighbors / weights / epochs_per_sample up to
+ * `capacity` entries, neighbours ascending per row); *nnz and *max_weight returned. */
+int fastembedr_cuda_umap_graph_from_knn(const int* indices, const float* distances, int n, int k, int index_offset,
+                                        int* offsets, int* neighbors, float* weights, float* epochs_per_sample,
+                                        long long capacity, long long* nnz, float* max_weight);
+
+/* No reference counterpart (the reference builds the graph on the host): KNN -> fuzzy graph ->
+ * SGD entirely on the GPU, with a/b from the package's min_dist policy (spread 1). */
+int fastembedr_cuda_umap_from_knn(const int* indices, const float* distances, const float* init, int n, int k,
+                                  int index_offset, int n_epochs, int negative_sample_rate, float learning_rate,
+                                  float min_dist, float repulsion_strength, unsigned int seed, float* out);
+
 /* ---------------------------------------------------------------- t-SNE diagnostics */
 
 /* GPU twin of the affinity part of opentsne_force_diagnostic_cpp
