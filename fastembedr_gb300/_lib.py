@@ -38,6 +38,8 @@ SIGNATURES = {
     "fastembedr_cuda_umap_graph_from_knn": (I, [vp, vp, I, I, I, vp, vp, vp, vp, L, C.POINTER(L), C.POINTER(F)]),
     "fastembedr_cuda_umap_from_knn": (I, [vp, vp, vp, I, I, I, I, I, F, F, F, U, vp]),
     "fastembedr_cuda_tsne_exact_repulsion_noalloc": (I, [vp, I, vp, vp, vp]),
+    "fastembedr_cuda_transform_tsne": (I, [vp, I, vp, vp, I, I, vp, I, C.c_char_p, D, I, I, D, D, D, D, D, D, D, I, I,
+                                           I, vp]),
     "fastembedr_tsne_plan_create": (I, [vp, vp, vp, I, I, F, I, I, I, U, C.POINTER(vp)]),
     "fastembedr_tsne_plan_run": (I, [vp, I, F, F, F, F, F, I]),
     "fastembedr_tsne_plan_profile": (I, [vp, I, F, F, F, F, F, C.POINTER(F), C.POINTER(F), C.POINTER(F)]),

@@ -309,3 +309,87 @@ def umap_knn(indices, distances, init, n_components=2, seed=42, n_epochs=None, m
                   repulsion_strength=float(repulsion_strength), graph_mode="native_csr_graph",
                   graph_prep_backend="cuda_fuzzy_csr", optimizer_math="coo_atomic_edge_sampler_philox", seed=int(seed))
     return UmapFit(out, config)
+
+
+def transform_tsne(reference_layout, knn, k=None, perplexity=5.0, initialization="median", Y_init=None,
+                   n_iter=250, early_exaggeration_iter=0, learning_rate=0.1, early_exaggeration=4.0,
+                   exaggeration=1.5, initial_momentum=0.8, final_momentum=0.8, max_grad_norm=0.25,
+                   max_step_norm=math.inf, n_negatives=None, exact_repulsion_threshold=4096, seed=4,
+                   backend="cuda"):
+    """Place query points into a fixed reference layout (transform_tsne, R/transform_tsne.R:58-104).
+
+    ``knn`` is ``dict(indices=..., distances=...)``: (n_query, k) KNN of each query into the
+    reference rows. Policy restated from prepare_tsne_transform_controls (:186-229): n_negatives
+    defaults to n_reference when n_reference <= exact_repulsion_threshold, else min(256,
+    n_reference). Returns the (n_query, 2) layout and the recorded configuration of
+    tsne_transform_config (:323-352)."""
+    if backend != "cuda":
+        raise ValueError("fastembedr_gb300 implements backend = 'cuda' only")
+    ref = np.asarray(reference_layout, np.float64)
+    if ref.ndim != 2 or ref.shape[0] < 1:
+        raise ValueError("`reference_layout` must be a non-empty matrix.")
+    if ref.shape[1] != 2:
+        raise ValueError("cuda t-SNE transform currently supports only two-dimensional reference layouts.")
+    if not isinstance(knn, dict) or "indices" not in knn or "distances" not in knn:
+        raise ValueError("`knn` must contain `indices` and `distances`.")
+    idx = np.asarray(knn["indices"])
+    dist = np.asarray(knn["distances"], np.float64)
+    if idx.shape != dist.shape:
+        raise ValueError("KNN `indices` and `distances` must have the same dimensions.")
+    if idx.ndim != 2 or idx.shape[0] < 1 or idx.shape[1] < 1:
+        raise ValueError("`knn` must have at least one row and one neighbor column.")
+    if k is not None:
+        k = int(k)
+        if k < 1:
+            raise ValueError("`k` must be NULL or a positive integer.")
+        if k > idx.shape[1]:
+            raise ValueError("`k` cannot be larger than the available reference count.")
+        idx, dist = idx[:, :k], dist[:, :k]
+    nq, kk = idx.shape
+    n_ref = ref.shape[0]
+    perplexity = float(perplexity)
+    if not math.isfinite(perplexity) or perplexity <= 0:
+        raise ValueError("`perplexity` must be a positive number.")
+    n_iter, early = int(n_iter), int(early_exaggeration_iter)
+    if n_iter < 0 or early < 0 or n_iter + early < 1:
+        raise ValueError("Transform iteration counts must be non-negative and sum to at least one.")
+    threshold = 4096 if exact_repulsion_threshold is None else int(exact_repulsion_threshold)
+    if n_negatives is None:
+        n_negatives = n_ref if n_ref <= threshold else min(256, n_ref)
+    n_negatives = int(n_negatives)
+    if n_negatives < 1:
+        raise ValueError("`n_negatives` must be NULL or a positive integer.")
+    if initialization not in ("median", "weighted", "random"):
+        raise ValueError("`initialization` must be 'median', 'weighted', or 'random'.")
+    init = 0
+    y0 = np.zeros((0, 2))
+    if Y_init is not None:
+        y0 = np.asarray(Y_init, np.float64)
+        if y0.shape != (nq, 2):
+            raise ValueError("`Y_init` must have one row per query and the same columns as `reference_layout`.")
+        init = 1
+    out = np.zeros((2, nq), np.float64)  # column-major n_query x 2
+    ref_cm, idx_cm, dist_cm = _colmajor(ref, np.float64), _colmajor(idx, np.int32), _colmajor(dist, np.float64)
+    y0_cm = _colmajor(y0, np.float64)
+    lib = _lib.require_gpu()
+    st = lib.fastembedr_cuda_transform_tsne(ref_cm.ctypes.data, n_ref, idx_cm.ctypes.data, dist_cm.ctypes.data, nq, kk,
+                                            y0_cm.ctypes.data if init else None, init, initialization.encode(),
+                                            perplexity, n_iter, early, float(learning_rate),
+                                            float(early_exaggeration), float(exaggeration), float(initial_momentum),
+                                            float(final_momentum), float(max_grad_norm), float(max_step_norm),
+                                            n_negatives, threshold, int(seed), out.ctypes.data)
+    _lib.check(st, "CUDA t-SNE transform")
+    n_neg_eff = min(n_negatives, n_ref)
+    exact = n_ref <= max(threshold, 1) or n_neg_eff >= n_ref
+    config = dict(method="transform_tsne", backend="cuda", n_reference=n_ref, n_query=nq, k=kk, perplexity=perplexity,
+                  n_iter=n_iter, early_exaggeration_iter=early, learning_rate=float(learning_rate),
+                  early_exaggeration=float(early_exaggeration), exaggeration=float(exaggeration),
+                  initial_momentum=float(initial_momentum), final_momentum=float(final_momentum),
+                  max_grad_norm=float(max_grad_norm), max_step_norm=float(max_step_norm), n_negatives=n_neg_eff,
+                  exact_repulsion_threshold=threshold, initialization=initialization,
+                  optimizer="opentsne_style_fixed_reference_transform_cuda",
+                  repulsion="exact_reference_cuda" if exact else "sampled_reference_cuda",
+                  affinities="precomputed_query_conditional", affinity_storage="flat_row_major_double",
+                  transform_batch_size=nq, transform_batches=1, seed=int(seed),
+                  provenance="fixed_reference_tsne_native_cpp")
+    return TsneFit(np.ascontiguousarray(out.T), config)

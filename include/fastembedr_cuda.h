@@ -133,6 +133,24 @@ int fastembedr_cuda_tsne_force_diagnostic(const int* indices, const float* dista
 int fastembedr_cuda_tsne_exact_repulsion_noalloc(const float* layout, int n, float* repulsive, double* sum_q,
                                                  void* stream);
 
+/* ---------------------------------------------------------------- fixed-reference transform
+ * Replaces transform_tsne_cuda_cpp, which R/transform_tsne.R:272-289 calls for
+ * transform_tsne(backend = "cuda") but which the reference never defines; arguments follow
+ * transform_tsne_cpp (src/tsne_neighbors.cpp:2124-2144) minus n_threads / batch_size / verbose.
+ * Matrices are R layout (column-major doubles): reference_layout n_reference x 2, indices /
+ * distances n_query x k (1- or 0-based, detected as resolve_reference_index_offset does),
+ * y_init n_query x 2 when init != 0, out n_query x 2. initialization: "median" or "weighted"
+ * when init == 0. Repulsion is exact for n_reference <= exact_repulsion_threshold, else
+ * n_negatives references per query and iteration from the reference's xorshift32 stream.
+ * Host pointers; returns after the result is in `out`. */
+int fastembedr_cuda_transform_tsne(const double* reference_layout, int n_reference, const int* indices,
+                                   const double* distances, int n_query, int k, const double* y_init, int init,
+                                   const char* initialization, double perplexity, int n_iter,
+                                   int early_exaggeration_iter, double learning_rate, double early_exaggeration,
+                                   double exaggeration, double initial_momentum, double final_momentum,
+                                   double max_grad_norm, double max_step_norm, int n_negatives,
+                                   int exact_repulsion_threshold, int seed, double* out);
+
 /* ---------------------------------------------------------------- resident t-SNE plan
  * No reference counterpart: the reference rebuilds everything per call. A plan keeps P, the
  * layout and the optimizer state resident in HBM so iterations can be timed and driven in
