@@ -40,6 +40,12 @@ SIGNATURES = {
     "fastembedr_cuda_tsne_exact_repulsion_noalloc": (I, [vp, I, vp, vp, vp]),
     "fastembedr_cuda_transform_tsne": (I, [vp, I, vp, vp, I, I, vp, I, C.c_char_p, D, I, I, D, D, D, D, D, D, D, I, I,
                                            I, vp]),
+    "fastembedr_transform_server_create": (I, [vp, I, D, I, I, D, D, D, D, D, D, D, I, I, I, C.c_char_p, C.c_ulonglong,
+                                               I, C.POINTER(vp)]),
+    "fastembedr_transform_server_submit": (I, [vp, vp, vp, I, I, C.POINTER(C.c_ulonglong)]),
+    "fastembedr_transform_server_wait": (I, [vp, C.c_ulonglong, I, vp, C.POINTER(D)]),
+    "fastembedr_transform_server_stats": (I, [vp] + [C.POINTER(C.c_ulonglong)] * 6),
+    "fastembedr_transform_server_destroy": (None, [vp]),
     "fastembedr_tsne_plan_create": (I, [vp, vp, vp, I, I, F, I, I, I, U, C.POINTER(vp)]),
     "fastembedr_tsne_plan_run": (I, [vp, I, F, F, F, F, F, I]),
     "fastembedr_tsne_plan_profile": (I, [vp, I, F, F, F, F, F, C.POINTER(F), C.POINTER(F), C.POINTER(F)]),

@@ -393,3 +393,87 @@ def transform_tsne(reference_layout, knn, k=None, perplexity=5.0, initialization
                   transform_batch_size=nq, transform_batches=1, seed=int(seed),
                   provenance="fixed_reference_tsne_native_cpp")
     return TsneFit(np.ascontiguousarray(out.T), config)
+
+
+class TransformServer:
+    """Resident serving loop for transform_tsne (C ABI fastembedr_transform_server_*).
+
+    The reference layout stays on the device; ``submit`` queues one query batch (its KNN into
+    the reference, int32 / float32) and returns a request id at once; ``result`` waits for it.
+    Requests are admitted in arrival order against ``memory_budget_bytes`` and run merged with
+    whatever else is admitted at the same time; every result equals ``transform_tsne`` on the
+    same request. Options follow transform_tsne and are fixed per server."""
+
+    def __init__(self, reference_layout, perplexity=5.0, initialization="median", n_iter=250,
+                 early_exaggeration_iter=0, learning_rate=0.1, early_exaggeration=4.0, exaggeration=1.5,
+                 initial_momentum=0.8, final_momentum=0.8, max_grad_norm=0.25, max_step_norm=math.inf,
+                 n_negatives=None, exact_repulsion_threshold=4096, seed=4, memory_budget_bytes=0, max_inflight=4):
+        ref = np.asarray(reference_layout, np.float64)
+        if ref.ndim != 2 or ref.shape[0] < 1 or ref.shape[1] != 2:
+            raise ValueError("`reference_layout` must be a non-empty two-column matrix.")
+        n_ref = ref.shape[0]
+        threshold = 4096 if exact_repulsion_threshold is None else int(exact_repulsion_threshold)
+        if n_negatives is None:
+            n_negatives = n_ref if n_ref <= threshold else min(256, n_ref)
+        self.n_reference = n_ref
+        self.n_negatives = min(int(n_negatives), n_ref)
+        self.exact = n_ref <= max(threshold, 1) or self.n_negatives >= n_ref
+        self._lib = _lib.require_gpu()
+        self._h = C.c_void_p()
+        ref_cm = _colmajor(ref, np.float64)
+        st = self._lib.fastembedr_transform_server_create(
+            ref_cm.ctypes.data, n_ref, float(perplexity), int(n_iter), int(early_exaggeration_iter),
+            float(learning_rate), float(early_exaggeration), float(exaggeration), float(initial_momentum),
+            float(final_momentum), float(max_grad_norm), float(max_step_norm), int(n_negatives), threshold, int(seed),
+            str(initialization).encode(), int(memory_budget_bytes), int(max_inflight), C.byref(self._h))
+        _lib.check(st, "CUDA t-SNE transform server")
+        self._shape = {}
+
+    def submit(self, indices, distances) -> int:
+        idx = _colmajor(np.asarray(indices), np.int32)
+        dist = _colmajor(np.asarray(distances), np.float32)
+        if idx.shape != dist.shape or idx.ndim != 2:
+            raise ValueError("KNN `indices` and `distances` must have the same dimensions.")
+        rid = C.c_ulonglong()
+        st = self._lib.fastembedr_transform_server_submit(self._h, idx.ctypes.data, dist.ctypes.data, idx.shape[0],
+                                                          idx.shape[1], C.byref(rid))
+        _lib.check(st, "CUDA t-SNE transform request")
+        self._shape[rid.value] = idx.shape[0]
+        return rid.value
+
+    def result(self, request_id, timeout_ms=-1):
+        """(layout (n_query, 2), latency_ms) or None when not finished within timeout_ms."""
+        nq = self._shape[request_id]
+        out = np.zeros((2, nq), np.float64)
+        lat = C.c_double()
+        st = self._lib.fastembedr_transform_server_wait(self._h, C.c_ulonglong(request_id), int(timeout_ms),
+                                                        out.ctypes.data, C.byref(lat))
+        if st == 2:
+            return None
+        del self._shape[request_id]
+        _lib.check(st, "CUDA t-SNE transform request")
+        return np.ascontiguousarray(out.T), lat.value
+
+    def stats(self) -> dict:
+        vals = [C.c_ulonglong() for _ in range(6)]
+        _lib.check(self._lib.fastembedr_transform_server_stats(self._h, *[C.byref(v) for v in vals]),
+                   "CUDA t-SNE transform server stats")
+        keys = ("completed", "queries", "groups", "launches", "peak_bytes", "budget_bytes")
+        return {k: v.value for k, v in zip(keys, vals)}
+
+    def close(self):
+        if self._h:
+            self._lib.fastembedr_transform_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -151,6 +151,40 @@ int fastembedr_cuda_transform_tsne(const double* reference_layout, int n_referen
                                    double max_grad_norm, double max_step_norm, int n_negatives,
                                    int exact_repulsion_threshold, int seed, double* out);
 
+/* ---------------------------------------------------------------- transform serving loop
+ * No counterpart in the reference: fastembedr_cuda_landmark_tsne_from_device_knn
+ * (src/embedding_cuda_kernels.cpp:3572-3686) uploads the reference and rebuilds its state on
+ * every call. A server keeps the reference layout resident, accepts query batches from any
+ * thread, admits them in arrival order while their device memory fits `memory_budget_bytes`
+ * (0: 40 GiB, capped by free memory) and one of `max_inflight` streams is free, and runs each
+ * admitted group of requests as one merged launch. Options are those of
+ * fastembedr_cuda_transform_tsne, fixed per server. Each result equals the one-shot transform
+ * of the same request bit for bit, whatever else is in flight. */
+typedef struct fastembedr_transform_server fastembedr_transform_server;
+
+int fastembedr_transform_server_create(const double* reference_layout, int n_reference, double perplexity, int n_iter,
+                                       int early_exaggeration_iter, double learning_rate, double early_exaggeration,
+                                       double exaggeration, double initial_momentum, double final_momentum,
+                                       double max_grad_norm, double max_step_norm, int n_negatives,
+                                       int exact_repulsion_threshold, int seed, const char* initialization,
+                                       unsigned long long memory_budget_bytes, int max_inflight,
+                                       fastembedr_transform_server** server);
+/* indices (int32) / distances (float32): host, column-major n_query x k KNN into the reference
+ * (1- or 0-based). The arrays are copied before the call returns. */
+int fastembedr_transform_server_submit(fastembedr_transform_server* server, const int* indices, const float* distances,
+                                       int n_query, int k, unsigned long long* request_id);
+/* Wait up to timeout_ms (< 0: no limit). Returns 0 when done (out: column-major n_query x 2
+ * doubles, latency_ms: submit to result on the host; a non-NULL out consumes the request),
+ * 2 while still queued or running, 1 on error. */
+int fastembedr_transform_server_wait(fastembedr_transform_server* server, unsigned long long request_id, int timeout_ms,
+                                     double* out, double* latency_ms);
+int fastembedr_transform_server_stats(fastembedr_transform_server* server, unsigned long long* completed,
+                                      unsigned long long* queries, unsigned long long* groups,
+                                      unsigned long long* launches, unsigned long long* peak_bytes,
+                                      unsigned long long* budget_bytes);
+/* Finishes the groups on the device, fails queued requests, frees everything. */
+void fastembedr_transform_server_destroy(fastembedr_transform_server* server);
+
 /* ---------------------------------------------------------------- resident t-SNE plan
  * No reference counterpart: the reference rebuilds everything per call. A plan keeps P, the
  * layout and the optimizer state resident in HBM so iterations can be timed and driven in
