@@ -301,6 +301,279 @@ def run_gpu(args):
     return 0
 
 
+# ---------------------------------------------------------------- secondary workloads
+SERVE_N_REF = 500_000
+SERVE_K = 90
+SERVE_ITERS = 250
+
+
+def _serving_inputs(args, device):
+    """Reference 500,000 x 50 (20 clusters) embedded once with t-SNE (perplexity 30, k = 90, the
+    package schedule) and a 100,000-query pool with exact k = 90 KNN into the reference; the
+    request list: batch sizes log-uniform in [1, 50,000], Poisson arrivals."""
+    from fastembedr_gb300 import api
+    from fastembedr_gb300 import synthetic as S
+
+    n_ref = args.n_ref
+    ref_x, pool_x = S.serving_transform(n_ref=n_ref)
+    ridx, rdist = S.exact_knn_torch(ref_x, SERVE_K, device=device)
+    fit = api.tsne_knn(ridx.cpu().numpy(), rdist.cpu().numpy(), perplexity=30.0, Y_init=S.tsne_init(n_ref))
+    del ridx, rdist
+    qidx, qdist = S.exact_knn_query_torch(ref_x, pool_x, SERVE_K, device=device)
+    qidx = (qidx + 1).cpu().numpy()  # 1-based, as R passes them
+    qdist = qdist.cpu().numpy()
+    rng = np.random.default_rng(17)
+    sizes = np.exp(rng.uniform(0.0, np.log(50_000), args.requests)).astype(np.int64).clip(1, 50_000)
+    offsets = np.array([rng.integers(0, qidx.shape[0] - s_ + 1) for s_ in sizes])
+    gaps = rng.exponential(1.0, args.requests)  # unit-rate Poisson gaps, scaled per run
+    reqs = [(np.asfortranarray(qidx[o:o + s_]), np.asfortranarray(qdist[o:o + s_])) for o, s_ in zip(offsets, sizes)]
+    return fit.layout.astype(np.float64), reqs, gaps
+
+
+def _serve(ref_layout, reqs, arrivals, budget):
+    """Submit each request at its arrival time (None: all at once); return wall seconds,
+    latencies (ms) and the server counters."""
+    from fastembedr_gb300 import api
+
+    with api.TransformServer(ref_layout, perplexity=5.0, memory_budget_bytes=budget, max_inflight=4) as sv:
+        sv.result(sv.submit(reqs[0][0][:4], reqs[0][1][:4]))  # warm-up: kernels loaded, pools touched
+        ids = []
+        t0 = time.perf_counter()
+        for j, (qi, qd) in enumerate(reqs):
+            if arrivals is not None:
+                while time.perf_counter() - t0 < arrivals[j]:
+                    time.sleep(0.0001)
+            ids.append(sv.submit(qi, qd))
+        lat = [sv.result(i)[1] for i in ids]
+        wall = time.perf_counter() - t0
+        stats = sv.stats()
+    return wall, np.array(lat), stats
+
+
+def run_serving(args):
+    """Serving form of transform_tsne (fixed-reference transform) on one GPU."""
+    import torch
+
+    from fastembedr_gb300 import api
+
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    device = f"cuda:{local}"
+    ref_layout, reqs, gaps = _serving_inputs(args, device)
+    torch.cuda.empty_cache()
+    points = int(sum(r[0].shape[0] for r in reqs))
+    budget = 40 << 30
+    # warm-up, then saturation: every request queued at t = 0 (closed loop, capacity)
+    _serve(ref_layout, reqs[: args.warmup], None, budget)
+    clocks = ClockSampler(local)
+    wall, lat_sat, st = _serve(ref_layout, reqs, None, budget)
+    clk = clocks.stop()
+    capacity = points / wall
+    # open loop: Poisson arrivals at 70% of capacity (in requests/s)
+    rate = 0.7 * len(reqs) / wall
+    wall_p, lat, st_p = _serve(ref_layout, reqs, np.cumsum(gaps) / rate, budget)
+    # the plain one-instance-per-call GPU form: each request through the one-shot C ABI in turn
+    n_plain = min(len(reqs), args.plain_requests)
+    t0 = time.perf_counter()
+    for qi, qd in reqs[:n_plain]:
+        api.transform_tsne(ref_layout, dict(indices=qi, distances=qd.astype(np.float64)), perplexity=5.0)
+    plain_wall = time.perf_counter() - t0
+    plain_points = int(sum(r[0].shape[0] for r in reqs[:n_plain]))
+    # the largest group alone: iterate-kernel throughput for the roofline
+    big = max(range(len(reqs)), key=lambda j: reqs[j][0].shape[0])
+    _, _, st_big = _serve(ref_layout, [reqs[big]], None, budget)
+    nq_big = st_big["largest_group_queries"]
+    it_ms = st_big["largest_group_iterate_ms"]
+    n_neg = 256
+    alg_bytes = nq_big * SERVE_ITERS * (SERVE_K * 12 + n_neg * 8)
+    peak, peak_kind = measured_peak_hbm()
+    achieved = alg_bytes / (it_ms * 1e-3) / 1e9
+    h2d = int(sum(r[0].nbytes + r[1].nbytes for r in reqs))
+    line = {
+        "metric": "transform_points_per_s_served", "value": capacity, "unit": "points/s", "n_gpus": 1,
+        "steps": len(reqs), "warmup": args.warmup, "ms_per_step": 1e3 * wall / len(reqs), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "transform_tsne_serving_ref500k_k90", "n_reference": SERVE_N_REF if args.n_ref == SERVE_N_REF
+                   else args.n_ref, "k": SERVE_K, "iterations": SERVE_ITERS, "repulsion": "sampled, 256 negatives",
+                   "requests": len(reqs), "points": points, "batch_sizes": "log-uniform [1, 50000]",
+                   "memory_budget_gb": 40, "l2": "reference layout is L2-resident by design; no flush"},
+        "points_iterations_per_s": capacity * SERVE_ITERS,
+        "latency_ms": {"rate_req_per_s": rate, "p50": float(np.percentile(lat, 50)),
+                       "p99": float(np.percentile(lat, 99)), "wall_s": wall_p,
+                       "saturated_p50": float(np.percentile(lat_sat, 50)),
+                       "saturated_p99": float(np.percentile(lat_sat, 99))},
+        "plain_gpu": {"points_per_s": plain_points / plain_wall, "requests": n_plain,
+                      "form": "one fastembedr_cuda_transform_tsne call per request, in turn"},
+        "served_vs_plain": capacity / (plain_points / plain_wall),
+        "server": st, "clocks": clk,
+        "e2e": {"value": capacity, "unit": "points/s", "h2d_bytes_per_step": h2d // len(reqs),
+                "d2h_bytes_per_step": points * 16 // len(reqs),
+                "note": "the serving API takes host KNN and returns host layouts: value is end to end"},
+        "roofline": {"kernel": "transform_iterate_kernel", "bound": "hbm", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                     "algorithmic_bytes": alg_bytes, "avg_launch_ms": it_ms, "group_queries": nq_big,
+                     "note": "P/neighbour rows and the sampled reference gathers are L2-resident"},
+        "gpu_launches": int(st["launches"]),
+    }
+    if not args.no_cpu:
+        line["cpu_baseline"] = _cpu_transform_baseline(ref_layout, reqs)
+    print(json.dumps(line))
+    return 0
+
+
+def _cpu_transform_baseline(ref_layout, reqs):
+    """transform_tsne_cpp restated (oracle, OpenMP over this host's cores) on the first
+    requests, up to ~4,000 queries: same options as the served run."""
+    import oracle as O
+
+    O.build()
+    threads = O.orc().orc_set_threads(0)
+    sample, total = [], 0
+    for qi, qd in reqs:
+        if total >= 4000:
+            break
+        sample.append((qi, qd))
+        total += qi.shape[0]
+    t = time.perf_counter()
+    for qi, qd in sample:
+        O.transform_tsne(ref_layout, qi, qd.astype(np.float64), n_negatives=256, exact_threshold=4096, seed=4)
+    dt = time.perf_counter() - t
+    return {"value": total / dt, "unit": "points/s", "cores": threads, "kind": "port",
+            "sample": f"{len(sample)} requests, {total} queries x {SERVE_ITERS} iterations ({dt:.1f} s)"}
+
+
+def run_serving_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    import torch
+
+    if not torch.cuda.is_available():
+        print(json.dumps({"impl": "reference", "unavailable": "no GPU to synthesise the serving inputs"}))
+        return 0
+    ref_layout, reqs, _ = _serving_inputs(args, f"cuda:{local}")
+    b = _cpu_transform_baseline(ref_layout, reqs)
+    print(json.dumps({"impl": "reference", "metric": "transform_points_per_s_served", "value": b["value"],
+                      "unit": "points/s", "n_gpus": world, "steps": 1, "warmup": 0, "higher_is_better": True,
+                      "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                      "config": {"workload": "transform_tsne_serving_ref500k_k90"}, "cpu_baseline": b,
+                      "e2e": {"value": b["value"], "unit": "points/s", "h2d_bytes_per_step": 0,
+                              "d2h_bytes_per_step": 0}}))
+    return 0
+
+
+UMAP_N = 100_000
+UMAP_K = 15
+UMAP_EPOCHS = 500
+
+
+def _pca_init(x):
+    """Top two principal components scaled to max |y| = 10: a data-derived start that stands in
+    for the package's spectral initialisation (computed outside the optimizer, fed to both sides)."""
+    xc = x.astype(np.float64) - x.mean(0)
+    _, _, vt = np.linalg.svd(xc[:: max(1, x.shape[0] // 20000)], full_matrices=False)
+    y = xc @ vt[:2].T
+    return (y * (10.0 / np.abs(y).max())).astype(np.float32)
+
+
+def run_umap(args):
+    """UMAP epochs per second at 100,000 x 50 (20 clusters, log-normal sizes), k = 15, 500 epochs."""
+    import ctypes as C
+
+    import torch
+
+    from fastembedr_gb300 import _lib
+    from fastembedr_gb300 import synthetic as S
+
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    x, _ = S.plain_umap_100k(n=args.n_umap)
+    idx, dist = S.exact_knn_torch(x, UMAP_K, device=f"cuda:{local}")
+    idx_h = np.asfortranarray(idx.cpu().numpy())
+    dist_h = np.asfortranarray(dist.cpu().numpy())
+    n = idx_h.shape[0]
+    init = _pca_init(x)
+    out = np.zeros((n, 2), np.float32)
+    lib = _lib.require_gpu()
+    gm, sm = C.c_float(), C.c_float()
+
+    def job(epochs):
+        t = time.perf_counter()
+        st = lib.fastembedr_cuda_umap_from_knn_profile(idx_h.ctypes.data, dist_h.ctypes.data, init.ctypes.data, n,
+                                                       UMAP_K, 0, epochs, 5, 1.0, 0.01, 1.0, 42, out.ctypes.data,
+                                                       C.byref(gm), C.byref(sm))
+        _lib.check(st, "UMAP")
+        return time.perf_counter() - t
+
+    for _ in range(args.warmup):
+        job(25)
+    clocks = ClockSampler(local)
+    wall = job(UMAP_EPOCHS)
+    clk = clocks.stop()
+    sgd_ms, graph_ms = sm.value, gm.value
+    line = {
+        "metric": "umap_epochs_per_s_100k", "value": UMAP_EPOCHS / (sgd_ms * 1e-3), "unit": "epochs/s",
+        "n_gpus": 1, "steps": UMAP_EPOCHS, "warmup": args.warmup, "ms_per_step": sgd_ms / UMAP_EPOCHS,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "umap_knn_100k_k15_500epochs", "n": n, "k": UMAP_K, "epochs": UMAP_EPOCHS,
+                   "negative_sample_rate": 5, "min_dist": 0.01, "init": "PCA stand-in for the spectral start",
+                   "l2": "edge list and layout are L2-resident (about 40 MB); no flush"},
+        "graph_ms": graph_ms, "clocks": clk,
+        "e2e": {"value": UMAP_EPOCHS / wall, "unit": "epochs/s", "h2d_bytes_per_step": (idx_h.nbytes + dist_h.nbytes
+                + init.nbytes) // UMAP_EPOCHS, "d2h_bytes_per_step": out.nbytes // UMAP_EPOCHS,
+                "job": "H2D KNN + GPU fuzzy graph + 500 epochs + D2H layout"},
+        "gpu_launches": 2 * UMAP_EPOCHS,
+    }
+    if not args.no_cpu:
+        line["cpu_baseline"] = _cpu_umap_baseline(idx_h, dist_h, init)
+    print(json.dumps(line))
+    return 0
+
+
+def _cpu_umap_baseline(idx_h, dist_h, init, epochs=20):
+    """Reference CPU SGD (oracle restatement of optimize_layout_csr, deterministic single-thread
+    branch) on the same graph and start, `epochs` epochs."""
+    import oracle as O
+
+    O.build()
+    n = idx_h.shape[0]
+    off, nb, w, e, mw = O.umap_graph(np.ascontiguousarray(idx_h), np.ascontiguousarray(dist_h))
+    a, b = O.umap_ab(0.01)
+    emb = np.ascontiguousarray(init.T.astype(np.float64)).ravel().copy()
+    t = time.perf_counter()
+    O.orc().orc_umap_sgd_serial(n, off, nb, w, emb, epochs, a, b, 5, 1.0, 1.0, 42)
+    dt = time.perf_counter() - t
+    return {"value": epochs / dt, "unit": "epochs/s", "cores": 1, "kind": "port",
+            "sample": f"first {epochs} of {UMAP_EPOCHS} epochs on the same graph and start ({dt:.1f} s)"}
+
+
+def run_umap_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    import torch
+
+    from fastembedr_gb300 import synthetic as S
+
+    if not torch.cuda.is_available():
+        print(json.dumps({"impl": "reference", "unavailable": "no GPU to synthesise the KNN input"}))
+        return 0
+    x, _ = S.plain_umap_100k(n=args.n_umap)
+    idx, dist = S.exact_knn_torch(x, UMAP_K, device=f"cuda:{local}")
+    b = _cpu_umap_baseline(np.asfortranarray(idx.cpu().numpy()), np.asfortranarray(dist.cpu().numpy()), _pca_init(x))
+    print(json.dumps({"impl": "reference", "metric": "umap_epochs_per_s_100k", "value": b["value"],
+                      "unit": "epochs/s", "n_gpus": world, "steps": 20, "warmup": 0, "higher_is_better": True,
+                      "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                      "config": {"workload": "umap_knn_100k_k15_500epochs"}, "cpu_baseline": b,
+                      "e2e": {"value": b["value"], "unit": "epochs/s", "h2d_bytes_per_step": 0,
+                              "d2h_bytes_per_step": 0}}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -312,9 +585,19 @@ def main():
     ap.add_argument("--no-kl", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--n", type=int, default=N_POINTS, help="points (profiling captures use a smaller case)")
+    ap.add_argument("--workload", default="tsne", choices=["tsne", "serving", "umap"],
+                    help="tsne: the headline 1M-point optimizer; serving: transform_tsne served; umap: 100k UMAP")
+    ap.add_argument("--n-ref", type=int, default=SERVE_N_REF)
+    ap.add_argument("--requests", type=int, default=160)
+    ap.add_argument("--plain-requests", type=int, default=60)
+    ap.add_argument("--n-umap", type=int, default=UMAP_N)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.workload == "serving":
+        return run_serving_reference(args) if args.impl == "reference" else run_serving(args)
+    if args.workload == "umap":
+        return run_umap_reference(args) if args.impl == "reference" else run_umap(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

@@ -37,6 +37,8 @@ SIGNATURES = {
     "fastembedr_cuda_umap_optimize_coo": (I, [vp, vp, vp, vp, vp, I, I, I, I, F, F, F, F, U, I, vp]),
     "fastembedr_cuda_umap_graph_from_knn": (I, [vp, vp, I, I, I, vp, vp, vp, vp, L, C.POINTER(L), C.POINTER(F)]),
     "fastembedr_cuda_umap_from_knn": (I, [vp, vp, vp, I, I, I, I, I, F, F, F, U, vp]),
+    "fastembedr_cuda_umap_from_knn_profile": (I, [vp, vp, vp, I, I, I, I, I, F, F, F, U, vp, C.POINTER(F),
+                                                  C.POINTER(F)]),
     "fastembedr_cuda_tsne_exact_repulsion_noalloc": (I, [vp, I, vp, vp, vp]),
     "fastembedr_cuda_transform_tsne": (I, [vp, I, vp, vp, I, I, vp, I, C.c_char_p, D, I, I, D, D, D, D, D, D, D, I, I,
                                            I, vp]),
@@ -44,7 +46,8 @@ SIGNATURES = {
                                                I, C.POINTER(vp)]),
     "fastembedr_transform_server_submit": (I, [vp, vp, vp, I, I, C.POINTER(C.c_ulonglong)]),
     "fastembedr_transform_server_wait": (I, [vp, C.c_ulonglong, I, vp, C.POINTER(D)]),
-    "fastembedr_transform_server_stats": (I, [vp] + [C.POINTER(C.c_ulonglong)] * 6),
+    "fastembedr_transform_server_stats": (I, [vp] + [C.POINTER(C.c_ulonglong)] * 6 + [C.POINTER(D)] * 2
+                                          + [C.POINTER(L), C.POINTER(D)]),
     "fastembedr_transform_server_destroy": (None, [vp]),
     "fastembedr_tsne_plan_create": (I, [vp, vp, vp, I, I, F, I, I, I, U, C.POINTER(vp)]),
     "fastembedr_tsne_plan_run": (I, [vp, I, F, F, F, F, F, I]),

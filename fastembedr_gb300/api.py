@@ -455,10 +455,11 @@ class TransformServer:
         return np.ascontiguousarray(out.T), lat.value
 
     def stats(self) -> dict:
-        vals = [C.c_ulonglong() for _ in range(6)]
+        vals = [C.c_ulonglong() for _ in range(6)] + [C.c_double(), C.c_double(), C.c_longlong(), C.c_double()]
         _lib.check(self._lib.fastembedr_transform_server_stats(self._h, *[C.byref(v) for v in vals]),
                    "CUDA t-SNE transform server stats")
-        keys = ("completed", "queries", "groups", "launches", "peak_bytes", "budget_bytes")
+        keys = ("completed", "queries", "groups", "launches", "peak_bytes", "budget_bytes", "device_ms", "iterate_ms",
+                "largest_group_queries", "largest_group_iterate_ms")
         return {k: v.value for k, v in zip(keys, vals)}
 
     def close(self):

@@ -117,6 +117,8 @@ struct Slot {
   std::atomic<bool> done{false};
   bool busy = false;
   void* server = nullptr;
+  cudaEvent_t ev_begin = nullptr, ev_iterate = nullptr, ev_end = nullptr;  // device time of the group
+  long long group_queries = 0;
 };
 
 constexpr int kMaxSegments = 4096;
@@ -147,6 +149,8 @@ class TransformServer {
   int device = 0;
   // statistics
   unsigned long long completed = 0, queries_done = 0, groups = 0, launches = 0;
+  double device_ms = 0.0, iterate_ms = 0.0, max_group_iterate_ms = 0.0;
+  long long max_group_queries = 0;
 
   ~TransformServer() { shutdown(); }
 
@@ -224,13 +228,17 @@ class TransformServer {
       total += r->nq;
     }
     FE_CUDA(cudaMemcpyAsync(slot.d_segs, slot.h_segs, sizeof(TransformSegment) * nseg, cudaMemcpyHostToDevice, s));
+    slot.group_queries = total;
+    FE_CUDA(cudaEventRecord(slot.ev_begin, s));
     transform_prepare(ref, ref_d, slot.d_segs, nseg, total, tp, s);
+    FE_CUDA(cudaEventRecord(slot.ev_iterate, s));
     int max_k = 1;
     for (Request* r : slot.reqs) max_k = std::max(max_k, r->k);
     const int chunk = transform_chunk(total, tp, max_k);
     int n_launch = 2;
     for (int it = 0; it < tp.iter_total; it += chunk, ++n_launch)
       transform_iterate(ref, slot.d_segs, nseg, total, tp, jump, it, std::min(tp.iter_total, it + chunk), s);
+    FE_CUDA(cudaEventRecord(slot.ev_end, s));
     for (int g = 0; g < nseg; ++g) {
       Request* r = slot.reqs[g];
       const std::size_t items = (std::size_t)r->nq * r->k;
@@ -271,6 +279,18 @@ class TransformServer {
         Slot& sl = *slp;
         if (!sl.busy || !sl.done.load()) continue;
         const cudaError_t e = cudaStreamQuery(sl.stream);
+        float g_ms = 0.0f, i_ms = 0.0f;
+        if ((e == cudaSuccess || e == cudaErrorNotReady) &&
+            cudaEventElapsedTime(&g_ms, sl.ev_begin, sl.ev_end) == cudaSuccess &&
+            cudaEventElapsedTime(&i_ms, sl.ev_iterate, sl.ev_end) == cudaSuccess) {
+          device_ms += g_ms;
+          iterate_ms += i_ms;
+          if (sl.group_queries >= max_group_queries) {
+            max_group_queries = sl.group_queries;
+            max_group_iterate_ms = i_ms;
+          }
+        }
+        cudaGetLastError();
         for (Request* r : sl.reqs) {
           const std::size_t items = (std::size_t)r->nq * r->k;
           const double* h_out = reinterpret_cast<const double*>(host_pool + r->host_off + align256(items * sizeof(int)) +
@@ -392,6 +412,8 @@ class TransformServer {
       if (sl->stream) cudaStreamDestroy(sl->stream);
       if (sl->h_segs) cudaFreeHost(sl->h_segs);
       if (sl->d_segs) cudaFree(sl->d_segs);
+      for (cudaEvent_t ev : {sl->ev_begin, sl->ev_iterate, sl->ev_end})
+        if (ev) cudaEventDestroy(ev);
       sl->stream = nullptr;
       sl->h_segs = nullptr;
     }
@@ -484,6 +506,9 @@ extern "C" int fastembedr_transform_server_create(const double* reference_layout
       FE_CUDA(cudaStreamCreateWithFlags(&sl->stream, cudaStreamNonBlocking));
       FE_CUDA(cudaHostAlloc(&sl->h_segs, sizeof(fe::TransformSegment) * fe::kMaxSegments, cudaHostAllocDefault));
       FE_CUDA(cudaMalloc(&sl->d_segs, sizeof(fe::TransformSegment) * fe::kMaxSegments));
+      FE_CUDA(cudaEventCreate(&sl->ev_begin));
+      FE_CUDA(cudaEventCreate(&sl->ev_iterate));
+      FE_CUDA(cudaEventCreate(&sl->ev_end));
       sl->server = &sv;
       sv.slots.push_back(std::move(sl));
     }
@@ -572,7 +597,9 @@ extern "C" int fastembedr_transform_server_wait(fastembedr_transform_server* ser
 extern "C" int fastembedr_transform_server_stats(fastembedr_transform_server* server, unsigned long long* completed,
                                                  unsigned long long* queries, unsigned long long* groups,
                                                  unsigned long long* launches, unsigned long long* peak_bytes,
-                                                 unsigned long long* budget_bytes) {
+                                                 unsigned long long* budget_bytes, double* device_ms,
+                                                 double* iterate_ms, long long* largest_group_queries,
+                                                 double* largest_group_iterate_ms) {
   return fe::guarded([&] {
     fe::TransformServer* sv = impl(server);
     std::lock_guard<std::mutex> lk(sv->mu);
@@ -582,6 +609,10 @@ extern "C" int fastembedr_transform_server_stats(fastembedr_transform_server* se
     if (launches) *launches = sv->launches;
     if (peak_bytes) *peak_bytes = sv->dev_alloc.peak();
     if (budget_bytes) *budget_bytes = sv->dev_alloc.capacity();
+    if (device_ms) *device_ms = sv->device_ms;
+    if (iterate_ms) *iterate_ms = sv->iterate_ms;
+    if (largest_group_queries) *largest_group_queries = sv->max_group_queries;
+    if (largest_group_iterate_ms) *largest_group_iterate_ms = sv->max_group_iterate_ms;
   });
 }
 

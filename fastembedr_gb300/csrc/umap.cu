@@ -660,9 +660,10 @@ int fastembedr_cuda_umap_graph_from_knn(const int* indices, const float* distanc
   });
 }
 
-int fastembedr_cuda_umap_from_knn(const int* indices, const float* distances, const float* init, int n, int k,
-                                  int index_offset, int n_epochs, int negative_sample_rate, float learning_rate,
-                                  float min_dist, float repulsion_strength, unsigned int seed, float* out) {
+int fastembedr_cuda_umap_from_knn_profile(const int* indices, const float* distances, const float* init, int n,
+                                          int k, int index_offset, int n_epochs, int negative_sample_rate,
+                                          float learning_rate, float min_dist, float repulsion_strength,
+                                          unsigned int seed, float* out, float* graph_ms, float* sgd_ms) {
   return fe::guarded([&] {
     if (!indices || !distances || !init || !out) throw fe::Error("null UMAP input pointer");
     if (n < 2 || k < 1 || n_epochs < 1 || negative_sample_rate < 0 || !(learning_rate > 0.0f) || min_dist < 0.0f ||
@@ -681,18 +682,42 @@ int fastembedr_cuda_umap_from_knn(const int* indices, const float* distances, co
     FE_CUDA(cudaMemcpyAsync(d_idx, indices, sizeof(int) * items, cudaMemcpyHostToDevice, s));
     FE_CUDA(cudaMemcpyAsync(d_dist, distances, sizeof(float) * items, cudaMemcpyHostToDevice, s));
     FE_CUDA(cudaMemcpyAsync(job.y, init, sizeof(float) * 2 * n, cudaMemcpyHostToDevice, s));
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    const bool timed = graph_ms || sgd_ms;
+    if (timed)
+      for (auto& e : ev) FE_CUDA(cudaEventCreate(&e));
+    struct EventGuard {
+      cudaEvent_t* e;
+      ~EventGuard() {
+        for (int i = 0; i < 3; ++i)
+          if (e[i]) cudaEventDestroy(e[i]);
+      }
+    } guard{ev};
+    if (timed) FE_CUDA(cudaEventRecord(ev[0], s));
     fe::validate_knn(d_idx, d_dist, n, k, index_offset, s);
     fe::UmapGraph g;
     fe::umap_build_graph(d_idx, d_dist, n, k, index_offset, g, s);
-    a.release();
+    if (timed) FE_CUDA(cudaEventRecord(ev[1], s));
     double av = 0.0, bv = 0.0;
     fe::umap_ab_params(1.0, min_dist, &av, &bv);
     const fe::UmapParams p{n, n_epochs, negative_sample_rate, seed, learning_rate, (float)av, (float)bv,
                            repulsion_strength};
     job.run(g.heads, g.neighbors, g.eps, g.nnz, p);
+    if (timed) FE_CUDA(cudaEventRecord(ev[2], s));
     FE_CUDA(cudaMemcpyAsync(out, job.y, sizeof(float) * 2 * n, cudaMemcpyDeviceToHost, s));
     FE_CUDA(cudaStreamSynchronize(s));
+    a.release();
+    if (graph_ms) FE_CUDA(cudaEventElapsedTime(graph_ms, ev[0], ev[1]));
+    if (sgd_ms) FE_CUDA(cudaEventElapsedTime(sgd_ms, ev[1], ev[2]));
   });
+}
+
+int fastembedr_cuda_umap_from_knn(const int* indices, const float* distances, const float* init, int n, int k,
+                                  int index_offset, int n_epochs, int negative_sample_rate, float learning_rate,
+                                  float min_dist, float repulsion_strength, unsigned int seed, float* out) {
+  return fastembedr_cuda_umap_from_knn_profile(indices, distances, init, n, k, index_offset, n_epochs,
+                                               negative_sample_rate, learning_rate, min_dist, repulsion_strength, seed,
+                                               out, nullptr, nullptr);
 }
 
 }  // extern "C"

@@ -8,6 +8,8 @@ distances, both ``(n, k)``; the C ABI takes them column-major (``np.asfortranarr
 * ``plain_umap_100k``: 100,000 x 50, 20 clusters, log-normal(sigma = 1) sizes, centres
   N(0, 3^2 I), per-dimension sd U(0.5, 2).
 * ``tsne_1m``: 1,000,000 x 50, 30 anisotropic clusters (diagonal sd U(0.5, 2)), log-normal sizes.
+* ``serving_transform``: a 500,000 x 50 reference of 20 clusters and a query pool, 95% drawn
+  from the same mixture and 5% uniform in the reference's bounding box.
 
 Points are shuffled so that index order carries no cluster locality.
 """
@@ -80,6 +82,45 @@ def exact_knn_torch(x, k, device="cuda", chunk=4096):
     finally:
         torch.backends.cuda.matmul.allow_tf32 = prev
     return idx, dist
+
+
+def exact_knn_query_torch(ref, queries, k, device="cuda", chunk=4096):
+    """Brute-force exact KNN of each query row among the reference rows (no self exclusion)."""
+    import torch
+
+    rt = torch.as_tensor(np.asarray(ref, np.float32), device=device)
+    qt = torch.as_tensor(np.asarray(queries, np.float32), device=device)
+    sq_r = (rt.double() ** 2).sum(1).float()
+    sq_q = (qt.double() ** 2).sum(1).float()
+    nq = qt.shape[0]
+    idx = torch.empty((nq, k), dtype=torch.int32, device=device)
+    dist = torch.empty((nq, k), dtype=torch.float32, device=device)
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        for s in range(0, nq, chunk):
+            e = min(nq, s + chunk)
+            d2 = sq_q[s:e, None] + sq_r[None, :] - 2.0 * (qt[s:e] @ rt.T)
+            d2.clamp_(min=0.0)
+            val, sel = torch.topk(d2, k, dim=1, largest=False, sorted=True)
+            idx[s:e] = sel.int()
+            dist[s:e] = val.sqrt()
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+    return idx, dist
+
+
+def serving_transform(seed=5, n_ref=500_000, n_pool=100_000, dim=50, n_clusters=20):
+    """Reference rows and a query pool for the serving transform: 20 clusters, centres
+    N(0, 4^2 I), within N(0, I); 95% of the pool from the same mixture, 5% uniform in the
+    reference's bounding box, shuffled."""
+    n_mix = int(round(0.95 * n_pool))
+    x, _ = mixture(n_ref + n_mix, dim, n_clusters, seed, centre_sd=4.0, within_sd=1.0)
+    ref, q_mix = x[:n_ref], x[n_ref:]
+    rng = np.random.default_rng(seed + 1)
+    q_uni = rng.uniform(ref.min(0), ref.max(0), (n_pool - n_mix, dim)).astype(np.float32)
+    pool = np.vstack([q_mix, q_uni])
+    return ref, pool[rng.permutation(n_pool)]
 
 
 def plain_tsne_10k(seed=1, n=10_000, k=90):

@@ -42,8 +42,8 @@ int fastembedr_cuda_opentsne_fft_grid_size(int n);
  * the gains/momentum optimizer with FFT-grid repulsion (grid nodes per side from
  * fastembedr_cuda_opentsne_fft_grid_size). learning_rate_auto: lr = n / exaggeration
  * of each phase. max_step_norm <= 0 or non-finite disables the step clip. has_init = 0 draws a
- * seeded N(0, 1e-4^2) layout. Repulsion interpolation: FASTEMBEDR_TSNE_INTERPOLATION=bilinear
- * selects the reference stencil, otherwise 3-node Lagrange boxes. */
+ * seeded N(0, 1e-4^2) layout. Repulsion interpolation: the reference's bilinear stencil;
+ * FASTEMBEDR_TSNE_INTERPOLATION=lagrange selects 3-node Lagrange boxes. */
 int fastembedr_cuda_opentsne_fft_from_knn_float(const int* indices, const float* distances, const float* init,
                                                 int has_init, int n, int k, int n_components, float perplexity,
                                                 int early_exaggeration_iter, int n_iter, float early_exaggeration,
@@ -98,6 +98,12 @@ int fastembedr_cuda_umap_graph_from_knn(const int* indices, const float* distanc
 int fastembedr_cuda_umap_from_knn(const int* indices, const float* distances, const float* init, int n, int k,
                                   int index_offset, int n_epochs, int negative_sample_rate, float learning_rate,
                                   float min_dist, float repulsion_strength, unsigned int seed, float* out);
+/* The same job, reporting device time (CUDA events on the job's stream) of the graph build and
+ * of the n_epochs SGD epochs; either output may be NULL. */
+int fastembedr_cuda_umap_from_knn_profile(const int* indices, const float* distances, const float* init, int n,
+                                          int k, int index_offset, int n_epochs, int negative_sample_rate,
+                                          float learning_rate, float min_dist, float repulsion_strength,
+                                          unsigned int seed, float* out, float* graph_ms, float* sgd_ms);
 
 /* ---------------------------------------------------------------- t-SNE diagnostics */
 
@@ -178,10 +184,14 @@ int fastembedr_transform_server_submit(fastembedr_transform_server* server, cons
  * 2 while still queued or running, 1 on error. */
 int fastembedr_transform_server_wait(fastembedr_transform_server* server, unsigned long long request_id, int timeout_ms,
                                      double* out, double* latency_ms);
+/* Counters since creation. device_ms / iterate_ms: summed device time of the groups (CUDA events
+ * on each group's stream: prepare + iterations / iterations only; overlapping groups each count
+ * their own span). largest_group_*: the iterate time of the group with the most queries. */
 int fastembedr_transform_server_stats(fastembedr_transform_server* server, unsigned long long* completed,
                                       unsigned long long* queries, unsigned long long* groups,
                                       unsigned long long* launches, unsigned long long* peak_bytes,
-                                      unsigned long long* budget_bytes);
+                                      unsigned long long* budget_bytes, double* device_ms, double* iterate_ms,
+                                      long long* largest_group_queries, double* largest_group_iterate_ms);
 /* Finishes the groups on the device, fails queued requests, frees everything. */
 void fastembedr_transform_server_destroy(fastembedr_transform_server* server);
 
