@@ -23,6 +23,18 @@ def _colmajor(a, dtype):
     return np.asfortranarray(np.asarray(a, dtype=dtype))
 
 
+def _settle(*tensors):
+    """The library reads device inputs on its own streams: finish the producer's stream first
+    (torch tensors written on a non-default stream are not covered by the legacy-stream order
+    the library applies itself)."""
+    for t in tensors:
+        if getattr(t, "is_cuda", False):
+            import torch
+
+            torch.cuda.current_stream(t.device).synchronize()
+            return
+
+
 def knn_index_offset(indices) -> int:
     """1 when every index lies in [1, n], else 0 (src/embedding_cuda_impl.cpp:933,
     src/tsne_neighbors.cpp:90-101)."""
@@ -176,6 +188,7 @@ class TsnePlan:
                  interpolation=0, seed=4):
         self.lib = _lib.require_gpu()
         self.n = int(n)
+        _settle(d_indices_cm, d_distances_cm)
         h = C.c_void_p()
         init_a = None if init is None else np.ascontiguousarray(init, np.float32)
         st = self.lib.fastembedr_tsne_plan_create(_lib.ptr(d_indices_cm), _lib.ptr(d_distances_cm),

@@ -54,3 +54,12 @@ int sm_count() {
 }
 
 }  // namespace fe
+
+void fe::order_after_legacy_stream(cudaStream_t s) {
+  cudaEvent_t e = nullptr;
+  FE_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  const cudaError_t r1 = cudaEventRecord(e, cudaStreamLegacy);
+  const cudaError_t r2 = r1 == cudaSuccess ? cudaStreamWaitEvent(s, e, 0) : r1;
+  cudaEventDestroy(e);
+  FE_CUDA(r2);
+}

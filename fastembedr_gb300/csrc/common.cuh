@@ -89,6 +89,12 @@ struct Stream {
 };
 
 inline int ceil_div(long long a, long long b) { return static_cast<int>((a + b - 1) / b); }
+
+// Entry points that read caller-owned device buffers run on their own non-blocking stream,
+// which does not wait for the legacy default stream. Order `s` after everything enqueued so far
+// on the legacy stream (and, through it, on every blocking stream) so that the caller's last
+// writes to those buffers are complete.
+void order_after_legacy_stream(cudaStream_t s);
 int sm_count();
 
 // ---------------------------------------------------------------- device helpers

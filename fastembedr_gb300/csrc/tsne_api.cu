@@ -66,6 +66,7 @@ struct TsneJob {
   void prepare(const int* d_idx, const float* d_dist, const float* init_host, int n, int k, float perplexity,
                int offset, int grid, int mode, unsigned seed) {
     cudaStream_t s = stream.s;
+    order_after_legacy_stream(s);  // d_idx / d_dist may be the caller's buffers
     validate_knn(d_idx, d_dist, n, k, offset, s);
     {
       float* d_p = nullptr;
@@ -173,6 +174,7 @@ int run_tsne_from_knn(const int* indices, const DistT* distances, bool on_device
                     early_exag, exag, lr, lr_auto, m0, m1, min_gain, out);
     auto job = std::make_unique<TsneJob>();
     cudaStream_t s = job->stream.s;
+    if (on_device) order_after_legacy_stream(s);
     const std::size_t items = (std::size_t)n * k;
     int* d_idx = nullptr;
     float* d_dist = nullptr;
