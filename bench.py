@@ -272,7 +272,7 @@ def run_gpu(args):
                 "traffic": None if tpn is None else tpn * nnz,
                 "algorithmic_bytes": alg_bytes, "avg_launch_ms": attr_ms,
                 "step_fraction_of_hbm": (8 * nnz + 60 * n) / (ms / args.steps * 1e-3) / 1e9 / peak}
-    launches = args.steps * info["launches_per_iteration"] + ((args.steps + 24) // 25) * 22
+    launches = args.steps * info["launches_per_iteration"] + ((args.steps + 24) // 25) * info["launches_per_reorder"]
 
     line = {
         "metric": "tsne_iterations_per_s_1M", "value": value, "unit": "iter/s", "n_gpus": world, "steps": args.steps,
@@ -574,6 +574,127 @@ def run_umap_reference(args):
     return 0
 
 
+BATCH_TSNE_ITERS = (250, 750)
+
+
+def _batched_instances(args, device):
+    """Instances of the batched workload: sizes log-uniform in [2,000, 200,000], each a 50-d
+    mixture of 5-15 clusters with exact KNN (k = 90 for t-SNE)."""
+    from fastembedr_gb300 import synthetic as S
+
+    rng = np.random.default_rng(23)
+    sizes = np.exp(rng.uniform(np.log(2_000), np.log(200_000), args.instances)).astype(np.int64)
+    knns = []
+    for j, n in enumerate(sizes):
+        x, _ = S.mixture(int(n), 50, int(rng.integers(5, 16)), 1000 + j, centre_sd=4.0, lognormal_sizes=True)
+        idx, dist = S.exact_knn_torch(x, K, device=device)
+        knns.append((idx.cpu().numpy(), dist.cpu().numpy()))
+    return knns
+
+
+def _run_batch(knns, inits, grid_policy, work):
+    """One batched job: create (affinities of every instance), 250 + 750 iterations timed with
+    CUDA events on the batch's stream, layouts back to the host; the wall clock covers it all."""
+    import torch
+
+    from fastembedr_gb300 import api
+
+    t0 = time.perf_counter()
+    b = api.TsneBatch(knns, inits=inits, grid_size=grid_policy)
+    t_create = time.perf_counter() - t0
+    info = b.info()
+    stream = torch.cuda.ExternalStream(b.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    b.iterate(BATCH_TSNE_ITERS[0], 12.0, 1.0 / 12.0)
+    b.iterate(BATCH_TSNE_ITERS[1], 1.0, 1.0 / 12.0)
+    e1.record(stream)
+    b.synchronize()
+    iter_ms = e0.elapsed_time(e1)
+    b.layouts()
+    wall = time.perf_counter() - t0
+    return b, {"grid_policy": grid_policy, "grid_classes": info["grid_classes"], "nnz_P": info["nnz"],
+               "iterations_value": work / (iter_ms * 1e-3), "ms_per_iteration": iter_ms / sum(BATCH_TSNE_ITERS),
+               "e2e_value": work / wall, "job_seconds": wall, "create_seconds": t_create,
+               "launches_per_iteration": info["launches_per_iteration"],
+               "launches_per_reorder": info["launches_per_reorder"]}
+
+
+def run_batched(args):
+    """Batched t-SNE: many instances per launch against one instance per call, with the CUDA
+    grid-size policy and with the adaptive box count."""
+    import torch
+
+    from fastembedr_gb300 import api
+    from fastembedr_gb300 import synthetic as S
+
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    knns = _batched_instances(args, f"cuda:{local}")
+    torch.cuda.empty_cache()
+    sizes = np.array([i.shape[0] for i, _ in knns])
+    iters = sum(BATCH_TSNE_ITERS)
+    inits = [S.tsne_init(int(n), seed=40 + j) for j, n in enumerate(sizes)]
+    work = float(sizes.sum()) * iters
+    with api.TsneBatch(knns[:3], inits=inits[:3]) as w:  # warm-up
+        w.iterate(5, 12.0, 1.0 / 12.0)
+        w.synchronize()
+    # plain form on a size-stratified subset: every `stride`-th instance by size, one call each
+    order = np.argsort(sizes)
+    subset = order[:: max(1, args.plain_stride)]
+    kl_rows = [j for j in subset if sizes[j] <= 60_000][: args.kl_instances]
+    plain_t, plain_work, plain_kl = 0.0, 0.0, {}
+    for j in subset:
+        idx, dist = knns[j]
+        t = time.perf_counter()
+        fit = api.tsne_knn(idx, dist, perplexity=PERPLEXITY, Y_init=inits[j], n_iter=BATCH_TSNE_ITERS[1])
+        plain_t += time.perf_counter() - t
+        plain_work += float(sizes[j]) * iters
+        if j in kl_rows:
+            with api.TsneBatch([(idx, dist)], inits=[fit.layout]) as one:  # exact KL of the given layout
+                plain_kl[int(j)] = one.kl(0)
+    plain_rate = plain_work / plain_t
+    clocks = ClockSampler(local)
+    runs = {}
+    for policy in ("cuda", "adaptive"):
+        b, r = _run_batch(knns, inits, policy, work)
+        r["kl_vs_plain"] = [{"n": int(sizes[j]), "kl_batched": b.kl(int(j)), "kl_plain": plain_kl[int(j)]}
+                            for j in kl_rows]
+        for e in r["kl_vs_plain"]:
+            e["rel"] = (e["kl_batched"] - e["kl_plain"]) / e["kl_plain"]
+        r["max_abs_kl_rel"] = max(abs(e["rel"]) for e in r["kl_vs_plain"]) if r["kl_vs_plain"] else None
+        r["vs_plain_e2e"] = r["e2e_value"] / plain_rate
+        b.close()
+        runs[policy] = r
+    clk = clocks.stop()
+    head = runs["adaptive"]
+    line = {
+        "metric": "batched_tsne_points_iterations_per_s", "value": head["iterations_value"],
+        "unit": "points*iterations/s", "n_gpus": 1, "steps": iters, "warmup": 1,
+        "ms_per_step": head["ms_per_iteration"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "batched_tsne_knn_sizes_2k_200k_k90", "instances": len(knns),
+                   "points": int(sizes.sum()), "iterations": list(BATCH_TSNE_ITERS), "perplexity": PERPLEXITY,
+                   "grid_policy": "adaptive box count (node spacing <= 0.7, re-chosen every 25 iterations)",
+                   "nnz_P": head["nnz_P"],
+                   "l2": "P of the batch (%.1f GB) exceeds L2; no flush" % (8 * head["nnz_P"] / 1e9)},
+        "e2e": {"value": head["e2e_value"], "unit": "points*iterations/s",
+                "h2d_bytes_per_step": int(sum(i.nbytes + d.nbytes for i, d in knns) / iters),
+                "d2h_bytes_per_step": int(sizes.sum() * 8 / iters), "job_seconds": head["job_seconds"],
+                "job": "batch create (affinities of every instance) + 250 + 750 iterations + layouts"},
+        "plain_gpu": {"value": plain_rate, "unit": "points*iterations/s", "instances": int(len(subset)),
+                      "form": "fastembedr_cuda_opentsne_fft_from_knn_float once per instance, CUDA size policy "
+                              f"(every {max(1, args.plain_stride)}th instance by size)"},
+        "batched": runs, "batched_vs_plain_e2e": head["vs_plain_e2e"],
+        "clocks": clk, "gpu_launches": iters * head["launches_per_iteration"] + (
+            (BATCH_TSNE_ITERS[0] + 24) // 25 + (BATCH_TSNE_ITERS[1] + 24) // 25) * head["launches_per_reorder"],
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -585,8 +706,12 @@ def main():
     ap.add_argument("--no-kl", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--n", type=int, default=N_POINTS, help="points (profiling captures use a smaller case)")
-    ap.add_argument("--workload", default="tsne", choices=["tsne", "serving", "umap"],
-                    help="tsne: the headline 1M-point optimizer; serving: transform_tsne served; umap: 100k UMAP")
+    ap.add_argument("--workload", default="tsne", choices=["tsne", "serving", "umap", "batched"],
+                    help="tsne: the headline 1M-point optimizer; serving: transform_tsne served; umap: 100k UMAP; "
+                         "batched: many t-SNE instances per launch")
+    ap.add_argument("--instances", type=int, default=256)
+    ap.add_argument("--plain-stride", type=int, default=4)
+    ap.add_argument("--kl-instances", type=int, default=6)
     ap.add_argument("--n-ref", type=int, default=SERVE_N_REF)
     ap.add_argument("--requests", type=int, default=160)
     ap.add_argument("--plain-requests", type=int, default=60)
@@ -598,6 +723,12 @@ def main():
         return run_serving_reference(args) if args.impl == "reference" else run_serving(args)
     if args.workload == "umap":
         return run_umap_reference(args) if args.impl == "reference" else run_umap(args)
+    if args.workload == "batched":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the batched form has no CPU counterpart; "
+                                                                  "per-instance CPU timing is the tsne workload's"}))
+            return 0
+        return run_batched(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

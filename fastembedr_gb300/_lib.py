@@ -55,9 +55,20 @@ SIGNATURES = {
     "fastembedr_tsne_plan_synchronize": (I, [vp]),
     "fastembedr_tsne_plan_stream": (vp, [vp]),
     "fastembedr_tsne_plan_layout": (I, [vp, vp]),
-    "fastembedr_tsne_plan_info": (I, [vp, C.POINTER(L), C.POINTER(I), C.POINTER(I), C.POINTER(I)]),
+    "fastembedr_tsne_plan_info": (I, [vp, C.POINTER(L), C.POINTER(I), C.POINTER(I), C.POINTER(I), C.POINTER(I)]),
     "fastembedr_tsne_plan_kl": (I, [vp, C.POINTER(D)]),
     "fastembedr_tsne_plan_destroy": (None, [vp]),
+    "fastembedr_tsne_batch_create": (I, [I, vp, vp, vp, vp, I, F, I, I, I, U, C.POINTER(vp)]),
+    "fastembedr_tsne_batch_run": (I, [vp, I, I, F, F, F, F, F, F, F]),
+    "fastembedr_tsne_batch_iterate": (I, [vp, I, F, F, F, F, F]),
+    "fastembedr_tsne_batch_synchronize": (I, [vp]),
+    "fastembedr_tsne_batch_stream": (vp, [vp]),
+    "fastembedr_tsne_batch_layout": (I, [vp, vp]),
+    "fastembedr_tsne_batch_kl": (I, [vp, I, C.POINTER(D)]),
+    "fastembedr_tsne_batch_info": (I, [vp, C.POINTER(L), C.POINTER(L), C.POINTER(I), C.POINTER(I), C.POINTER(I)]),
+    "fastembedr_tsne_batch_grids": (I, [vp, vp, C.POINTER(I)]),
+    "fastembedr_tsne_batch_destroy": (None, [vp]),
+    "fastembedr_cuda_tsne_batch_from_knn": (I, [I, vp, vp, vp, vp, I, F, I, I, F, F, F, F, F, F, F, U, I, vp]),
 }
 
 

@@ -224,10 +224,11 @@ class TsnePlan:
         return out
 
     def info(self):
-        nnz, g, it, la = C.c_longlong(), C.c_int(), C.c_int(), C.c_int()
-        _lib.check(self.lib.fastembedr_tsne_plan_info(self.h, C.byref(nnz), C.byref(g), C.byref(it), C.byref(la)),
-                   "t-SNE plan info")
-        return dict(nnz=nnz.value, grid_size=g.value, interpolation=it.value, launches_per_iteration=la.value)
+        nnz, g, it, la, lr = C.c_longlong(), C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        _lib.check(self.lib.fastembedr_tsne_plan_info(self.h, C.byref(nnz), C.byref(g), C.byref(it), C.byref(la),
+                                                      C.byref(lr)), "t-SNE plan info")
+        return dict(nnz=nnz.value, grid_size=g.value, interpolation=it.value, launches_per_iteration=la.value,
+                    launches_per_reorder=lr.value)
 
     def kl(self):
         v = C.c_double()
@@ -247,6 +248,119 @@ class TsnePlan:
 
 
 # ---------------------------------------------------------------------------- UMAP
+def _concat_knn(knns):
+    """Column-major KNN blocks of the instances, one after another (int32 / float32)."""
+    idx = np.concatenate([np.asfortranarray(np.asarray(i, np.int32)).ravel(order="F") for i, _ in knns])
+    dist = np.concatenate([np.asfortranarray(np.asarray(d, np.float32)).ravel(order="F") for _, d in knns])
+    return idx, dist
+
+
+class TsneBatch:
+    """Many independent t-SNE instances optimised together (C ABI fastembedr_tsne_batch_*).
+
+    ``knns`` is a list of ``(indices, distances)`` pairs, one (n_b, k) KNN per instance with its
+    own 0- or 1-based row numbers. Every instance follows the single-instance algorithm with its
+    own grid, bounding box, Z and learning rate (opt-SNE: n_b / early exaggeration). ``grid_size``:
+    "cuda" (the CUDA size policy, 256 / 512 / 1024 nodes by n), "cpu" (the reference CPU policy,
+    128 / 256), "adaptive" (per instance and per 25-iteration chunk, the smallest grid of at least
+    128 nodes with node spacing <= 0.7 over the current layout) or a power of two for every
+    instance."""
+
+    def __init__(self, knns, perplexity=30.0, inits=None, grid_size="cuda", interpolation=0, seed=4):
+        grid_size = {"cuda": 0, "cpu": -1, "adaptive": -2}.get(grid_size, grid_size)
+        if not knns:
+            raise ValueError("at least one instance is required")
+        ks = {np.asarray(i).shape[1] for i, _ in knns}
+        if len(ks) != 1:
+            raise ValueError("every instance needs the same number of neighbours")
+        self.k = ks.pop()
+        self.sizes = np.array([np.asarray(i).shape[0] for i, _ in knns], np.int32)
+        offs = {knn_index_offset(i) for i, _ in knns}
+        off = 1 if offs == {1} else 0
+        idx, dist = _concat_knn(knns)
+        init = None
+        if inits is not None:
+            init = np.concatenate([np.ascontiguousarray(y, np.float32).ravel() for y in inits])
+        self.lib = _lib.require_gpu()
+        self.h = C.c_void_p()
+        st = self.lib.fastembedr_tsne_batch_create(len(knns), self.sizes.ctypes.data, idx.ctypes.data,
+                                                   dist.ctypes.data, None if init is None else init.ctypes.data,
+                                                   self.k, float(perplexity), off, int(grid_size), int(interpolation),
+                                                   int(seed) & 0xFFFFFFFF, C.byref(self.h))
+        _lib.check(st, "t-SNE batch create")
+
+    @property
+    def stream(self):
+        return self.lib.fastembedr_tsne_batch_stream(self.h)
+
+    def run(self, early_exaggeration_iter=250, n_iter=750, early_exaggeration=12.0, exaggeration=1.0,
+            learning_rate="auto", initial_momentum=0.8, final_momentum=0.8, min_gain=0.01, max_step_norm=5.0):
+        """learning_rate: per-point factor (instance b uses learning_rate x n_b in both phases);
+        "auto" is the package's opt-SNE rate n_b / early_exaggeration."""
+        lr = -1.0 if learning_rate == "auto" else float(learning_rate)
+        _lib.check(self.lib.fastembedr_tsne_batch_run(self.h, int(early_exaggeration_iter), int(n_iter),
+                                                      float(early_exaggeration), float(exaggeration), lr,
+                                                      float(initial_momentum), float(final_momentum), float(min_gain),
+                                                      float(max_step_norm)), "t-SNE batch run")
+
+    def iterate(self, iters, exaggeration, learning_rate_per_point, momentum=0.8, min_gain=0.01, max_step_norm=5.0):
+        _lib.check(self.lib.fastembedr_tsne_batch_iterate(self.h, int(iters), float(exaggeration),
+                                                          float(learning_rate_per_point), float(momentum),
+                                                          float(min_gain), float(max_step_norm)), "t-SNE batch iterate")
+
+    def synchronize(self):
+        _lib.check(self.lib.fastembedr_tsne_batch_synchronize(self.h), "t-SNE batch synchronize")
+
+    def layouts(self):
+        out = np.zeros((int(self.sizes.sum()), 2), np.float32)
+        _lib.check(self.lib.fastembedr_tsne_batch_layout(self.h, out.ctypes.data), "t-SNE batch layout")
+        return np.split(out, np.cumsum(self.sizes)[:-1])
+
+    def kl(self, instance):
+        v = C.c_double()
+        _lib.check(self.lib.fastembedr_tsne_batch_kl(self.h, int(instance), C.byref(v)), "t-SNE batch KL")
+        return v.value
+
+    def grids(self):
+        g = np.zeros(len(self.sizes), np.int32)
+        r = C.c_int()
+        _lib.check(self.lib.fastembedr_tsne_batch_grids(self.h, g.ctypes.data, C.byref(r)), "t-SNE batch grids")
+        return g, r.value
+
+    def info(self):
+        nnz, pts, gc, la, lr = C.c_longlong(), C.c_longlong(), C.c_int(), C.c_int(), C.c_int()
+        _lib.check(self.lib.fastembedr_tsne_batch_info(self.h, C.byref(nnz), C.byref(pts), C.byref(gc), C.byref(la),
+                                                       C.byref(lr)), "t-SNE batch info")
+        return dict(nnz=nnz.value, points=pts.value, grid_classes=gc.value, launches_per_iteration=la.value,
+                    launches_per_reorder=lr.value)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fastembedr_tsne_batch_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def tsne_knn_batch(knns, perplexity=30.0, inits=None, seed=4, early_exaggeration_iter=250, n_iter=750,
+                   early_exaggeration=12.0, exaggeration=1.0, max_step_norm=5.0, grid_size="cuda"):
+    """tsne_knn over many instances at once: the package schedule (opt-SNE learning rate per
+    instance) on every instance; returns one (n_b, 2) layout per instance."""
+    with TsneBatch(knns, perplexity=perplexity, inits=inits, seed=seed, grid_size=grid_size) as b:
+        b.run(early_exaggeration_iter, n_iter, early_exaggeration, exaggeration, max_step_norm=max_step_norm)
+        return b.layouts()
+
+
 @dataclass
 class UmapFit:
     layout: np.ndarray

@@ -50,6 +50,7 @@ void radix_sort_pairs(unsigned* keys, int* vals, unsigned* keys_tmp, int* vals_t
 // Grid policy of the reference CUDA path (src/embedding_cuda_kernels.cpp:5610-5623), including
 // the FASTEMBEDR_TSNE_FFT_GRID override.
 int cuda_fft_grid_size(int n);
+int cpu_fft_grid_size(int n);
 
 // Interpolation scheme of the grid repulsion.
 enum InterpMode { kInterpBilinear = 0, kInterpLagrange3 = 1 };

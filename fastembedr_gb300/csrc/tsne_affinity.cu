@@ -512,6 +512,10 @@ int cuda_fft_grid_size(int n) {
   return g;
 }
 
+// The reference CPU policy (tsne_fft_grid_size, src/tsne_neighbors.cpp:403-413 without its
+// environment override): 128 nodes per side below 50,000 points, 256 from there.
+int cpu_fft_grid_size(int n) { return n >= 50000 ? 256 : 128; }
+
 // Default: the reference's bilinear stencil. FASTEMBEDR_TSNE_INTERPOLATION=lagrange selects
 // 3-node Lagrange boxes (more accurate forces in L2, but an interpolant that is discontinuous
 // at box edges, which measurably degrades the local neighbourhood structure of the result).

@@ -2,6 +2,8 @@
 // the GB300 counterpart of fastembedr_cuda_opentsne_fft_from_knn_impl
 // (fastEmbedR src/embedding_cuda_kernels.cpp:5629-6176) and of the validation in
 // knn_tsne_opentsne_cuda_float_impl (src/embedding_cuda_impl.cpp:2239-2370).
+#include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -47,7 +49,18 @@ bool graph_capture_enabled() {
            std::strcmp(env, "no") == 0 || std::strcmp(env, "NO") == 0);
 }
 
-// Optimizer state of one t-SNE instance resident on the device.
+// Append one instance's CSR to the batch CSR: rows shifted by the instance's nnz offset, columns
+// by its first slot; the last instance's end offset closes row_ptr.
+__global__ void append_csr_kernel(const int* __restrict__ rp, const int* __restrict__ col, int n, long long nnz,
+                                  int nnz_off, int first, int* __restrict__ rp_out, int* __restrict__ col_out) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t <= n; t += stride)
+    rp_out[t] = nnz_off + rp[t];
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nnz; t += stride)
+    col_out[t] = col[t] + first;
+}
+
+// Optimizer state of one t-SNE instance (or a batch of instances) resident on the device.
 struct TsneJob {
   DeviceCsr P;
   TsneDevice D;
@@ -55,17 +68,56 @@ struct TsneJob {
   // graph cache keyed by (iterations, exaggeration, lr, momentum, min_gain, max_step)
   using Key = std::tuple<int, float, float, float, float, float>;
   std::map<Key, std::pair<cudaGraph_t, cudaGraphExec_t>> graphs;
-  ~TsneJob() {
+  // Adaptive box count: at the start of every chunk each instance gets the smallest power-of-two
+  // grid whose node spacing over its current bounding square is at most `spacing` (clamped to
+  // [grid_min, grid_max]); grids grow at once and shrink only when four times too fine.
+  bool adaptive = false;
+  float spacing = 0.7f;
+  int grid_min = 128, grid_max = 1024;
+  int regrids = 0;
+  ~TsneJob() { clear_graphs(); }
+  void clear_graphs() {
     for (auto& kv : graphs) {
       if (kv.second.second) cudaGraphExecDestroy(kv.second.second);
       if (kv.second.first) cudaGraphDestroy(kv.second.first);
     }
+    graphs.clear();
+  }
+  // Adaptive grids when asked for, or when FASTEMBEDR_TSNE_FFT_GRID=adaptive; the target spacing
+  // comes from FASTEMBEDR_TSNE_GRID_SPACING when set.
+  void configure_adaptive(bool on) {
+    const char* env = std::getenv("FASTEMBEDR_TSNE_FFT_GRID");
+    adaptive = on || (env && std::strcmp(env, "adaptive") == 0);
+    const char* sp = std::getenv("FASTEMBEDR_TSNE_GRID_SPACING");
+    if (sp && sp[0]) {
+      const float v = (float)std::atof(sp);
+      if (v > 0.0f && std::isfinite(v)) spacing = v;
+    }
+  }
+  void adapt_grids() {
+    cudaStream_t s = stream.s;
+    const std::vector<float> ext = tsne_grid_extents(D, s);
+    std::vector<int> grids(D.inst.size());
+    bool changed = false;
+    for (std::size_t b = 0; b < grids.size(); ++b) {
+      const float need = (std::isfinite(ext[b]) ? ext[b] : 0.0f) / spacing + 1.0f;
+      int g = grid_min;
+      while (g < grid_max && (float)g < need) g <<= 1;
+      const int cur = D.inst[b].grid;
+      grids[b] = (g > cur || 4 * g <= cur) ? g : cur;
+      changed |= grids[b] != cur;
+    }
+    if (!changed) return;
+    clear_graphs();
+    tsne_regrid(D, grids, s);
+    ++regrids;
   }
 
   // KNN (device, column-major) -> P (CSR) -> optimizer state with the given init.
   void prepare(const int* d_idx, const float* d_dist, const float* init_host, int n, int k, float perplexity,
                int offset, int grid, int mode, unsigned seed) {
     cudaStream_t s = stream.s;
+    configure_adaptive(false);
     order_after_legacy_stream(s);  // d_idx / d_dist may be the caller's buffers
     validate_knn(d_idx, d_dist, n, k, offset, s);
     {
@@ -91,6 +143,104 @@ struct TsneJob {
     FE_CUDA(cudaStreamSynchronize(s));
   }
 
+  // Batch: instances in table order (equal grids consecutive); `user` maps table position to
+  // the caller's instance index. KNN / init are the caller's host arrays, instance after
+  // instance. P of every instance is built on its own and appended to one CSR whose rows and
+  // columns are offset by the instance's first slot.
+  std::vector<int> user, user_off;
+  void prepare_batch(int ninst, const int* sizes, const int* idx_h, const float* dist_h, const float* init_h, int k,
+                     float perplexity, int offset, int grid_size, int mode, unsigned seed) {
+    cudaStream_t s = stream.s;
+    std::vector<int> grid_u(ninst);
+    user_off.assign(ninst + 1, 0);
+    for (int u = 0; u < ninst; ++u) {
+      if (sizes[u] < 2) throw Error("t-SNE batch: every instance needs at least two points");
+      grid_u[u] = grid_size > 0 ? grid_size
+                                : (grid_size == -1 ? cpu_fft_grid_size(sizes[u])
+                                                   : (grid_size == -2 ? grid_min : default_grid_size(sizes[u], mode)));
+      user_off[u + 1] = user_off[u] + sizes[u];
+    }
+    user.resize(ninst);
+    for (int u = 0; u < ninst; ++u) user[u] = u;
+    std::stable_sort(user.begin(), user.end(), [&](int a, int b) { return grid_u[a] > grid_u[b]; });
+    std::vector<int> sz(ninst), gr(ninst);
+    std::vector<float> lr(ninst);
+    int max_n = 0;
+    for (int t = 0; t < ninst; ++t) {
+      sz[t] = sizes[user[t]];
+      gr[t] = grid_u[user[t]];
+      lr[t] = (float)sz[t];
+      max_n = std::max(max_n, sz[t]);
+    }
+    tsne_batch_alloc(D, sz, gr, lr, mode);
+    const int n = D.n;
+    std::vector<std::unique_ptr<DeviceCsr>> parts(ninst);
+    long long total_nnz = 0;
+    double total_mass = 0.0;
+    {
+      int* d_idx = nullptr;
+      float* d_dist = nullptr;
+      float* d_p = nullptr;
+      Arena tmp;
+      tmp.reserve(&d_idx, (std::size_t)max_n * k);
+      tmp.reserve(&d_dist, (std::size_t)max_n * k);
+      tmp.reserve(&d_p, (std::size_t)max_n * k);
+      tmp.commit("t-SNE batch affinities");
+      for (int t = 0; t < ninst; ++t) {
+        const int u = user[t], nb = sz[t];
+        const std::size_t items = (std::size_t)nb * k, at = (std::size_t)user_off[u] * k;
+        FE_CUDA(cudaMemcpyAsync(d_idx, idx_h + at, sizeof(int) * items, cudaMemcpyHostToDevice, s));
+        FE_CUDA(cudaMemcpyAsync(d_dist, dist_h + at, sizeof(float) * items, cudaMemcpyHostToDevice, s));
+        validate_knn(d_idx, d_dist, nb, k, offset, s);
+        row_probabilities(d_idx, d_dist, nb, k, perplexity, d_p, nullptr, s);
+        parts[t] = std::make_unique<DeviceCsr>();
+        symmetrise(d_idx, d_p, nb, k, offset, *parts[t], s);
+        total_nnz += parts[t]->nnz;
+        total_mass += parts[t]->total_mass;
+      }
+    }
+    if (total_nnz > INT_MAX) throw Error("t-SNE batch: more than 2^31 affinities; split the batch");
+    P.n = n;
+    P.nnz = total_nnz;
+    P.total_mass = total_mass;
+    P.arena.release();
+    P.arena.reserve(&P.row_ptr, (std::size_t)n + 1);
+    P.arena.reserve(&P.col, (std::size_t)std::max<long long>(total_nnz, 1));
+    P.arena.reserve(&P.val, (std::size_t)std::max<long long>(total_nnz, 1));
+    P.arena.commit("t-SNE batch P");
+    long long nnz_off = 0;
+    for (int t = 0; t < ninst; ++t) {
+      const DeviceCsr& q = *parts[t];
+      const int first = D.inst[t].pt_begin;
+      append_csr_kernel<<<std::max(1, std::min(ceil_div(std::max<long long>(q.nnz, q.n + 1), 256), sm_count() * 8)),
+                          256, 0, s>>>(q.row_ptr, q.col, q.n, q.nnz, (int)nnz_off, first, P.row_ptr + first,
+                                       P.col + nnz_off);
+      FE_LAUNCH("append_csr_kernel");
+      FE_CUDA(cudaMemcpyAsync(P.val + nnz_off, q.val, sizeof(float) * q.nnz, cudaMemcpyDeviceToDevice, s));
+      nnz_off += q.nnz;
+    }
+    FE_CUDA(cudaStreamSynchronize(s));
+    parts.clear();
+    float2* d_init = nullptr;
+    Arena tmp;
+    tmp.reserve(&d_init, n);
+    tmp.commit("t-SNE batch init");
+    for (int t = 0; t < ninst; ++t) {
+      const int u = user[t];
+      float2* dst = d_init + D.inst[t].pt_begin;
+      if (init_h) {
+        FE_CUDA(cudaMemcpyAsync(dst, init_h + 2 * (std::size_t)user_off[u], sizeof(float2) * sz[t],
+                                cudaMemcpyHostToDevice, s));
+      } else {
+        random_init_kernel<<<std::max(1, std::min(ceil_div(sz[t], 256), sm_count() * 8)), 256, 0, s>>>(dst, sz[t],
+                                                                                                      seed);
+        FE_LAUNCH("random_init_kernel");
+      }
+    }
+    tsne_device_init(D, reinterpret_cast<const float*>(d_init), s);
+    FE_CUDA(cudaStreamSynchronize(s));
+  }
+
   // Iterations in chunks of 25; each chunk starts with a spatial reorder of the points and
   // is one CUDA graph launch (two streams inside).
   void run(int iters, float exag, float lr, float mom, float min_gain, float max_step, bool use_graph) {
@@ -102,6 +252,7 @@ struct TsneJob {
     int left = iters;
     while (left > 0) {
       const int c = std::min(kChunk, left);
+      if (adaptive) adapt_grids();
       if (!graph) {
         if (reorder) tsne_reorder(D, P, s);
         for (int r = 0; r < c; ++r) tsne_iteration(D, P, exag, lr, mom, min_gain, max_step, s);
@@ -217,6 +368,10 @@ int run_tsne_from_knn(const int* indices, const DistT* distances, bool on_device
 }  // namespace fe
 
 struct fastembedr_tsne_plan {
+  fe::TsneJob job;
+};
+
+struct fastembedr_tsne_batch {
   fe::TsneJob job;
 };
 
@@ -449,13 +604,14 @@ int fastembedr_tsne_plan_layout(fastembedr_tsne_plan* plan, float* out) {
 }
 
 int fastembedr_tsne_plan_info(fastembedr_tsne_plan* plan, long long* nnz, int* grid_size, int* interpolation,
-                              int* launches) {
+                              int* launches, int* launches_per_reorder) {
   return fe::guarded([&] {
     if (!plan) throw fe::Error("null CUDA t-SNE plan");
     if (nnz) *nnz = plan->job.P.nnz;
     if (grid_size) *grid_size = plan->job.D.grid;
     if (interpolation) *interpolation = plan->job.D.mode;
-    if (launches) *launches = fe::tsne_launches_per_iteration();
+    if (launches) *launches = fe::tsne_launches_per_iteration(plan->job.D);
+    if (launches_per_reorder) *launches_per_reorder = fe::tsne_reorder_launches(plan->job.D);
   });
 }
 
@@ -482,5 +638,143 @@ int fastembedr_tsne_plan_kl(fastembedr_tsne_plan* plan, double* kl) {
 }
 
 void fastembedr_tsne_plan_destroy(fastembedr_tsne_plan* plan) { delete plan; }
+
+// ---------------------------------------------------------------- batches
+int fastembedr_tsne_batch_create(int n_instances, const int* sizes, const int* indices, const float* distances,
+                                 const float* init, int k, float perplexity, int index_offset, int grid_size,
+                                 int interpolation, unsigned int seed, fastembedr_tsne_batch** batch) {
+  return fe::guarded([&] {
+    if (!sizes || !indices || !distances || !batch) throw fe::Error("null CUDA t-SNE batch pointer");
+    if (n_instances < 1 || k < 1 || k > 1024 || !(perplexity > 0.0f))
+      throw fe::Error("invalid CUDA t-SNE batch parameters");
+    if (grid_size > 0 && (grid_size < 8 || grid_size > 2048 || (grid_size & (grid_size - 1)) != 0))
+      throw fe::Error("`grid_size` must be a power of two between 8 and 2048.");
+    if (grid_size < -2)
+      throw fe::Error("`grid_size`: 0 (CUDA size policy), -1 (CPU size policy), -2 (adaptive) or a size");
+    const int mode = interpolation == 0 ? fe::kInterpBilinear : fe::kInterpLagrange3;
+    auto b = std::make_unique<fastembedr_tsne_batch>();
+    b->job.configure_adaptive(grid_size == -2);
+    b->job.prepare_batch(n_instances, sizes, indices, distances, init, k, perplexity, index_offset, grid_size, mode,
+                         seed);
+    *batch = b.release();
+  });
+}
+
+int fastembedr_tsne_batch_iterate(fastembedr_tsne_batch* batch, int iters, float exaggeration, float learning_rate,
+                                  float momentum, float min_gain, float max_step_norm) {
+  return fe::guarded([&] {
+    if (!batch || iters < 0) throw fe::Error("invalid CUDA t-SNE batch run");
+    batch->job.run(iters, exaggeration, learning_rate, momentum, min_gain, max_step_norm, true);
+  });
+}
+
+int fastembedr_tsne_batch_run(fastembedr_tsne_batch* batch, int early_exaggeration_iter, int n_iter,
+                              float early_exaggeration, float exaggeration, float learning_rate,
+                              float initial_momentum, float final_momentum, float min_gain, float max_step_norm) {
+  return fe::guarded([&] {
+    if (!batch || early_exaggeration_iter < 0 || n_iter < 0 || !(early_exaggeration > 0.0f) ||
+        !(exaggeration > 0.0f) || !(min_gain > 0.0f))
+      throw fe::Error("invalid CUDA t-SNE batch schedule");
+    // opt-SNE rate of the package's auto configuration: n_b / early_exaggeration in both phases
+    const float lr = learning_rate > 0.0f ? learning_rate : 1.0f / early_exaggeration;
+    fe::TsneJob& J = batch->job;
+    J.run(early_exaggeration_iter, early_exaggeration, lr, initial_momentum, min_gain, max_step_norm, true);
+    J.run(n_iter, exaggeration, lr, final_momentum, min_gain, max_step_norm, true);
+    FE_CUDA(cudaStreamSynchronize(J.stream.s));
+  });
+}
+
+int fastembedr_tsne_batch_synchronize(fastembedr_tsne_batch* batch) {
+  return fe::guarded([&] {
+    if (!batch) throw fe::Error("null CUDA t-SNE batch");
+    FE_CUDA(cudaStreamSynchronize(batch->job.stream.s));
+  });
+}
+
+void* fastembedr_tsne_batch_stream(fastembedr_tsne_batch* batch) {
+  return batch ? static_cast<void*>(batch->job.stream.s) : nullptr;
+}
+
+int fastembedr_tsne_batch_layout(fastembedr_tsne_batch* batch, float* out) {
+  return fe::guarded([&] {
+    if (!batch || !out) throw fe::Error("null CUDA t-SNE batch or output");
+    fe::TsneJob& J = batch->job;
+    cudaStream_t s = J.stream.s;
+    float* d_out = nullptr;
+    fe::Arena tmp;
+    tmp.reserve(&d_out, 2 * (std::size_t)J.D.n);
+    tmp.commit("t-SNE batch output");
+    fe::tsne_finalize(J.D, d_out, s);
+    for (std::size_t t = 0; t < J.user.size(); ++t) {
+      const int u = J.user[t];
+      FE_CUDA(cudaMemcpyAsync(out + 2 * (std::size_t)J.user_off[u], d_out + 2 * (std::size_t)J.D.inst[t].pt_begin,
+                              sizeof(float) * 2 * J.D.inst[t].n, cudaMemcpyDeviceToHost, s));
+    }
+    FE_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int fastembedr_tsne_batch_kl(fastembedr_tsne_batch* batch, int instance, double* kl) {
+  return fe::guarded([&] {
+    if (!batch || !kl) throw fe::Error("null CUDA t-SNE batch or output");
+    fe::TsneJob& J = batch->job;
+    if (instance < 0 || instance >= (int)J.user.size()) throw fe::Error("t-SNE batch: instance out of range");
+    int t = 0;
+    while (J.user[t] != instance) ++t;
+    const fe::TsneInstance& I = J.D.inst[t];
+    cudaStream_t s = J.stream.s;
+    double *d_zrow = nullptr, *d_work = nullptr, *d_sc = nullptr;
+    fe::Arena a;
+    a.reserve(&d_zrow, I.n);
+    a.reserve(&d_work, I.n);
+    a.reserve(&d_sc, 2);
+    a.commit("t-SNE batch KL");
+    fe::exact_kl_range(J.P.row_ptr + I.pt_begin, J.P.col, J.P.val, I.n, reinterpret_cast<const float*>(J.D.y),
+                       J.D.inv + I.pt_begin, I.pt_begin, d_zrow, d_work, d_sc, s);
+    FE_CUDA(cudaMemcpyAsync(kl, d_sc + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
+    FE_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int fastembedr_tsne_batch_info(fastembedr_tsne_batch* batch, long long* nnz, long long* points, int* grid_classes,
+                               int* launches_per_iteration, int* launches_per_reorder) {
+  return fe::guarded([&] {
+    if (!batch) throw fe::Error("null CUDA t-SNE batch");
+    fe::TsneJob& J = batch->job;
+    if (nnz) *nnz = J.P.nnz;
+    if (points) *points = J.D.n;
+    if (grid_classes) *grid_classes = (int)J.D.classes.size();
+    if (launches_per_iteration) *launches_per_iteration = fe::tsne_launches_per_iteration(J.D);
+    if (launches_per_reorder) *launches_per_reorder = fe::tsne_reorder_launches(J.D);
+  });
+}
+
+int fastembedr_tsne_batch_grids(fastembedr_tsne_batch* batch, int* grids, int* regrids) {
+  return fe::guarded([&] {
+    if (!batch) throw fe::Error("null CUDA t-SNE batch");
+    fe::TsneJob& J = batch->job;
+    if (grids)
+      for (std::size_t t = 0; t < J.user.size(); ++t) grids[J.user[t]] = J.D.inst[t].grid;
+    if (regrids) *regrids = J.regrids;
+  });
+}
+
+void fastembedr_tsne_batch_destroy(fastembedr_tsne_batch* batch) { delete batch; }
+
+int fastembedr_cuda_tsne_batch_from_knn(int n_instances, const int* sizes, const int* indices, const float* distances,
+                                        const float* init, int k, float perplexity, int early_exaggeration_iter,
+                                        int n_iter, float early_exaggeration, float exaggeration, float learning_rate,
+                                        float initial_momentum, float final_momentum, float min_gain,
+                                        float max_step_norm, unsigned int seed, int index_offset, float* out) {
+  fastembedr_tsne_batch* b = nullptr;
+  int st = fastembedr_tsne_batch_create(n_instances, sizes, indices, distances, init, k, perplexity, index_offset, 0,
+                                        fe::interp_mode_from_env(), seed, &b);
+  if (st == 0)
+    st = fastembedr_tsne_batch_run(b, early_exaggeration_iter, n_iter, early_exaggeration, exaggeration,
+                                   learning_rate, initial_momentum, final_momentum, min_gain, max_step_norm);
+  if (st == 0) st = fastembedr_tsne_batch_layout(b, out);
+  fastembedr_tsne_batch_destroy(b);
+  return st;
+}
 
 }  // extern "C"

@@ -113,13 +113,17 @@ void exact_repulsion(const float* d_y, int n, double* d_rep, double* d_zrow, dou
 
 void exact_kl(const DeviceCsr& P, const float* d_y, const int* d_inv, double* d_zrow, double* d_work,
               double* d_scalars, cudaStream_t s) {
-  const int n = P.n;
+  exact_kl_range(P.row_ptr, P.col, P.val, P.n, d_y, d_inv, 0, d_zrow, d_work, d_scalars, s);
+}
+
+void exact_kl_range(const int* row_ptr, const int* col, const float* val, int n, const float* d_y, const int* d_inv,
+                    int y_begin, double* d_zrow, double* d_work, double* d_scalars, cudaStream_t s) {
   const float2* y = reinterpret_cast<const float2*>(d_y);
-  sum_q_rows_kernel<<<ceil_div(n, 256), 256, 0, s>>>(y, n, d_zrow);
+  sum_q_rows_kernel<<<ceil_div(n, 256), 256, 0, s>>>(y + y_begin, n, d_zrow);
   FE_LAUNCH("sum_q_rows_kernel");
   reduce_double_kernel<<<1, 1024, 0, s>>>(d_zrow, n, d_scalars);
   FE_LAUNCH("reduce_double_kernel");
-  kl_rows_kernel<<<ceil_div(n, 256), 256, 0, s>>>(P.row_ptr, P.col, P.val, y, d_inv, n, d_scalars, d_work);
+  kl_rows_kernel<<<ceil_div(n, 256), 256, 0, s>>>(row_ptr, col, val, y, d_inv, n, d_scalars, d_work);
   FE_LAUNCH("kl_rows_kernel");
   reduce_double_kernel<<<1, 1024, 0, s>>>(d_work, n, d_scalars + 1);
   FE_LAUNCH("reduce_double_kernel");

@@ -22,6 +22,7 @@
 #include <cfloat>
 #include <climits>
 #include <cmath>
+#include <algorithm>
 #include <vector>
 
 #include "tsne_grid.cuh"
@@ -157,14 +158,15 @@ __device__ __forceinline__ void block_partial(float mnx, float mxx, float mny, f
   }
 }
 
-// Returns true in exactly one block: the last one to finish (counter reset for reuse).
-__device__ __forceinline__ bool last_block_done(unsigned* counter) {
+// Returns true in exactly one of the `blocks` blocks sharing `counter`: the last one to finish
+// (counter reset for reuse).
+__device__ __forceinline__ bool last_block_done(unsigned* counter, int blocks) {
   __shared__ bool s_last;
   __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) {
     const unsigned prev = atomicAdd(counter, 1u);
-    s_last = prev == gridDim.x - 1;
+    s_last = prev == (unsigned)blocks - 1u;
     if (s_last) *counter = 0u;
   }
   __syncthreads();
@@ -172,30 +174,36 @@ __device__ __forceinline__ bool last_block_done(unsigned* counter) {
   return s_last;
 }
 
-// Initial statistics of ynew (setup, and after an external layout write).
+// Initial statistics of ynew (setup, and after an external layout write). One point per thread;
+// each instance's last block finishes that instance's grid.
 __global__ void __launch_bounds__(kStepThreads)
-layout_stats_kernel(const float2* __restrict__ ynew, int n, int grid, int mode, StepPartial* __restrict__ part,
+layout_stats_kernel(const float2* __restrict__ ynew, const TsneInstance* __restrict__ inst,
+                    const int2* __restrict__ blocks, int mode, StepPartial* __restrict__ part,
                     unsigned* __restrict__ counter, GridState* __restrict__ next) {
+  const int2 bl = blocks[blockIdx.x];
+  const TsneInstance I = inst[bl.x];
+  const int i = bl.y + threadIdx.x;
   float mnx = FLT_MAX, mxx = -FLT_MAX, mny = FLT_MAX, mxy = -FLT_MAX;
   double sx = 0.0, sy = 0.0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  if (i < I.pt_begin + I.n) {
     const float2 p = ynew[i];
-    mnx = fminf(mnx, p.x);
-    mxx = fmaxf(mxx, p.x);
-    mny = fminf(mny, p.y);
-    mxy = fmaxf(mxy, p.y);
-    sx += p.x;
-    sy += p.y;
+    mnx = mxx = p.x;
+    mny = mxy = p.y;
+    sx = p.x;
+    sy = p.y;
   }
   block_partial(mnx, mxx, mny, mxy, sx, sy, part + blockIdx.x);
-  if (last_block_done(counter)) finish_layout_stats(part, gridDim.x, n, grid, mode, next);
+  if (last_block_done(counter + bl.x, I.blocks))
+    finish_layout_stats(part + I.block_begin, I.blocks, I.n, I.grid, mode, next + bl.x);
 }
 
 // ---------------------------------------------------------------- scatter
-// Each point adds (w, w*(x - cx), w*(y - cy)) to its TAPS x TAPS stencil nodes; block 0 also
-// promotes the grid computed by the previous update (`next`) to `cur`.
-// Points are stored in spatial (Morton) order and every block takes 256 consecutive points, so
-// a block covers a compact patch of the grid even when clusters collapse onto a few cells:
+// Each point adds (w, w*(x - cx), w*(y - cy)) to its TAPS x TAPS stencil nodes of its instance's
+// grid; the first block of every instance also promotes the grid computed by the previous update
+// (`next`) to `cur`.
+// Points are stored in spatial (Morton) order and every block takes 256 consecutive points of one
+// instance, so a block covers a compact patch of the grid even when clusters collapse onto a few
+// cells:
 //   1. runs of equal stencil anchors inside a warp are summed by a segmented shuffle reduction;
 //   2. run heads accumulate into a kTile x kTile node tile in shared memory anchored at the
 //      block's lowest anchor (heads outside the tile go straight to global memory);
@@ -204,13 +212,17 @@ constexpr int kScatterTile = 32;
 
 template <int TAPS>
 __global__ void __launch_bounds__(256)
-scatter_kernel(const float2* __restrict__ y, int n, int grid, GridState* __restrict__ cur,
-               const GridState* __restrict__ next, float4* __restrict__ charges) {
+scatter_kernel(const float2* __restrict__ y, const TsneInstance* __restrict__ inst, const int2* __restrict__ blocks,
+               GridState* __restrict__ cur, const GridState* __restrict__ next) {
   constexpr int NV = TAPS * TAPS * 3;
   __shared__ float tile[kScatterTile * kScatterTile * 3];
   __shared__ int s_box[4];
-  const GridState g = *next;
-  if (blockIdx.x == 0 && threadIdx.x == 0) *cur = g;
+  const int2 bl = blocks[blockIdx.x];
+  const TsneInstance I = inst[bl.x];
+  const int grid = I.grid;
+  float4* __restrict__ charges = I.charges;
+  const GridState g = next[bl.x];
+  if (bl.y == I.pt_begin && threadIdx.x == 0) cur[bl.x] = g;
   const int lane = threadIdx.x & 31;
   for (int t = threadIdx.x; t < kScatterTile * kScatterTile * 3; t += blockDim.x) tile[t] = 0.0f;
   if (threadIdx.x == 0) {
@@ -219,8 +231,8 @@ scatter_kernel(const float2* __restrict__ y, int n, int grid, GridState* __restr
     s_box[2] = -1;
     s_box[3] = -1;
   }
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool valid = i < n;
+  const int i = bl.y + threadIdx.x;
+  const bool valid = i < I.pt_begin + I.n;
   const float2 p = valid ? y[i] : make_float2(g.cx, g.cy);
   const Stencil<TAPS> sx = make_stencil<TAPS>(p.x, g.x0, g.inv_h, g.inv_box, g.nodes);
   const Stencil<TAPS> sy = make_stencil<TAPS>(p.y, g.y0, g.inv_h, g.inv_box, g.nodes);
@@ -411,12 +423,19 @@ __device__ void fft_dif(float2* buf, int count, int logm, const float2* __restri
 // A = (x-charge) + i (y-charge), B = mass (the charge row is cleared for the next scatter).
 // Blocks [nodes, 2 nodes): kernel row dy = r - nodes -> forward FFT of (q + i q^2); the
 // kernel is even in dx, so the transform is real-even and only M/2 + 1 entries are kept.
+// blockIdx.y selects the instance members[blockIdx.y] of the grid class.
 __global__ void __launch_bounds__(kFftThreads)
-rows_forward_kernel(float4* __restrict__ charges, int grid, int nodes, int logm, const float2* __restrict__ tw,
-                    const GridState* __restrict__ cur, float2* __restrict__ rows, float2* __restrict__ krows) {
+rows_forward_kernel(const TsneInstance* __restrict__ inst, const int* __restrict__ members, int grid, int nodes,
+                    int logm, const float2* __restrict__ tw, const GridState* __restrict__ cur,
+                    float2* __restrict__ rows, float2* __restrict__ krows) {
   extern __shared__ float2 sbuf[];
   const int m = 1 << logm;
   const int r = blockIdx.x;
+  const int b = members[blockIdx.y];
+  float4* __restrict__ charges = inst[b].charges;
+  cur += b;
+  rows += (long long)blockIdx.y * 2 * nodes * m;
+  krows += (long long)blockIdx.y * nodes * ((m >> 1) + 1);
   if (r < nodes) {
     float4* crow = charges + (long long)r * grid;
     for (int c = threadIdx.x; c < m; c += blockDim.x) {
@@ -472,6 +491,9 @@ columns_convolve_kernel(float2* __restrict__ rows, const float2* __restrict__ kr
   __shared__ double s_z[kFftThreads / 32];
   const int m = 1 << logm;
   const int half = m >> 1;
+  rows += (long long)blockIdx.y * 2 * nodes * m;
+  krows += (long long)blockIdx.y * nodes * (half + 1);
+  zpart += (long long)blockIdx.y * gridDim.x;
   const int c0 = blockIdx.x * cc;
   float2* kbuf = sbuf + (2 * cc << logm);
   for (int t = threadIdx.x; t < cc * m; t += blockDim.x) {
@@ -525,12 +547,19 @@ columns_convolve_kernel(float2* __restrict__ rows, const float2* __restrict__ kr
 // Inverse row pass -> potentials (phi_q2, phi_x, phi_y) per node; block 0 also finalises
 // Z = sum_k |F_mass|^2 Kq / M^2 - n (the reference's sum_i q_grid(y_i) - n).
 __global__ void __launch_bounds__(kFftThreads)
-rows_inverse_kernel(const float2* __restrict__ rows, int grid, int nodes, int logm, const float2* __restrict__ tw,
-                    const double* __restrict__ zpart, int zblocks, int n, GridState* __restrict__ cur,
-                    float4* __restrict__ potential) {
+rows_inverse_kernel(const float2* __restrict__ rows, const TsneInstance* __restrict__ inst,
+                    const int* __restrict__ members, int grid, int nodes, int logm, const float2* __restrict__ tw,
+                    const double* __restrict__ zpart, int zblocks, GridState* __restrict__ cur) {
   extern __shared__ float2 sbuf[];
   const int m = 1 << logm;
   const int r = blockIdx.x;
+  const int b = members[blockIdx.y];
+  const TsneInstance& I = inst[b];
+  float4* __restrict__ potential = I.potential;
+  const int n = I.n;
+  cur += b;
+  rows += (long long)blockIdx.y * 2 * nodes * m;
+  zpart += (long long)blockIdx.y * zblocks;
   const float2* ina = rows + (long long)r * m;
   const float2* inb = rows + (long long)(nodes + r) * m;
   for (int c = threadIdx.x; c < m; c += blockDim.x) {
@@ -671,16 +700,22 @@ __device__ __forceinline__ int sign3(float v) { return (v > 0.0f) - (v < 0.0f); 
 template <int TAPS, bool DIAG>
 __global__ void __launch_bounds__(kStepThreads)
 update_kernel(float2* __restrict__ y, const float2* __restrict__ attr, float2* __restrict__ gains,
-              float2* __restrict__ update, const float4* __restrict__ pot, int grid, int n,
+              float2* __restrict__ update, const TsneInstance* __restrict__ inst, const int2* __restrict__ blocks,
               const GridState* __restrict__ cur, GridState* __restrict__ next, StepPartial* __restrict__ part,
               unsigned* __restrict__ counter, int mode, float lr, float mom, float min_gain, float max_step,
               float2* __restrict__ out_rep) {
-  const GridState g = *cur;
+  const int2 bl = blocks[blockIdx.x];
+  const TsneInstance I = inst[bl.x];
+  const GridState g = cur[bl.x];
+  const float4* __restrict__ pot = I.potential;
+  const int grid = I.grid;
+  const float lr_i = lr * I.lr_mult;
   const bool clip = isfinite(max_step) && max_step > 0.0f;
   const float max2 = max_step * max_step;
   float mnx = FLT_MAX, mxx = -FLT_MAX, mny = FLT_MAX, mxy = -FLT_MAX;
   double sx = 0.0, sy = 0.0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  const int i = bl.y + threadIdx.x;
+  if (i < I.pt_begin + I.n) {
     const float2 p = y[i];
     const Stencil<TAPS> stx = make_stencil<TAPS>(p.x, g.x0, g.inv_h, g.inv_box, g.nodes);
     const Stencil<TAPS> sty = make_stencil<TAPS>(p.y, g.y0, g.inv_h, g.inv_box, g.nodes);
@@ -709,8 +744,8 @@ update_kernel(float2* __restrict__ y, const float2* __restrict__ attr, float2* _
       float gny = sign3(up.y) != sign3(gy) ? ga.y + 0.2f : ga.y * 0.8f + min_gain;
       if (gnx < min_gain) gnx = min_gain;
       if (gny < min_gain) gny = min_gain;
-      float ux = mom * up.x - lr * gnx * gx;
-      float uy = mom * up.y - lr * gny * gy;
+      float ux = mom * up.x - lr_i * gnx * gx;
+      float uy = mom * up.y - lr_i * gny * gy;
       const float s2 = ux * ux + uy * uy;
       if (clip && s2 > max2) {
         const float sc = max_step / sqrtf(fmaxf(s2, FLT_MIN));
@@ -722,17 +757,16 @@ update_kernel(float2* __restrict__ y, const float2* __restrict__ attr, float2* _
       gains[i] = make_float2(gnx, gny);
       update[i] = make_float2(ux, uy);
       y[i] = make_float2(nx, ny);
-      mnx = fminf(mnx, nx);
-      mxx = fmaxf(mxx, nx);
-      mny = fminf(mny, ny);
-      mxy = fmaxf(mxy, ny);
-      sx += nx;
-      sy += ny;
+      mnx = mxx = nx;
+      mny = mxy = ny;
+      sx = nx;
+      sy = ny;
     }
   }
   if constexpr (!DIAG) {
     block_partial(mnx, mxx, mny, mxy, sx, sy, part + blockIdx.x);
-    if (last_block_done(counter)) finish_layout_stats(part, gridDim.x, n, grid, mode, next);
+    if (last_block_done(counter + bl.x, I.blocks))
+      finish_layout_stats(part + I.block_begin, I.blocks, I.n, I.grid, mode, next + bl.x);
   }
 }
 
@@ -743,10 +777,14 @@ __global__ void fill_state_kernel(float2* __restrict__ gains, float2* __restrict
   }
 }
 
-__global__ void finalize_kernel(const float2* __restrict__ y, const GridState* __restrict__ next, int n,
+__global__ void finalize_kernel(const float2* __restrict__ y, const TsneInstance* __restrict__ inst,
+                                const int2* __restrict__ blocks, const GridState* __restrict__ next,
                                 const int* __restrict__ perm, float2* __restrict__ out) {
-  const float mx = (float)next->mean_x, my = (float)next->mean_y;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  const int2 bl = blocks[blockIdx.x];
+  const TsneInstance& I = inst[bl.x];
+  const float mx = (float)next[bl.x].mean_x, my = (float)next[bl.x].mean_y;
+  const int i = bl.y + threadIdx.x;
+  if (i < I.pt_begin + I.n) {
     const float2 p = y[i];
     out[perm ? perm[i] : i] = make_float2(p.x - mx, p.y - my);
   }
@@ -762,15 +800,21 @@ __device__ __forceinline__ unsigned spread_bits(unsigned v) {
   return v;
 }
 
+// Sort key: instance index above the Morton code of the stencil anchor, so a stable sort keeps
+// every instance inside its slot range.
 template <int TAPS>
-__global__ void anchor_keys_kernel(const float2* __restrict__ y, int n, const GridState* __restrict__ next,
-                                   unsigned* __restrict__ keys, int* __restrict__ order) {
-  const GridState g = *next;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+__global__ void anchor_keys_kernel(const float2* __restrict__ y, const TsneInstance* __restrict__ inst,
+                                   const int2* __restrict__ blocks, const GridState* __restrict__ next,
+                                   int morton_bits, unsigned* __restrict__ keys, int* __restrict__ order) {
+  const int2 bl = blocks[blockIdx.x];
+  const TsneInstance& I = inst[bl.x];
+  const GridState g = next[bl.x];
+  const int i = bl.y + threadIdx.x;
+  if (i < I.pt_begin + I.n) {
     const float2 p = y[i];
     const int bx = make_stencil<TAPS>(p.x, g.x0, g.inv_h, g.inv_box, g.nodes).base;
     const int by = make_stencil<TAPS>(p.y, g.y0, g.inv_h, g.inv_box, g.nodes).base;
-    keys[i] = spread_bits((unsigned)bx) | (spread_bits((unsigned)by) << 1);
+    keys[i] = ((unsigned)bl.x << morton_bits) | spread_bits((unsigned)bx) | (spread_bits((unsigned)by) << 1);
     order[i] = i;
   }
 }
@@ -826,6 +870,12 @@ int persistent_blocks(K kernel, int threads, long long warps_needed) {
   return std::max(1, (int)std::min<long long>((long long)per_sm * sm_count(), (warps_needed + threads / 32 - 1) /
                                                                                    (threads / 32)));
 }
+
+int log2_ceil(int v) {
+  int b = 0;
+  while ((1 << b) < v) ++b;
+  return b;
+}
 }  // namespace
 
 TsneDevice::~TsneDevice() {
@@ -837,36 +887,122 @@ TsneDevice::~TsneDevice() {
 int default_grid_size(int n, int /*mode*/) { return cuda_fft_grid_size(n); }
 
 void tsne_device_alloc(TsneDevice& d, int n, int grid, int mode) {
-  d.n = n;
-  d.grid = grid;
-  d.fft = 2 * grid;
-  d.log_fft = 0;
-  while ((1 << d.log_fft) < d.fft) ++d.log_fft;
+  tsne_batch_alloc(d, std::vector<int>{n}, std::vector<int>{grid}, std::vector<float>{1.0f}, mode);
+}
+
+namespace {
+// Group instances by grid size, allocate the class workspaces in d.grid_arena and point the
+// instance table at them (host copy; the caller uploads it).
+void build_grid_classes(TsneDevice& d, const std::vector<int>& grids) {
+  const int ninst = (int)d.inst.size();
+  std::vector<int> distinct(grids.begin(), grids.end());
+  std::sort(distinct.begin(), distinct.end());
+  distinct.erase(std::unique(distinct.begin(), distinct.end()), distinct.end());
+  d.classes.assign(distinct.size(), GridClass{});
+  std::vector<std::vector<int>> members(distinct.size());
+  for (int b = 0; b < ninst; ++b) {
+    const int g = grids[b];
+    if (g < 8 || g > 2048 || (g & (g - 1)) != 0) throw Error("`grid_size` must be a power of two between 8 and 2048.");
+    const int c = (int)(std::lower_bound(distinct.begin(), distinct.end(), g) - distinct.begin());
+    members[c].push_back(b);
+  }
+  d.grid_arena.release();
+  int* d_members = nullptr;
+  d.grid_arena.reserve(&d_members, ninst);
+  for (std::size_t c = 0; c < distinct.size(); ++c) {
+    GridClass& k = d.classes[c];
+    k.grid = distinct[c];
+    k.nodes = d.mode == kInterpBilinear ? k.grid : 3 * (k.grid / 3);
+    k.fft = 2 * k.grid;
+    k.log_fft = log2_ceil(k.fft);
+    k.count = (int)members[c].size();
+    k.cols_per_block = k.fft >= 512 ? 2 : 1;
+    k.col_blocks = k.fft / k.cols_per_block;
+    const std::size_t m = k.fft;
+    d.grid_arena.reserve(&k.charges, (std::size_t)k.count * k.grid * k.grid);
+    d.grid_arena.reserve(&k.potential, (std::size_t)k.count * k.grid * k.grid);
+    d.grid_arena.reserve(&k.rows, (std::size_t)k.count * 2 * k.nodes * m);
+    d.grid_arena.reserve(&k.krows, (std::size_t)k.count * k.nodes * (m / 2 + 1));
+    d.grid_arena.reserve(&k.twiddle, m / 2);
+    d.grid_arena.reserve(&k.zpart, (std::size_t)k.count * k.col_blocks);
+  }
+  d.grid_arena.commit("t-SNE grid workspaces");
+  std::vector<int> flat;
+  int max_m = 0, max_grid = 0;
+  for (std::size_t c = 0; c < distinct.size(); ++c) {
+    GridClass& k = d.classes[c];
+    k.members = d_members + flat.size();
+    const int m = k.fft;
+    max_m = std::max(max_m, m);
+    max_grid = std::max(max_grid, k.grid);
+    for (int j = 0; j < k.count; ++j) {
+      const int b = members[c][j];
+      flat.push_back(b);
+      TsneInstance& I = d.inst[b];
+      I.grid = k.grid;
+      I.nodes = k.nodes;
+      I.charges = k.charges + (std::size_t)j * k.grid * k.grid;
+      I.potential = k.potential + (std::size_t)j * k.grid * k.grid;
+    }
+    std::vector<float2> tw(m / 2);
+    for (int t = 0; t < m / 2; ++t) {
+      const double ang = -2.0 * M_PI * (double)t / (double)m;
+      tw[t] = make_float2((float)std::cos(ang), (float)std::sin(ang));
+    }
+    FE_CUDA(cudaMemcpy(k.twiddle, tw.data(), sizeof(float2) * tw.size(), cudaMemcpyHostToDevice));
+    FE_CUDA(cudaMemset(k.charges, 0, sizeof(float4) * (std::size_t)k.count * k.grid * k.grid));
+    FE_CUDA(cudaMemset(k.potential, 0, sizeof(float4) * (std::size_t)k.count * k.grid * k.grid));
+  }
+  FE_CUDA(cudaMemcpy(d_members, flat.data(), sizeof(int) * ninst, cudaMemcpyHostToDevice));
+  d.grid = d.inst[0].grid;
+  d.nodes = d.inst[0].nodes;
+  d.key_bits = 2 * log2_ceil(max_grid);
+  d.sort_bits = d.key_bits + log2_ceil(ninst);
+  if (d.sort_bits > 32) throw Error("t-SNE batch: too many instances for the spatial sort key");
+  const int big = 3 * (max_m >= 512 ? 2 : 1) * max_m * (int)sizeof(float2);
+  FE_CUDA(cudaFuncSetAttribute(columns_convolve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  const int rowb = 2 * max_m * (int)sizeof(float2);
+  FE_CUDA(cudaFuncSetAttribute(rows_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, rowb));
+  FE_CUDA(cudaFuncSetAttribute(rows_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, rowb));
+}
+}  // namespace
+
+void tsne_batch_alloc(TsneDevice& d, const std::vector<int>& sizes, const std::vector<int>& grids,
+                      const std::vector<float>& lr_mult, int mode) {
+  const int ninst = (int)sizes.size();
+  if (ninst < 1 || grids.size() != sizes.size() || lr_mult.size() != sizes.size())
+    throw Error("t-SNE batch: one size, grid and learning-rate multiplier per instance");
   d.mode = mode;
-  d.nodes = mode == kInterpBilinear ? grid : 3 * (grid / 3);
-  const int m = d.fft;
-  d.cols_per_block = m >= 512 ? 2 : 1;
-  d.col_blocks = m / d.cols_per_block;
+  d.inst.assign(ninst, TsneInstance{});
+  long long total = 0;
+  int nblocks = 0;
+  for (int b = 0; b < ninst; ++b) {
+    if (sizes[b] < 2) throw Error("t-SNE batch: every instance needs at least two points");
+    TsneInstance& I = d.inst[b];
+    I.pt_begin = (int)total;
+    I.n = sizes[b];
+    I.block_begin = nblocks;
+    I.blocks = ceil_div(sizes[b], kPointBlock);
+    I.lr_mult = lr_mult[b];
+    total += sizes[b];
+    nblocks += I.blocks;
+  }
+  if (total > INT_MAX / 2) throw Error("t-SNE batch: too many points");
+  const int n = (int)total;
+  d.n = n;
+  d.nblocks = nblocks;
   d.attr_blocks = persistent_blocks(attractive_kernel, kAttrThreads, n);
-  d.update_blocks = mode == kInterpBilinear
-                        ? persistent_blocks(update_kernel<2, false>, kStepThreads, ceil_div(n, 32))
-                        : persistent_blocks(update_kernel<3, false>, kStepThreads, ceil_div(n, 32));
-  const int nparts = std::max(d.update_blocks, point_blocks(n));
   d.arena.release();
+  d.arena.reserve(&d.d_inst, ninst);
+  d.arena.reserve(&d.blocks, nblocks);
   d.arena.reserve(&d.y, n);
   d.arena.reserve(&d.attr, n);
   d.arena.reserve(&d.gains, n);
   d.arena.reserve(&d.update, n);
-  d.arena.reserve(&d.charges, (std::size_t)grid * grid);
-  d.arena.reserve(&d.rows, (std::size_t)2 * d.nodes * m);
-  d.arena.reserve(&d.krows, (std::size_t)d.nodes * (m / 2 + 1));
-  d.arena.reserve(&d.potential, (std::size_t)grid * grid);
-  d.arena.reserve(&d.twiddle, m / 2);
-  d.arena.reserve(&d.zpart, d.col_blocks);
-  d.arena.reserve(&d.cur, 1);
-  d.arena.reserve(&d.next, 1);
-  d.arena.reserve(&d.partial, nparts);
-  d.arena.reserve(&d.counter, 1);
+  d.arena.reserve(&d.cur, ninst);
+  d.arena.reserve(&d.next, ninst);
+  d.arena.reserve(&d.partial, nblocks);
+  d.arena.reserve(&d.counter, ninst);
   const int nb = radix_sort_blocks(n);
   d.arena.reserve(&d.perm, n);
   d.arena.reserve(&d.inv, n);
@@ -882,27 +1018,42 @@ void tsne_device_alloc(TsneDevice& d, int n, int grid, int mode) {
   d.arena.reserve(&d.radix.scan_tmp, ceil_div(256LL * nb, 1024));
   d.arena.commit("t-SNE optimizer state");
   d.reordered = false;
-  std::vector<float2> tw(m / 2);
-  for (int t = 0; t < m / 2; ++t) {
-    const double a = -2.0 * M_PI * (double)t / (double)m;
-    tw[t] = make_float2((float)std::cos(a), (float)std::sin(a));
-  }
-  FE_CUDA(cudaMemcpy(d.twiddle, tw.data(), sizeof(float2) * tw.size(), cudaMemcpyHostToDevice));
-  FE_CUDA(cudaMemset(d.charges, 0, sizeof(float4) * (std::size_t)grid * grid));
-  FE_CUDA(cudaMemset(d.potential, 0, sizeof(float4) * (std::size_t)grid * grid));
-  FE_CUDA(cudaMemset(d.counter, 0, sizeof(unsigned)));
-  FE_CUDA(cudaMemset(d.cur, 0, sizeof(GridState)));
+  build_grid_classes(d, grids);
+  std::vector<int2> blk(nblocks);
+  for (int b = 0; b < ninst; ++b)
+    for (int t = 0; t < d.inst[b].blocks; ++t)
+      blk[d.inst[b].block_begin + t] = make_int2(b, d.inst[b].pt_begin + t * kPointBlock);
+  FE_CUDA(cudaMemcpy(d.d_inst, d.inst.data(), sizeof(TsneInstance) * ninst, cudaMemcpyHostToDevice));
+  FE_CUDA(cudaMemcpy(d.blocks, blk.data(), sizeof(int2) * nblocks, cudaMemcpyHostToDevice));
+  FE_CUDA(cudaMemset(d.counter, 0, sizeof(unsigned) * ninst));
+  FE_CUDA(cudaMemset(d.cur, 0, sizeof(GridState) * ninst));
   if (!d.side) FE_CUDA(cudaStreamCreateWithFlags(&d.side, cudaStreamNonBlocking));
   if (!d.fork) FE_CUDA(cudaEventCreateWithFlags(&d.fork, cudaEventDisableTiming));
   if (!d.join) FE_CUDA(cudaEventCreateWithFlags(&d.join, cudaEventDisableTiming));
-  const int big = 3 * d.cols_per_block * m * (int)sizeof(float2);
-  FE_CUDA(cudaFuncSetAttribute(columns_convolve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  const int rowb = 2 * m * (int)sizeof(float2);
-  FE_CUDA(cudaFuncSetAttribute(rows_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, rowb));
-  FE_CUDA(cudaFuncSetAttribute(rows_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, rowb));
   // the synchronous setup above ran on the legacy stream, which the job's non-blocking streams
   // do not wait for
   FE_CUDA(cudaDeviceSynchronize());
+}
+
+void tsne_regrid(TsneDevice& d, const std::vector<int>& grids, cudaStream_t s) {
+  if (grids.size() != d.inst.size()) throw Error("t-SNE regrid: one grid size per instance");
+  FE_CUDA(cudaStreamSynchronize(s));
+  build_grid_classes(d, grids);
+  FE_CUDA(cudaMemcpy(d.d_inst, d.inst.data(), sizeof(TsneInstance) * d.inst.size(), cudaMemcpyHostToDevice));
+  FE_CUDA(cudaDeviceSynchronize());
+  // `next` of every instance was laid out for its old grid: recompute it from the layout
+  layout_stats_kernel<<<d.nblocks, kStepThreads, 0, s>>>(d.y, d.d_inst, d.blocks, d.mode, d.partial, d.counter,
+                                                          d.next);
+  FE_LAUNCH("layout_stats_kernel");
+}
+
+std::vector<float> tsne_grid_extents(TsneDevice& d, cudaStream_t s) {
+  std::vector<GridState> g(d.inst.size());
+  FE_CUDA(cudaMemcpyAsync(g.data(), d.next, sizeof(GridState) * g.size(), cudaMemcpyDeviceToHost, s));
+  FE_CUDA(cudaStreamSynchronize(s));
+  std::vector<float> ext(g.size());
+  for (std::size_t b = 0; b < g.size(); ++b) ext[b] = g[b].h * (float)(g[b].nodes - 1);
+  return ext;
 }
 
 void tsne_device_init(TsneDevice& d, const float* d_init, cudaStream_t s) {
@@ -911,29 +1062,29 @@ void tsne_device_init(TsneDevice& d, const float* d_init, cudaStream_t s) {
   FE_LAUNCH("identity_kernel");
   fill_state_kernel<<<point_blocks(d.n), 256, 0, s>>>(d.gains, d.update, d.n);
   FE_LAUNCH("fill_state_kernel");
-  layout_stats_kernel<<<point_blocks(d.n), kStepThreads, 0, s>>>(d.y, d.n, d.grid, d.mode, d.partial, d.counter,
-                                                                  d.next);
+  layout_stats_kernel<<<d.nblocks, kStepThreads, 0, s>>>(d.y, d.d_inst, d.blocks, d.mode, d.partial, d.counter,
+                                                          d.next);
   FE_LAUNCH("layout_stats_kernel");
 }
 
 void tsne_grid_stage(TsneDevice& d, cudaStream_t s) {
-  const int m = d.fft;
   if (d.mode == kInterpBilinear)
-    scatter_kernel<2><<<ceil_div(d.n, 256), 256, 0, s>>>(d.y, d.n, d.grid, d.cur, d.next, d.charges);
+    scatter_kernel<2><<<d.nblocks, kPointBlock, 0, s>>>(d.y, d.d_inst, d.blocks, d.cur, d.next);
   else
-    scatter_kernel<3><<<ceil_div(d.n, 256), 256, 0, s>>>(d.y, d.n, d.grid, d.cur, d.next, d.charges);
+    scatter_kernel<3><<<d.nblocks, kPointBlock, 0, s>>>(d.y, d.d_inst, d.blocks, d.cur, d.next);
   FE_LAUNCH("scatter_kernel");
-  rows_forward_kernel<<<2 * d.nodes, kFftThreads, 2 * m * sizeof(float2), s>>>(d.charges, d.grid, d.nodes,
-                                                                                d.log_fft, d.twiddle, d.cur,
-                                                                                d.rows, d.krows);
-  FE_LAUNCH("rows_forward_kernel");
-  columns_convolve_kernel<<<d.col_blocks, kFftThreads, 3 * d.cols_per_block * m * sizeof(float2), s>>>(
-      d.rows, d.krows, d.nodes, d.log_fft, d.cols_per_block, d.twiddle, d.zpart);
-  FE_LAUNCH("columns_convolve_kernel");
-  rows_inverse_kernel<<<d.nodes, kFftThreads, 2 * m * sizeof(float2), s>>>(d.rows, d.grid, d.nodes, d.log_fft,
-                                                                            d.twiddle, d.zpart, d.col_blocks, d.n,
-                                                                            d.cur, d.potential);
-  FE_LAUNCH("rows_inverse_kernel");
+  for (const GridClass& c : d.classes) {
+    const int m = c.fft;
+    rows_forward_kernel<<<dim3(2 * c.nodes, c.count), kFftThreads, 2 * m * sizeof(float2), s>>>(
+        d.d_inst, c.members, c.grid, c.nodes, c.log_fft, c.twiddle, d.cur, c.rows, c.krows);
+    FE_LAUNCH("rows_forward_kernel");
+    columns_convolve_kernel<<<dim3(c.col_blocks, c.count), kFftThreads, 3 * c.cols_per_block * m * sizeof(float2),
+                              s>>>(c.rows, c.krows, c.nodes, c.log_fft, c.cols_per_block, c.twiddle, c.zpart);
+    FE_LAUNCH("columns_convolve_kernel");
+    rows_inverse_kernel<<<dim3(c.nodes, c.count), kFftThreads, 2 * m * sizeof(float2), s>>>(
+        c.rows, d.d_inst, c.members, c.grid, c.nodes, c.log_fft, c.twiddle, c.zpart, c.col_blocks, d.cur);
+    FE_LAUNCH("rows_inverse_kernel");
+  }
 }
 
 void tsne_attractive_stage(TsneDevice& d, const DeviceCsr& P, float exag, cudaStream_t s) {
@@ -944,13 +1095,13 @@ void tsne_attractive_stage(TsneDevice& d, const DeviceCsr& P, float exag, cudaSt
 
 void tsne_update_stage(TsneDevice& d, float lr, float mom, float min_gain, float max_step, cudaStream_t s) {
   if (d.mode == kInterpBilinear)
-    update_kernel<2, false><<<d.update_blocks, kStepThreads, 0, s>>>(
-        d.y, d.attr, d.gains, d.update, d.potential, d.grid, d.n, d.cur, d.next, d.partial, d.counter, d.mode, lr,
-        mom, min_gain, max_step, nullptr);
+    update_kernel<2, false><<<d.nblocks, kStepThreads, 0, s>>>(d.y, d.attr, d.gains, d.update, d.d_inst, d.blocks,
+                                                                d.cur, d.next, d.partial, d.counter, d.mode, lr, mom,
+                                                                min_gain, max_step, nullptr);
   else
-    update_kernel<3, false><<<d.update_blocks, kStepThreads, 0, s>>>(
-        d.y, d.attr, d.gains, d.update, d.potential, d.grid, d.n, d.cur, d.next, d.partial, d.counter, d.mode, lr,
-        mom, min_gain, max_step, nullptr);
+    update_kernel<3, false><<<d.nblocks, kStepThreads, 0, s>>>(d.y, d.attr, d.gains, d.update, d.d_inst, d.blocks,
+                                                                d.cur, d.next, d.partial, d.counter, d.mode, lr, mom,
+                                                                min_gain, max_step, nullptr);
   FE_LAUNCH("update_kernel");
 }
 
@@ -971,31 +1122,32 @@ void tsne_forces(TsneDevice& d, const DeviceCsr& P, float exag, float* d_attr, f
   FE_CUDA(cudaMemcpyAsync(d_attr, d.attr, sizeof(float2) * d.n, cudaMemcpyDeviceToDevice, s));
   float2* r = reinterpret_cast<float2*>(d_rep);
   if (d.mode == kInterpBilinear)
-    update_kernel<2, true><<<d.update_blocks, kStepThreads, 0, s>>>(
-        d.y, d.attr, d.gains, d.update, d.potential, d.grid, d.n, d.cur, d.next, d.partial, d.counter, d.mode, 0.0f,
-        0.0f, 0.0f, 0.0f, r);
+    update_kernel<2, true><<<d.nblocks, kStepThreads, 0, s>>>(d.y, d.attr, d.gains, d.update, d.d_inst, d.blocks,
+                                                               d.cur, d.next, d.partial, d.counter, d.mode, 0.0f,
+                                                               0.0f, 0.0f, 0.0f, r);
   else
-    update_kernel<3, true><<<d.update_blocks, kStepThreads, 0, s>>>(
-        d.y, d.attr, d.gains, d.update, d.potential, d.grid, d.n, d.cur, d.next, d.partial, d.counter, d.mode, 0.0f,
-        0.0f, 0.0f, 0.0f, r);
+    update_kernel<3, true><<<d.nblocks, kStepThreads, 0, s>>>(d.y, d.attr, d.gains, d.update, d.d_inst, d.blocks,
+                                                               d.cur, d.next, d.partial, d.counter, d.mode, 0.0f,
+                                                               0.0f, 0.0f, 0.0f, r);
   FE_LAUNCH("update_kernel(diagnostic)");
 }
 
 void tsne_finalize(TsneDevice& d, float* d_out, cudaStream_t s) {
-  finalize_kernel<<<point_blocks(d.n), 256, 0, s>>>(d.y, d.next, d.n, d.perm, reinterpret_cast<float2*>(d_out));
+  finalize_kernel<<<d.nblocks, kPointBlock, 0, s>>>(d.y, d.d_inst, d.blocks, d.next, d.perm,
+                                                     reinterpret_cast<float2*>(d_out));
   FE_LAUNCH("finalize_kernel");
 }
 
 void tsne_reorder(TsneDevice& d, DeviceCsr& P, cudaStream_t s) {
   const int n = d.n;
-  int bits = 0;
-  while ((1 << bits) < d.grid) ++bits;
   if (d.mode == kInterpBilinear)
-    anchor_keys_kernel<2><<<point_blocks(n), 256, 0, s>>>(d.y, n, d.next, d.keys, d.order);
+    anchor_keys_kernel<2><<<d.nblocks, kPointBlock, 0, s>>>(d.y, d.d_inst, d.blocks, d.next, d.key_bits, d.keys,
+                                                            d.order);
   else
-    anchor_keys_kernel<3><<<point_blocks(n), 256, 0, s>>>(d.y, n, d.next, d.keys, d.order);
+    anchor_keys_kernel<3><<<d.nblocks, kPointBlock, 0, s>>>(d.y, d.d_inst, d.blocks, d.next, d.key_bits, d.keys,
+                                                            d.order);
   FE_LAUNCH("anchor_keys_kernel");
-  radix_sort_pairs(d.keys, d.order, d.keys_tmp, d.order_tmp, n, 2 * bits, d.radix, s);
+  radix_sort_pairs(d.keys, d.order, d.keys_tmp, d.order_tmp, n, d.sort_bits, d.radix, s);
   gather_points_kernel<<<point_blocks(n), 256, 0, s>>>(d.order, n, d.y, d.gains, d.update, d.perm, d.scratch,
                                                        d.perm_tmp, d.delta);
   FE_LAUNCH("gather_points_kernel");
@@ -1008,11 +1160,11 @@ void tsne_reorder(TsneDevice& d, DeviceCsr& P, cudaStream_t s) {
   d.reordered = true;
 }
 
-int tsne_reorder_launches() {
-  // keys, 3 radix passes x (histogram + 3-kernel scan + scatter), gather, scatter, relabel
-  return 1 + 3 * 5 + 3;
+int tsne_reorder_launches(const TsneDevice& d) {
+  // keys, radix passes x (histogram + 3-kernel scan + scatter), gather, scatter, relabel
+  return 1 + ceil_div(d.sort_bits, 8) * 5 + 3;
 }
 
-int tsne_launches_per_iteration() { return 6; }
+int tsne_launches_per_iteration(const TsneDevice& d) { return 3 + 3 * (int)d.classes.size(); }
 
 }  // namespace fe

@@ -1,5 +1,8 @@
-// Per-iteration state and kernels of the t-SNE gradient loop on the GPU.
+// Per-iteration state and kernels of the t-SNE gradient loop on the GPU, for one instance or a
+// batch of independent instances that share every launch.
 #pragma once
+
+#include <vector>
 
 #include "tsne.cuh"
 
@@ -24,31 +27,57 @@ struct StepPartial {
   double sum_x, sum_y;
 };
 
-// Device buffers of one t-SNE instance (all inside one arena) and the side stream that runs
-// the attractive pass concurrently with the grid stage.
+// One instance of a batch (device table entry). Instances are stored in table order: their
+// points occupy consecutive storage slots and their CSR rows consecutive rows.
+struct TsneInstance {
+  int pt_begin, n;          // storage slots [pt_begin, pt_begin + n)
+  int grid, nodes;          // G and the nodes used per side
+  int block_begin, blocks;  // point blocks of this instance (and its StepPartial slice)
+  float lr_mult;            // learning rate of this instance = run learning rate x lr_mult
+  float4* charges;          // G x G (mass, mass*dx, mass*dy, 0)
+  float4* potential;        // G x G (phi_q2, phi_x, phi_y, 0)
+};
+
+// Instances with the same G, transformed by the same FFT launches (instance members[blockIdx.y]).
+struct GridClass {
+  int grid = 0, nodes = 0, fft = 0, log_fft = 0;
+  int count = 0;
+  int* members = nullptr;     // device: the class's instance indices
+  int cols_per_block = 1, col_blocks = 0;
+  float2* rows = nullptr;     // count x (2 planes x nodes x M): row-transformed charges
+  float2* krows = nullptr;    // count x (nodes x (M/2 + 1)): row-transformed kernel (q, q^2)
+  double* zpart = nullptr;    // count x col_blocks
+  float2* twiddle = nullptr;  // M / 2 forward twiddles
+  float4* charges = nullptr;  // count x G x G
+  float4* potential = nullptr;
+};
+
+constexpr int kPointBlock = 256;  // points per block of the point kernels
+
+// Device buffers of a batch of t-SNE instances (one arena) and the side stream that runs the
+// attractive pass concurrently with the grid stage. A single instance is a batch of one.
 struct TsneDevice {
-  int n = 0;
-  int grid = 0;     // G: nodes per side of the charge grid
-  int fft = 0;      // M = 2G
-  int log_fft = 0;
-  int mode = kInterpLagrange3;
+  int n = 0;        // points over all instances
+  int mode = kInterpBilinear;
+  int grid = 0;     // G of instance 0 (single-instance callers)
   int nodes = 0;
+  std::vector<TsneInstance> inst;  // host copy of the table
+  std::vector<GridClass> classes;
+  Arena grid_arena;           // class workspaces; rebuilt when grid sizes change
+  TsneInstance* d_inst = nullptr;
+  int2* blocks = nullptr;     // point block -> (instance, first storage slot)
+  int nblocks = 0;
   float2* y = nullptr;        // layout in storage order (recentred lazily by the update)
   float2* attr = nullptr;     // attractive force of the current iteration
   float2* gains = nullptr;
   float2* update = nullptr;
-  float4* charges = nullptr;  // G x G (mass, mass*dx, mass*dy, 0)
-  float2* rows = nullptr;     // 2 planes x nodes x M: row-transformed charges
-  float2* krows = nullptr;    // nodes x (G + 1): row-transformed kernel (q, q^2)
-  float4* potential = nullptr;  // G x G (phi_q2, phi_x, phi_y, 0)
-  float2* twiddle = nullptr;  // M / 2 forward twiddles
-  double* zpart = nullptr;    // one per column block
-  GridState* cur = nullptr;
-  GridState* next = nullptr;
-  StepPartial* partial = nullptr;
-  unsigned* counter = nullptr;
+  GridState* cur = nullptr;   // per instance
+  GridState* next = nullptr;  // per instance
+  StepPartial* partial = nullptr;  // per point block
+  unsigned* counter = nullptr;     // per instance
   // spatial order: storage slot t holds original point perm[t]; inv is the inverse. CSR rows stay
-  // in original order; CSR columns hold storage slots (relabelled at every reorder).
+  // in original order; CSR columns hold storage slots (relabelled at every reorder). Points never
+  // leave their instance's slot range.
   int* perm = nullptr;
   int* inv = nullptr;
   unsigned* keys = nullptr;
@@ -59,11 +88,10 @@ struct TsneDevice {
   float2* scratch = nullptr;  // 3 x n: y, gains, update while permuting
   int* perm_tmp = nullptr;
   RadixWorkspace radix;
+  int key_bits = 0;           // Morton bits of the largest grid; instance bits sit above them
+  int sort_bits = 0;
   bool reordered = false;
   int attr_blocks = 0;
-  int update_blocks = 0;
-  int col_blocks = 0;
-  int cols_per_block = 0;
   cudaStream_t side = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
   Arena arena;
@@ -77,26 +105,36 @@ struct TsneDevice {
 int default_grid_size(int n, int mode);
 
 void tsne_device_alloc(TsneDevice& d, int n, int grid, int mode);
+// Batch of instances: sizes[b] points on a grids[b] x grids[b] grid, learning rate multipliers
+// lr_mult[b].
+void tsne_batch_alloc(TsneDevice& d, const std::vector<int>& sizes, const std::vector<int>& grids,
+                      const std::vector<float>& lr_mult, int mode);
+// Change the instances' grid sizes: rebuild the grid classes and their workspaces, then
+// recompute every instance's next grid from the current layout (stream-ordered on s).
+void tsne_regrid(TsneDevice& d, const std::vector<int>& grids, cudaStream_t s);
+// Current grid extent (2 x half-width of the bounding square) of every instance, from `next`
+// (synchronises s).
+std::vector<float> tsne_grid_extents(TsneDevice& d, cudaStream_t s);
 // Copy a row-major float2 init into the layout, reset gains/update and compute `next`.
 void tsne_device_init(TsneDevice& d, const float* d_init, cudaStream_t s);
 // One optimizer iteration: grid stage on `s` concurrently with the attractive pass on the side
-// stream, then the update (6 launches).
+// stream, then the update (3 + 3 x grid classes launches).
 void tsne_iteration(TsneDevice& d, const DeviceCsr& P, float exaggeration, float learning_rate, float momentum,
                     float min_gain, float max_step_norm, cudaStream_t s);
-// Stages, for profiling: scatter + FFT convolution (4 launches), attractive (1), update (1).
+// Stages, for profiling: scatter + FFT convolution, attractive (1), update (1).
 void tsne_grid_stage(TsneDevice& d, cudaStream_t s);
 void tsne_attractive_stage(TsneDevice& d, const DeviceCsr& P, float exaggeration, cudaStream_t s);
 void tsne_update_stage(TsneDevice& d, float learning_rate, float momentum, float min_gain, float max_step_norm,
                        cudaStream_t s);
-// Sort points by the Morton code of their stencil anchor on the current grid and permute the
-// point state (storage order) and the CSR column labels accordingly.
+// Sort each instance's points by the Morton code of their stencil anchor on the current grid and
+// permute the point state (storage order) and the CSR column labels accordingly.
 void tsne_reorder(TsneDevice& d, DeviceCsr& P, cudaStream_t s);
-int tsne_reorder_launches();
-// out[original id] = y - mean(y), row-major float2.
+int tsne_reorder_launches(const TsneDevice& d);
+// out[original id] = y - mean(y of its instance), row-major float2.
 void tsne_finalize(TsneDevice& d, float* d_out, cudaStream_t s);
 // Forces on the current layout without updating it (diagnostics).
 void tsne_forces(TsneDevice& d, const DeviceCsr& P, float exaggeration, float* d_attr, float* d_rep,
                  cudaStream_t s);
-int tsne_launches_per_iteration();
+int tsne_launches_per_iteration(const TsneDevice& d);
 
 }  // namespace fe

@@ -218,11 +218,62 @@ int fastembedr_tsne_plan_synchronize(fastembedr_tsne_plan* plan);
 /* the plan's cudaStream_t, for callers that time with their own events */
 void* fastembedr_tsne_plan_stream(fastembedr_tsne_plan* plan);
 int fastembedr_tsne_plan_layout(fastembedr_tsne_plan* plan, float* out);
+/* launches_per_iteration: kernel launches of one iteration; launches_per_reorder: of the spatial
+ * reorder that starts every chunk of 25 iterations */
 int fastembedr_tsne_plan_info(fastembedr_tsne_plan* plan, long long* nnz, int* grid_size, int* interpolation,
-                              int* launches_per_iteration);
+                              int* launches_per_iteration, int* launches_per_reorder);
 /* exact KL of the current layout (all-pairs Z on the GPU) */
 int fastembedr_tsne_plan_kl(fastembedr_tsne_plan* plan, double* kl);
 void fastembedr_tsne_plan_destroy(fastembedr_tsne_plan* plan);
+
+/* ---------------------------------------------------------------- batched t-SNE
+ * No reference counterpart (the reference runs one instance per call). Many independent
+ * instances share every launch: their P matrices are appended into one CSR (rows and columns
+ * offset by each instance's first point), instances with the same grid size share the FFT
+ * launches, and every iteration of the whole batch is one CUDA graph node sequence
+ * (3 + 3 x grid sizes launches). Each instance follows exactly the single-instance algorithm with
+ * its own grid (the size policy of fastembedr_cuda_opentsne_fft_grid_size, or grid_size), its
+ * own bounding box, Z and recentring, and the opt-SNE learning rate n_b / exaggeration. */
+typedef struct fastembedr_tsne_batch fastembedr_tsne_batch;
+
+/* sizes[b] points per instance. indices / distances: host, each instance's column-major
+ * n_b x k KNN (its own rows 0..n_b-1, index_offset 0 or 1), instance after instance; init: host,
+ * row-major n_b x 2 per instance, instance after instance, or NULL (seeded N(0, 1e-4^2)).
+ * grid_size: 0 = the CUDA size policy per instance (256 / 512 / 1024 by n), -1 = the reference
+ * CPU policy (tsne_fft_grid_size, src/tsne_neighbors.cpp:403-413: 128 below 50,000 points, else
+ * 256), -2 = adaptive (at the start of every 25-iteration chunk each instance gets the smallest
+ * power of two in [128, 1024] whose node spacing over its current bounding square is at most 0.7,
+ * or FASTEMBEDR_TSNE_GRID_SPACING), > 0 = that many nodes per side for every instance. */
+int fastembedr_tsne_batch_create(int n_instances, const int* sizes, const int* indices, const float* distances,
+                                 const float* init, int k, float perplexity, int index_offset, int grid_size,
+                                 int interpolation, unsigned int seed, fastembedr_tsne_batch** batch);
+/* The two-phase schedule on every instance, returning when done. Instance b uses the learning
+ * rate learning_rate x n_b in both phases; learning_rate <= 0 selects the package's opt-SNE
+ * rate n_b / early_exaggeration (R/tsne_control.R:191-231). */
+int fastembedr_tsne_batch_run(fastembedr_tsne_batch* batch, int early_exaggeration_iter, int n_iter,
+                              float early_exaggeration, float exaggeration, float learning_rate,
+                              float initial_momentum, float final_momentum, float min_gain, float max_step_norm);
+/* Enqueue `iters` iterations on the batch's stream; instance b uses learning_rate x n_b. */
+int fastembedr_tsne_batch_iterate(fastembedr_tsne_batch* batch, int iters, float exaggeration, float learning_rate,
+                                  float momentum, float min_gain, float max_step_norm);
+int fastembedr_tsne_batch_synchronize(fastembedr_tsne_batch* batch);
+void* fastembedr_tsne_batch_stream(fastembedr_tsne_batch* batch);
+/* Recentred layouts, row-major n_b x 2 per instance, instance after instance. */
+int fastembedr_tsne_batch_layout(fastembedr_tsne_batch* batch, float* out);
+/* Exact KL of one instance (all-pairs Z of that instance). */
+int fastembedr_tsne_batch_kl(fastembedr_tsne_batch* batch, int instance, double* kl);
+int fastembedr_tsne_batch_info(fastembedr_tsne_batch* batch, long long* nnz, long long* points, int* grid_classes,
+                               int* launches_per_iteration, int* launches_per_reorder);
+/* Current grid size of every instance (caller order) and how many times the adaptive policy
+ * changed them; either output may be NULL. */
+int fastembedr_tsne_batch_grids(fastembedr_tsne_batch* batch, int* grids, int* regrids);
+void fastembedr_tsne_batch_destroy(fastembedr_tsne_batch* batch);
+/* create + run + layout + destroy with the size-policy grids. */
+int fastembedr_cuda_tsne_batch_from_knn(int n_instances, const int* sizes, const int* indices, const float* distances,
+                                        const float* init, int k, float perplexity, int early_exaggeration_iter,
+                                        int n_iter, float early_exaggeration, float exaggeration, float learning_rate,
+                                        float initial_momentum, float final_momentum, float min_gain,
+                                        float max_step_norm, unsigned int seed, int index_offset, float* out);
 
 #ifdef __cplusplus
 }

@@ -221,15 +221,20 @@ def test_spatial_reorder_preserves_results(small, monkeypatch):
     d_idx = torch.as_tensor(np.ascontiguousarray(idx.T), device="cuda")
     d_dist = torch.as_tensor(np.ascontiguousarray(dist.T), device="cuda")
     init = (np.random.default_rng(3).standard_normal((n, 2)) * 3).astype(np.float32)
-    outs, kls = [], []
+    outs, kls, firsts = [], [], []
     for flag in ("0", "1"):
         monkeypatch.setenv("FASTEMBEDR_TSNE_REORDER", flag)
         plan = api.TsnePlan(d_idx, d_dist, n, k, 15.0, init=init)
-        plan.run(30, 1.0, n / 12.0)
+        plan.run(1, 1.0, n / 12.0)
+        firsts.append(plan.layout())
+        plan.run(29, 1.0, n / 12.0)
         outs.append(plan.layout())
         kls.append(plan.kl())
         plan.close()
-    assert rel_l2(outs[1], outs[0].astype(np.float64)) < 1e-4
+    # one iteration: rounding only; 30 iterations: the atomic-order rounding grows chaotically but
+    # stays far below what a wrong permutation or relabelling would give (order 1)
+    assert rel_l2(firsts[1], firsts[0].astype(np.float64)) < 1e-6
+    assert rel_l2(outs[1], outs[0].astype(np.float64)) < 1e-3
     rp, col, val, _ = O.tsne_csr(idx, dist, 15.0)
     for y, kv in zip(outs, kls):
         assert kv == pytest.approx(O.kl(rp, col, val, y), rel=1e-5)
