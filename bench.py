@@ -200,9 +200,10 @@ def run_gpu(args):
     plan = api.TsnePlan(d_idx, d_dist, n, K, PERPLEXITY, init=init)
     info = plan.info()
     lr = n / 12.0
-    # untimed early-exaggeration phase, as in a real run, then the warm-up steps
+    # untimed early-exaggeration phase, as in a real run, then the warm-up steps: at least two
+    # 25-iteration chunks, so that the CUDA graphs of both CSR buffers of the reorder exist
     plan.run(250, 12.0, lr)
-    plan.run(args.warmup, 1.0, lr)
+    plan.run(max(args.warmup, 50), 1.0, lr)
     plan.synchronize()
 
     def barrier():

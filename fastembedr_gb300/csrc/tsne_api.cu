@@ -71,6 +71,7 @@ struct TsneJob {
   // Adaptive box count: at the start of every chunk each instance gets the smallest power-of-two
   // grid whose node spacing over its current bounding square is at most `spacing` (clamped to
   // [grid_min, grid_max]); grids grow at once and shrink only when four times too fine.
+  bool reorder = true;  // periodic spatial reorder (FASTEMBEDR_TSNE_REORDER=0 turns it off), fixed at prepare
   bool adaptive = false;
   float spacing = 0.7f;
   int grid_min = 128, grid_max = 1024;
@@ -129,6 +130,7 @@ struct TsneJob {
       symmetrise(d_idx, d_p, n, k, offset, P, s);
     }
     tsne_device_alloc(D, n, grid, mode);
+    reorder = reorder_enabled();
     float2* d_init = nullptr;
     Arena tmp;
     tmp.reserve(&d_init, n);
@@ -221,6 +223,7 @@ struct TsneJob {
     }
     FE_CUDA(cudaStreamSynchronize(s));
     parts.clear();
+    reorder = reorder_enabled();
     float2* d_init = nullptr;
     Arena tmp;
     tmp.reserve(&d_init, n);
@@ -247,7 +250,6 @@ struct TsneJob {
     cudaStream_t s = stream.s;
     if (iters <= 0) return;
     constexpr int kChunk = 25;
-    const bool reorder = reorder_enabled();
     const bool graph = use_graph && graph_capture_enabled();
     int left = iters;
     while (left > 0) {
@@ -556,7 +558,7 @@ int fastembedr_tsne_plan_profile(fastembedr_tsne_plan* plan, int iters, float ex
     if (!plan || iters < 1) throw fe::Error("invalid CUDA t-SNE profile request");
     fe::TsneJob& J = plan->job;
     cudaStream_t s = J.stream.s;
-    if (fe::reorder_enabled()) fe::tsne_reorder(J.D, J.P, s);
+    if (J.reorder) fe::tsne_reorder(J.D, J.P, s);
     std::vector<cudaEvent_t> ev(4 * (std::size_t)iters);
     for (auto& e : ev) FE_CUDA(cudaEventCreate(&e));
     for (int it = 0; it < iters; ++it) {

@@ -84,12 +84,12 @@ __global__ void reduce_double_kernel(const double* __restrict__ v, int n, double
 // Row i of P belongs to the point at y[inv[i]] (inv = nullptr: y is in row order); columns index y.
 __global__ void __launch_bounds__(256)
 kl_rows_kernel(const int* __restrict__ row_ptr, const int* __restrict__ col, const float* __restrict__ val,
-               const float2* __restrict__ y, const int* __restrict__ inv, int n, const double* __restrict__ zsum,
-               double* __restrict__ out) {
+               const float2* __restrict__ y, const float2* __restrict__ y_rows, const int* __restrict__ inv, int n,
+               const double* __restrict__ zsum, double* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double z = (double)(float)fmax(*zsum, (double)FLT_MIN);
-  const float2 yi = y[inv ? inv[i] : i];
+  const float2 yi = inv ? y[inv[i]] : y_rows[i];
   double acc = 0.0;
   for (int p = row_ptr[i]; p < row_ptr[i + 1]; ++p) {
     const float2 yj = y[col[p]];
@@ -123,7 +123,7 @@ void exact_kl_range(const int* row_ptr, const int* col, const float* val, int n,
   FE_LAUNCH("sum_q_rows_kernel");
   reduce_double_kernel<<<1, 1024, 0, s>>>(d_zrow, n, d_scalars);
   FE_LAUNCH("reduce_double_kernel");
-  kl_rows_kernel<<<ceil_div(n, 256), 256, 0, s>>>(row_ptr, col, val, y, d_inv, n, d_scalars, d_work);
+  kl_rows_kernel<<<ceil_div(n, 256), 256, 0, s>>>(row_ptr, col, val, y, y + y_begin, d_inv, n, d_scalars, d_work);
   FE_LAUNCH("kl_rows_kernel");
   reduce_double_kernel<<<1, 1024, 0, s>>>(d_work, n, d_scalars + 1);
   FE_LAUNCH("reduce_double_kernel");
