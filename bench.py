@@ -578,19 +578,58 @@ def run_umap_reference(args):
 BATCH_TSNE_ITERS = (250, 750)
 
 
-def _batched_instances(args, device):
+def _batched_instances(count, k, seed, device, with_x=False):
     """Instances of the batched workload: sizes log-uniform in [2,000, 200,000], each a 50-d
-    mixture of 5-15 clusters with exact KNN (k = 90 for t-SNE)."""
+    mixture of 5-15 clusters with exact KNN (k = 90 for t-SNE, 15 for UMAP)."""
     from fastembedr_gb300 import synthetic as S
 
-    rng = np.random.default_rng(23)
-    sizes = np.exp(rng.uniform(np.log(2_000), np.log(200_000), args.instances)).astype(np.int64)
-    knns = []
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(2_000), np.log(200_000), count)).astype(np.int64)
+    knns, xs = [], []
     for j, n in enumerate(sizes):
-        x, _ = S.mixture(int(n), 50, int(rng.integers(5, 16)), 1000 + j, centre_sd=4.0, lognormal_sizes=True)
-        idx, dist = S.exact_knn_torch(x, K, device=device)
+        x, _ = S.mixture(int(n), 50, int(rng.integers(5, 16)), seed * 1000 + j, centre_sd=4.0, lognormal_sizes=True)
+        idx, dist = S.exact_knn_torch(x, k, device=device)
         knns.append((idx.cpu().numpy(), dist.cpu().numpy()))
-    return knns
+        if with_x:
+            xs.append(x)
+    return (knns, xs) if with_x else knns
+
+
+def _run_batched_umap(args, device):
+    """UMAP half of the batched workload: instances with k = 15, 500 epochs, a data-derived start;
+    one batched job against one umap_knn call per instance (size-stratified subset)."""
+    import oracle as O
+    from fastembedr_gb300 import api
+
+    knns, xs = _batched_instances(args.instances - args.instances // 2, UMAP_K, 29, device, with_x=True)
+    inits = [_pca_init(x) for x in xs]
+    del xs
+    sizes = np.array([i.shape[0] for i, _ in knns])
+    api.umap_knn_batch(knns[:2], inits[:2], n_epochs=5)  # warm-up
+    t0 = time.perf_counter()
+    lays, sgd_ms = api.umap_knn_batch(knns, inits, n_epochs=UMAP_EPOCHS, return_time=True)
+    wall = time.perf_counter() - t0
+    order = np.argsort(sizes)
+    subset = order[:: max(1, args.plain_stride)]
+    plain_t, plain_work, pres = 0.0, 0.0, []
+    for j in subset:
+        idx, dist = knns[j]
+        t = time.perf_counter()
+        fit = api.umap_knn(idx, dist, inits[j], n_epochs=UMAP_EPOCHS)
+        plain_t += time.perf_counter() - t
+        plain_work += float(sizes[j]) * UMAP_EPOCHS
+        if len(pres) < args.kl_instances and sizes[j] <= 60_000:
+            keep = np.arange(0, sizes[j], 4, dtype=np.int32)
+            pres.append({"n": int(sizes[j]),
+                         "preservation_batched": O.knn_preservation(lays[j], idx, keep=keep, preserve_k=15),
+                         "preservation_plain": O.knn_preservation(fit.layout, idx, keep=keep, preserve_k=15)})
+    work = float(sizes.sum()) * UMAP_EPOCHS
+    return {"instances": len(knns), "points": int(sizes.sum()), "epochs": UMAP_EPOCHS, "k": UMAP_K,
+            "epochs_value": work / (sgd_ms * 1e-3), "unit": "points*epochs/s", "ms_per_epoch": sgd_ms / UMAP_EPOCHS,
+            "e2e_value": work / wall, "job_seconds": wall,
+            "plain_gpu": {"value": plain_work / plain_t, "instances": int(len(subset)),
+                          "form": "fastembedr_cuda_umap_from_knn once per instance"},
+            "batched_vs_plain_e2e": (work / wall) / (plain_work / plain_t), "preservation": pres}
 
 
 def _run_batch(knns, inits, grid_policy, work):
@@ -633,7 +672,7 @@ def run_batched(args):
     if rank != 0:
         return 0
     torch.cuda.set_device(local)
-    knns = _batched_instances(args, f"cuda:{local}")
+    knns = _batched_instances(args.instances // 2, K, 23, f"cuda:{local}")
     torch.cuda.empty_cache()
     sizes = np.array([i.shape[0] for i, _ in knns])
     iters = sum(BATCH_TSNE_ITERS)
@@ -669,6 +708,7 @@ def run_batched(args):
         r["vs_plain_e2e"] = r["e2e_value"] / plain_rate
         b.close()
         runs[policy] = r
+    umap = _run_batched_umap(args, f"cuda:{local}")
     clk = clocks.stop()
     head = runs["adaptive"]
     line = {
@@ -688,7 +728,7 @@ def run_batched(args):
         "plain_gpu": {"value": plain_rate, "unit": "points*iterations/s", "instances": int(len(subset)),
                       "form": "fastembedr_cuda_opentsne_fft_from_knn_float once per instance, CUDA size policy "
                               f"(every {max(1, args.plain_stride)}th instance by size)"},
-        "batched": runs, "batched_vs_plain_e2e": head["vs_plain_e2e"],
+        "batched": runs, "batched_vs_plain_e2e": head["vs_plain_e2e"], "umap": umap,
         "clocks": clk, "gpu_launches": iters * head["launches_per_iteration"] + (
             (BATCH_TSNE_ITERS[0] + 24) // 25 + (BATCH_TSNE_ITERS[1] + 24) // 25) * head["launches_per_reorder"],
     }
@@ -710,7 +750,7 @@ def main():
     ap.add_argument("--workload", default="tsne", choices=["tsne", "serving", "umap", "batched"],
                     help="tsne: the headline 1M-point optimizer; serving: transform_tsne served; umap: 100k UMAP; "
                          "batched: many t-SNE instances per launch")
-    ap.add_argument("--instances", type=int, default=256)
+    ap.add_argument("--instances", type=int, default=256, help="batched: half t-SNE (k = 90), half UMAP (k = 15)")
     ap.add_argument("--plain-stride", type=int, default=4)
     ap.add_argument("--kl-instances", type=int, default=6)
     ap.add_argument("--n-ref", type=int, default=SERVE_N_REF)

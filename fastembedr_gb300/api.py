@@ -605,3 +605,33 @@ class TransformServer:
             self.close()
         except Exception:
             pass
+
+
+def umap_knn_batch(knns, inits, seed=42, n_epochs=500, min_dist=0.01, negative_sample_rate=5, learning_rate=1.0,
+                   repulsion_strength=1.0, return_time=False):
+    """umap_knn over many instances at once (C ABI fastembedr_cuda_umap_batch_from_knn): every
+    instance gets its own fuzzy graph and the package's SGD; one epoch is one launch over all
+    instances' edges. Returns one (n_b, 2) layout per instance (and the SGD device time in ms)."""
+    if not knns:
+        raise ValueError("at least one instance is required")
+    ks = {np.asarray(i).shape[1] for i, _ in knns}
+    if len(ks) != 1:
+        raise ValueError("every instance needs the same number of neighbours")
+    k = ks.pop()
+    sizes = np.array([np.asarray(i).shape[0] for i, _ in knns], np.int32)
+    offs = {knn_index_offset(i) for i, _ in knns}
+    off = 1 if offs == {1} else 0
+    idx, dist = _concat_knn(knns)
+    y0 = np.concatenate([np.ascontiguousarray(y, np.float32).ravel() for y in inits])
+    if y0.size != 2 * sizes.sum():
+        raise ValueError("init row counts must match the KNN graphs")
+    out = np.zeros((int(sizes.sum()), 2), np.float32)
+    ms = C.c_float()
+    lib = _lib.require_gpu()
+    st = lib.fastembedr_cuda_umap_batch_from_knn(len(knns), sizes.ctypes.data, idx.ctypes.data, dist.ctypes.data,
+                                                 y0.ctypes.data, k, off, int(n_epochs), int(negative_sample_rate),
+                                                 float(learning_rate), float(min_dist), float(repulsion_strength),
+                                                 int(seed) & 0xFFFFFFFF, out.ctypes.data, C.byref(ms))
+    _lib.check(st, "CUDA UMAP batch")
+    lays = np.split(out, np.cumsum(sizes)[:-1])
+    return (lays, ms.value) if return_time else lays

@@ -429,16 +429,38 @@ __device__ __forceinline__ int umap_negative_samples(float period, int rate, uns
 // a captured graph of several epochs replays without re-capture.
 __global__ void __launch_bounds__(256)
 umap_epoch_kernel(float2* __restrict__ y, const int* __restrict__ heads, const int* __restrict__ tails,
-                  const float* __restrict__ eps, long long n_edges, UmapParams p, const unsigned* __restrict__ epoch_ptr) {
+                  const float* __restrict__ eps, long long n_edges, UmapParams p, const unsigned* __restrict__ epoch_ptr,
+                  const long long* __restrict__ edge_begin, const int* __restrict__ vert_begin, int ninst) {
+  // A batch (ninst > 1) lists its instances' edges one after another (edge_begin, ninst + 1
+  // entries) with vertices offset by each instance's first vertex (vert_begin); negatives are
+  // drawn inside the edge's own instance and keyed by the instance-local edge id, so an
+  // instance draws the same negatives alone and in a batch.
   const unsigned epoch = *epoch_ptr;
   const float alpha = p.learning_rate * (1.0f - (float)epoch / fmaxf(1.0f, (float)p.n_epochs));
   const float fe = 1.1920928955078125e-7f;
+  int inst = 0;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n_edges; e += (long long)gridDim.x * blockDim.x) {
     const float period = __ldg(eps + e);
     const int ps = umap_positive_samples(period, epoch);
     if (ps <= 0) continue;
+    long long e_local = e;
+    int v0 = 0, nv = p.n;
+    if (ninst > 1) {
+      if (e < edge_begin[inst] || e >= edge_begin[inst + 1]) {
+        int lo = 0, hi = ninst - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (edge_begin[mid] <= e) lo = mid;
+          else hi = mid - 1;
+        }
+        inst = lo;
+      }
+      e_local = e - edge_begin[inst];
+      v0 = vert_begin[inst];
+      nv = vert_begin[inst + 1] - v0;
+    }
     const int h = __ldg(heads + e), t = __ldg(tails + e);
-    if (h < 0 || h >= p.n || t < 0 || t >= p.n || h == t) continue;
+    if (h < v0 || h >= v0 + nv || t < v0 || t >= v0 + nv || h == t) continue;
     for (int s = 0; s < ps; ++s) {
       const float2 yh = y[h], yt = y[t];
       const float dx = yh.x - yt.x, dy = yh.y - yt.y;
@@ -453,10 +475,10 @@ umap_epoch_kernel(float2* __restrict__ y, const int* __restrict__ heads, const i
     uint4 r = make_uint4(0u, 0u, 0u, 0u);
     for (int s = 0; s < ns; ++s) {
       if ((s & 3) == 0)
-        r = philox4x32_10(make_uint4((unsigned)e, (unsigned)(e >> 32), epoch, (unsigned)(s >> 2)),
+        r = philox4x32_10(make_uint4((unsigned)e_local, (unsigned)(e_local >> 32), epoch, (unsigned)(s >> 2)),
                           make_uint2(p.seed, 0x5eed0f0cu));
       const unsigned draw = (s & 3) == 0 ? r.x : ((s & 3) == 1 ? r.y : ((s & 3) == 2 ? r.z : r.w));
-      const int neg = (int)bounded(draw, (unsigned)p.n);
+      const int neg = v0 + (int)bounded(draw, (unsigned)nv);
       if (neg == h || neg == t) continue;
       const float2 yh = y[h], yn = y[neg];
       const float dx = yh.x - yn.x, dy = yh.y - yn.y;
@@ -553,13 +575,18 @@ struct UmapJob {
     arena.reserve(&epoch, 1);
     arena.commit("UMAP layout");
   }
+  // batch view (set for batches: ninst > 1)
+  const long long* edge_begin = nullptr;
+  const int* vert_begin = nullptr;
+  int ninst = 1;
   void run(const int* heads, const int* tails, const float* eps, long long n_edges, const UmapParams& p) {
     cudaStream_t s = stream.s;
     FE_CUDA(cudaMemsetAsync(epoch, 0, sizeof(unsigned), s));
     const int eblocks = std::max(1, std::min(ceil_div(n_edges, 256), sm_count() * 8));
     const int pblocks = std::max(1, std::min(ceil_div(p.n, 256), sm_count() * 4));
     auto one_epoch = [&]() {
-      umap_epoch_kernel<<<eblocks, 256, 0, s>>>(y, heads, tails, eps, n_edges, p, epoch);
+      umap_epoch_kernel<<<eblocks, 256, 0, s>>>(y, heads, tails, eps, n_edges, p, epoch, edge_begin, vert_begin,
+                                                ninst);
       FE_LAUNCH("umap_epoch_kernel");
       umap_sanitize_kernel<<<pblocks, 256, 0, s>>>(y, p.n, epoch);
       FE_LAUNCH("umap_sanitize_kernel");
@@ -589,6 +616,16 @@ struct UmapJob {
     }
   }
 };
+
+// Append one instance's edges to a batch: heads and tails shifted by its first vertex.
+__global__ void umap_offset_edges_kernel(const int* __restrict__ heads, const int* __restrict__ tails,
+                                         long long nnz, int v0, int* __restrict__ heads_out,
+                                         int* __restrict__ tails_out) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nnz; e += (long long)gridDim.x * blockDim.x) {
+    heads_out[e] = heads[e] + v0;
+    tails_out[e] = tails[e] + v0;
+  }
+}
 
 void check_umap_params(int n, long long n_edges, int n_epochs, int nsr, float lr, float rep) {
   if (n < 2 || n_edges < 1 || n_epochs < 1 || nsr < 0 || !(lr > 0.0f) || !(rep > 0.0f))
@@ -709,6 +746,92 @@ int fastembedr_cuda_umap_from_knn_profile(const int* indices, const float* dista
     a.release();
     if (graph_ms) FE_CUDA(cudaEventElapsedTime(graph_ms, ev[0], ev[1]));
     if (sgd_ms) FE_CUDA(cudaEventElapsedTime(sgd_ms, ev[1], ev[2]));
+  });
+}
+
+int fastembedr_cuda_umap_batch_from_knn(int n_instances, const int* sizes, const int* indices, const float* distances,
+                                        const float* init, int k, int index_offset, int n_epochs,
+                                        int negative_sample_rate, float learning_rate, float min_dist,
+                                        float repulsion_strength, unsigned int seed, float* out, float* sgd_ms) {
+  return fe::guarded([&] {
+    if (!sizes || !indices || !distances || !init || !out) throw fe::Error("null UMAP batch pointer");
+    if (n_instances < 1 || k < 1 || n_epochs < 1 || negative_sample_rate < 0 || !(learning_rate > 0.0f) ||
+        min_dist < 0.0f || !(repulsion_strength > 0.0f))
+      throw fe::Error("invalid CUDA UMAP batch parameters");
+    std::vector<int> vb(n_instances + 1, 0);
+    int max_n = 0;
+    for (int b = 0; b < n_instances; ++b) {
+      if (sizes[b] < 2) throw fe::Error("UMAP batch: every instance needs at least two points");
+      if ((long long)vb[b] + sizes[b] > INT_MAX / 2) throw fe::Error("UMAP batch: too many points");
+      vb[b + 1] = vb[b] + sizes[b];
+      max_n = std::max(max_n, sizes[b]);
+    }
+    const int n = vb[n_instances];
+    fe::UmapJob job;
+    job.alloc(n);
+    cudaStream_t s = job.stream.s;
+    // one fuzzy graph per instance, then appended with vertex offsets
+    std::vector<std::unique_ptr<fe::UmapGraph>> graphs(n_instances);
+    std::vector<long long> eb(n_instances + 1, 0);
+    {
+      int* d_idx = nullptr;
+      float* d_dist = nullptr;
+      fe::Arena in;
+      in.reserve(&d_idx, (std::size_t)max_n * k);
+      in.reserve(&d_dist, (std::size_t)max_n * k);
+      in.commit("UMAP batch input");
+      for (int b = 0; b < n_instances; ++b) {
+        const std::size_t items = (std::size_t)sizes[b] * k, at = (std::size_t)vb[b] * k;
+        FE_CUDA(cudaMemcpyAsync(d_idx, indices + at, sizeof(int) * items, cudaMemcpyHostToDevice, s));
+        FE_CUDA(cudaMemcpyAsync(d_dist, distances + at, sizeof(float) * items, cudaMemcpyHostToDevice, s));
+        fe::validate_knn(d_idx, d_dist, sizes[b], k, index_offset, s);
+        graphs[b] = std::make_unique<fe::UmapGraph>();
+        fe::umap_build_graph(d_idx, d_dist, sizes[b], k, index_offset, *graphs[b], s);
+        eb[b + 1] = eb[b] + graphs[b]->nnz;
+      }
+    }
+    const long long n_edges = eb[n_instances];
+    int *heads = nullptr, *tails = nullptr, *d_vb = nullptr;
+    float* period = nullptr;
+    long long* d_eb = nullptr;
+    fe::Arena ga;
+    ga.reserve(&heads, (std::size_t)std::max<long long>(n_edges, 1));
+    ga.reserve(&tails, (std::size_t)std::max<long long>(n_edges, 1));
+    ga.reserve(&period, (std::size_t)std::max<long long>(n_edges, 1));
+    ga.reserve(&d_eb, n_instances + 1);
+    ga.reserve(&d_vb, n_instances + 1);
+    ga.commit("UMAP batch graph");
+    for (int b = 0; b < n_instances; ++b) {
+      const fe::UmapGraph& g = *graphs[b];
+      const int blocks = std::max(1, std::min(fe::ceil_div(g.nnz, 256), fe::sm_count() * 8));
+      fe::umap_offset_edges_kernel<<<blocks, 256, 0, s>>>(g.heads, g.neighbors, g.nnz, vb[b], heads + eb[b],
+                                                          tails + eb[b]);
+      FE_LAUNCH("umap_offset_edges_kernel");
+      FE_CUDA(cudaMemcpyAsync(period + eb[b], g.eps, sizeof(float) * g.nnz, cudaMemcpyDeviceToDevice, s));
+    }
+    FE_CUDA(cudaMemcpyAsync(d_eb, eb.data(), sizeof(long long) * eb.size(), cudaMemcpyHostToDevice, s));
+    FE_CUDA(cudaMemcpyAsync(d_vb, vb.data(), sizeof(int) * vb.size(), cudaMemcpyHostToDevice, s));
+    FE_CUDA(cudaMemcpyAsync(job.y, init, sizeof(float) * 2 * (std::size_t)n, cudaMemcpyHostToDevice, s));
+    FE_CUDA(cudaStreamSynchronize(s));
+    graphs.clear();
+    double av = 0.0, bv = 0.0;
+    fe::umap_ab_params(1.0, min_dist, &av, &bv);
+    const fe::UmapParams p{n, n_epochs, negative_sample_rate, seed, learning_rate, (float)av, (float)bv,
+                           repulsion_strength};
+    job.edge_begin = d_eb;
+    job.vert_begin = d_vb;
+    job.ninst = n_instances;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    for (auto& e : ev) FE_CUDA(cudaEventCreate(&e));
+    FE_CUDA(cudaEventRecord(ev[0], s));
+    job.run(heads, tails, period, n_edges, p);
+    FE_CUDA(cudaEventRecord(ev[1], s));
+    FE_CUDA(cudaMemcpyAsync(out, job.y, sizeof(float) * 2 * (std::size_t)n, cudaMemcpyDeviceToHost, s));
+    FE_CUDA(cudaStreamSynchronize(s));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, ev[0], ev[1]);
+    for (auto& e : ev) cudaEventDestroy(e);
+    if (sgd_ms) *sgd_ms = ms;
   });
 }
 

@@ -98,6 +98,17 @@ int fastembedr_cuda_umap_graph_from_knn(const int* indices, const float* distanc
 int fastembedr_cuda_umap_from_knn(const int* indices, const float* distances, const float* init, int n, int k,
                                   int index_offset, int n_epochs, int negative_sample_rate, float learning_rate,
                                   float min_dist, float repulsion_strength, unsigned int seed, float* out);
+/* No reference counterpart: many UMAP instances in one job. Each instance's fuzzy graph is built
+ * on its own and appended (vertices offset by the instance's first point); every epoch is one
+ * launch over all edges (negatives drawn inside the edge's own instance, Philox keyed by the
+ * instance-local edge, so an instance draws the same negatives alone and in a batch) and one
+ * clamp launch. sizes[b] points; indices / distances: each instance's column-major n_b x k KNN
+ * one after another (index_offset per instance); init / out: row-major n_b x 2 per instance one
+ * after another. sgd_ms (may be NULL): device time of the epochs. */
+int fastembedr_cuda_umap_batch_from_knn(int n_instances, const int* sizes, const int* indices, const float* distances,
+                                        const float* init, int k, int index_offset, int n_epochs,
+                                        int negative_sample_rate, float learning_rate, float min_dist,
+                                        float repulsion_strength, unsigned int seed, float* out, float* sgd_ms);
 /* The same job, reporting device time (CUDA events on the job's stream) of the graph build and
  * of the n_epochs SGD epochs; either output may be NULL. */
 int fastembedr_cuda_umap_from_knn_profile(const int* indices, const float* distances, const float* init, int n,

@@ -89,3 +89,22 @@ def test_umap_invalid_parameters():
     h = np.array([0, 1], np.int32)
     with pytest.raises(_lib.CudaEmbeddingError, match="invalid"):
         api.umap_optimize_coo(h, h[::-1].copy(), np.ones(2), np.ones(2), np.zeros((2, 2)), 0, 1.9, 0.8)
+
+
+def test_batched_umap_matches_each_instance_alone():
+    """Instances in one batched job reach the local structure they reach alone (15-NN
+    preservation within 0.01; float atomics make runs differ in rounding only)."""
+    knns, inits, xs = [], [], []
+    for j, n in enumerate([3000, 12000, 5000]):
+        x, _ = synthetic.mixture(n, 20, 6, 300 + j, centre_sd=3.0)
+        knns.append(synthetic.exact_knn_numpy(x, 15))
+        inits.append(_pca_init(x, 400 + j))
+    lays = api.umap_knn_batch(knns, inits, n_epochs=200)
+    for (idx, dist), y0, lay in zip(knns, inits, lays):
+        alone = api.umap_knn(idx, dist, y0, n_epochs=200).layout
+        n = idx.shape[0]
+        keep = np.arange(0, n, 2, dtype=np.int32)
+        pa = O.knn_preservation(alone, idx, keep=keep, preserve_k=15)
+        pb = O.knn_preservation(lay, idx, keep=keep, preserve_k=15)
+        assert np.all(np.isfinite(lay)) and np.abs(lay).max() <= 16.0
+        assert abs(pa - pb) < 0.01, (n, pa, pb)
