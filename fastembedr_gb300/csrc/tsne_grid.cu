@@ -316,7 +316,11 @@ scatter_kernel(const float2* __restrict__ y, const TsneInstance* __restrict__ in
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
-__device__ __forceinline__ int bitrev(int i, int logm) { return (int)(__brev((unsigned)i) >> (32 - logm)); }
+// Shared-memory index with one pad slot after every 8 complex values: the radix-2^3 passes with
+// small butterfly strides (1, 8) touch elements 8 or 64 apart from consecutive threads, which
+// would otherwise land on the same banks.
+__device__ __forceinline__ int sidx(int i) { return i + (i >> 3); }
+__host__ __device__ constexpr int padded(int count) { return count + count / 8; }
 
 // Radix-2 FFTs over `count` sequences of length M = 2^logm stored at buf + seq * M, with R
 // consecutive radix-2 stages fused per shared-memory pass (R <= 3): each work item keeps the
@@ -338,11 +342,10 @@ __device__ __forceinline__ void dit_pass(float2* buf, int count, int logm, int s
     const int seq = t >> (logm - R);
     const int rem = t & ((1 << (logm - R)) - 1);
     const int j = rem & (h - 1);
-    const int i0 = ((rem >> s) << (s + R)) + j;
-    float2* a = buf + (seq << logm) + i0;
+    const int i0 = (seq << logm) + ((rem >> s) << (s + R)) + j;
     float2 v[E];
 #pragma unroll
-    for (int e = 0; e < E; ++e) v[e] = a[e * h];
+    for (int e = 0; e < E; ++e) v[e] = buf[sidx(i0 + e * h)];
 #pragma unroll
     for (int st = 0; st < R; ++st) {
       const int span = 1 << st;            // partner distance in units of h
@@ -358,7 +361,7 @@ __device__ __forceinline__ void dit_pass(float2* buf, int count, int logm, int s
       }
     }
 #pragma unroll
-    for (int e = 0; e < E; ++e) a[e * h] = v[e];
+    for (int e = 0; e < E; ++e) buf[sidx(i0 + e * h)] = v[e];
   }
 }
 
@@ -373,11 +376,10 @@ __device__ __forceinline__ void dif_pass(float2* buf, int count, int logm, int s
     const int seq = t >> (logm - R);
     const int rem = t & ((1 << (logm - R)) - 1);
     const int j = rem & (h - 1);
-    const int i0 = ((rem >> s) << (s + R)) + j;
-    float2* a = buf + (seq << logm) + i0;
+    const int i0 = (seq << logm) + ((rem >> s) << (s + R)) + j;
     float2 v[E];
 #pragma unroll
-    for (int e = 0; e < E; ++e) v[e] = a[e * h];
+    for (int e = 0; e < E; ++e) v[e] = buf[sidx(i0 + e * h)];
 #pragma unroll
     for (int st = R - 1; st >= 0; --st) {
       const int span = 1 << st;
@@ -392,7 +394,7 @@ __device__ __forceinline__ void dif_pass(float2* buf, int count, int logm, int s
       }
     }
 #pragma unroll
-    for (int e = 0; e < E; ++e) a[e * h] = v[e];
+    for (int e = 0; e < E; ++e) buf[sidx(i0 + e * h)] = v[e];
   }
 }
 
@@ -419,10 +421,14 @@ __device__ void fft_dif(float2* buf, int count, int logm, const float2* __restri
   }
 }
 
+// Forward transforms are decimation in frequency (natural order in, bit-reversed order out) and
+// inverse transforms decimation in time (bit-reversed in, natural out): the spectra of the
+// charges and of the kernel are multiplied element by element in the same bit-reversed order,
+// so no bit-reversal permutation is ever applied.
 // Row pass. Blocks [0, nodes): charge row r -> forward FFT of the two packed planes
 // A = (x-charge) + i (y-charge), B = mass (the charge row is cleared for the next scatter).
-// Blocks [nodes, 2 nodes): kernel row dy = r - nodes -> forward FFT of (q + i q^2); the
-// kernel is even in dx, so the transform is real-even and only M/2 + 1 entries are kept.
+// Blocks [nodes, 2 nodes): kernel row dy = r - nodes -> forward FFT of (q + i q^2), all M
+// spectral positions kept.
 // blockIdx.y selects the instance members[blockIdx.y] of the grid class.
 __global__ void __launch_bounds__(kFftThreads)
 rows_forward_kernel(const TsneInstance* __restrict__ inst, const int* __restrict__ members, int grid, int nodes,
@@ -435,7 +441,7 @@ rows_forward_kernel(const TsneInstance* __restrict__ inst, const int* __restrict
   float4* __restrict__ charges = inst[b].charges;
   cur += b;
   rows += (long long)blockIdx.y * 2 * nodes * m;
-  krows += (long long)blockIdx.y * nodes * ((m >> 1) + 1);
+  krows += (long long)blockIdx.y * nodes * m;
   if (r < nodes) {
     float4* crow = charges + (long long)r * grid;
     for (int c = threadIdx.x; c < m; c += blockDim.x) {
@@ -446,17 +452,16 @@ rows_forward_kernel(const TsneInstance* __restrict__ inst, const int* __restrict
         a = make_float2(q.y, q.z);
         b = make_float2(q.x, 0.0f);
       }
-      const int rc = bitrev(c, logm);
-      sbuf[rc] = a;
-      sbuf[m + rc] = b;
+      sbuf[sidx(c)] = a;
+      sbuf[sidx(m + c)] = b;
     }
     __syncthreads();
-    fft_dit(sbuf, 2, logm, tw, false);
+    fft_dif(sbuf, 2, logm, tw, false);
     float2* outa = rows + (long long)r * m;
     float2* outb = rows + (long long)(nodes + r) * m;
     for (int c = threadIdx.x; c < m; c += blockDim.x) {
-      outa[c] = sbuf[c];
-      outb[c] = sbuf[m + c];
+      outa[c] = sbuf[sidx(c)];
+      outb[c] = sbuf[sidx(m + c)];
     }
   } else {
     const int kr = r - nodes;
@@ -471,12 +476,12 @@ rows_forward_kernel(const TsneInstance* __restrict__ inst, const int* __restrict
         const float q = 1.0f / (1.0f + d2);
         v = make_float2(q, q * q);
       }
-      sbuf[bitrev(c, logm)] = v;
+      sbuf[sidx(c)] = v;
     }
     __syncthreads();
-    fft_dit(sbuf, 1, logm, tw, false);
-    float2* out = krows + (long long)kr * ((m >> 1) + 1);
-    for (int c = threadIdx.x; c <= (m >> 1); c += blockDim.x) out[c] = sbuf[c];
+    fft_dif(sbuf, 1, logm, tw, false);
+    float2* out = krows + (long long)kr * m;
+    for (int c = threadIdx.x; c < m; c += blockDim.x) out[c] = sbuf[sidx(c)];
   }
 }
 
@@ -492,33 +497,31 @@ columns_convolve_kernel(float2* __restrict__ rows, const float2* __restrict__ kr
   const int m = 1 << logm;
   const int half = m >> 1;
   rows += (long long)blockIdx.y * 2 * nodes * m;
-  krows += (long long)blockIdx.y * nodes * (half + 1);
+  krows += (long long)blockIdx.y * nodes * m;
   zpart += (long long)blockIdx.y * gridDim.x;
   const int c0 = blockIdx.x * cc;
-  float2* kbuf = sbuf + (2 * cc << logm);
+  const int kbase = 2 * cc << logm;  // kernel sequences follow the 2 cc charge sequences
   for (int t = threadIdx.x; t < cc * m; t += blockDim.x) {
     const int j = t % cc, r = t / cc;
     const int c = c0 + j;
-    const int rb = bitrev(r, logm);
     float2 a = make_float2(0.0f, 0.0f), b = make_float2(0.0f, 0.0f);
     if (r < nodes) {
       a = rows[(long long)r * m + c];
       b = rows[(long long)(nodes + r) * m + c];
     }
-    sbuf[((2 * j) << logm) + rb] = a;
-    sbuf[((2 * j + 1) << logm) + rb] = b;
-    const int kc = c <= half ? c : m - c;
+    sbuf[sidx(((2 * j) << logm) + r)] = a;
+    sbuf[sidx(((2 * j + 1) << logm) + r)] = b;
     const int dy = r < half ? r : m - r;
-    kbuf[(j << logm) + rb] = dy <= nodes - 1 ? krows[(long long)dy * (half + 1) + kc] : make_float2(0.0f, 0.0f);
+    sbuf[sidx(kbase + (j << logm) + r)] = dy <= nodes - 1 ? krows[(long long)dy * m + c] : make_float2(0.0f, 0.0f);
   }
   __syncthreads();
-  fft_dit(sbuf, 3 * cc, logm, tw, false);
+  fft_dif(sbuf, 3 * cc, logm, tw, false);
   double zl = 0.0;
   for (int t = threadIdx.x; t < cc * m; t += blockDim.x) {
     const int j = t / m, kr = t % m;
-    const float2 kk = kbuf[(j << logm) + kr];
-    float2& a = sbuf[((2 * j) << logm) + kr];
-    float2& b = sbuf[((2 * j + 1) << logm) + kr];
+    const float2 kk = sbuf[sidx(kbase + (j << logm) + kr)];
+    float2& a = sbuf[sidx(((2 * j) << logm) + kr)];
+    float2& b = sbuf[sidx(((2 * j + 1) << logm) + kr)];
     zl += ((double)b.x * b.x + (double)b.y * b.y) * (double)kk.x;
     a.x *= kk.y;
     a.y *= kk.y;
@@ -526,13 +529,12 @@ columns_convolve_kernel(float2* __restrict__ rows, const float2* __restrict__ kr
     b.y *= kk.y;
   }
   __syncthreads();
-  fft_dif(sbuf, 2 * cc, logm, tw, true);
+  fft_dit(sbuf, 2 * cc, logm, tw, true);
   for (int t = threadIdx.x; t < cc * nodes; t += blockDim.x) {
     const int j = t % cc, r = t / cc;
     const int c = c0 + j;
-    const int rb = bitrev(r, logm);
-    rows[(long long)r * m + c] = sbuf[((2 * j) << logm) + rb];
-    rows[(long long)(nodes + r) * m + c] = sbuf[((2 * j + 1) << logm) + rb];
+    rows[(long long)r * m + c] = sbuf[sidx(((2 * j) << logm) + r)];
+    rows[(long long)(nodes + r) * m + c] = sbuf[sidx(((2 * j + 1) << logm) + r)];
   }
   zl = warp_sum(zl);
   if ((threadIdx.x & 31) == 0) s_z[threadIdx.x >> 5] = zl;
@@ -563,16 +565,15 @@ rows_inverse_kernel(const float2* __restrict__ rows, const TsneInstance* __restr
   const float2* ina = rows + (long long)r * m;
   const float2* inb = rows + (long long)(nodes + r) * m;
   for (int c = threadIdx.x; c < m; c += blockDim.x) {
-    sbuf[c] = ina[c];
-    sbuf[m + c] = inb[c];
+    sbuf[sidx(c)] = ina[c];
+    sbuf[sidx(m + c)] = inb[c];
   }
   __syncthreads();
-  fft_dif(sbuf, 2, logm, tw, true);
+  fft_dit(sbuf, 2, logm, tw, true);
   const float scale = 1.0f / ((float)m * (float)m);
   float4* out = potential + (long long)r * grid;
   for (int c = threadIdx.x; c < nodes; c += blockDim.x) {
-    const int cb = bitrev(c, logm);
-    const float2 a = sbuf[cb], b = sbuf[m + cb];
+    const float2 a = sbuf[sidx(c)], b = sbuf[sidx(m + c)];
     out[c] = make_float4(b.x * scale, a.x * scale, a.y * scale, 0.0f);
   }
   if (r == 0) {
@@ -922,7 +923,7 @@ void build_grid_classes(TsneDevice& d, const std::vector<int>& grids) {
     d.grid_arena.reserve(&k.charges, (std::size_t)k.count * k.grid * k.grid);
     d.grid_arena.reserve(&k.potential, (std::size_t)k.count * k.grid * k.grid);
     d.grid_arena.reserve(&k.rows, (std::size_t)k.count * 2 * k.nodes * m);
-    d.grid_arena.reserve(&k.krows, (std::size_t)k.count * k.nodes * (m / 2 + 1));
+    d.grid_arena.reserve(&k.krows, (std::size_t)k.count * k.nodes * m);
     d.grid_arena.reserve(&k.twiddle, m / 2);
     d.grid_arena.reserve(&k.zpart, (std::size_t)k.count * k.col_blocks);
   }
@@ -959,9 +960,9 @@ void build_grid_classes(TsneDevice& d, const std::vector<int>& grids) {
   d.key_bits = 2 * log2_ceil(max_grid);
   d.sort_bits = d.key_bits + log2_ceil(ninst);
   if (d.sort_bits > 32) throw Error("t-SNE batch: too many instances for the spatial sort key");
-  const int big = 3 * (max_m >= 512 ? 2 : 1) * max_m * (int)sizeof(float2);
+  const int big = padded(3 * (max_m >= 512 ? 2 : 1) * max_m) * (int)sizeof(float2);
   FE_CUDA(cudaFuncSetAttribute(columns_convolve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  const int rowb = 2 * max_m * (int)sizeof(float2);
+  const int rowb = padded(2 * max_m) * (int)sizeof(float2);
   FE_CUDA(cudaFuncSetAttribute(rows_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, rowb));
   FE_CUDA(cudaFuncSetAttribute(rows_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, rowb));
 }
@@ -1075,13 +1076,13 @@ void tsne_grid_stage(TsneDevice& d, cudaStream_t s) {
   FE_LAUNCH("scatter_kernel");
   for (const GridClass& c : d.classes) {
     const int m = c.fft;
-    rows_forward_kernel<<<dim3(2 * c.nodes, c.count), kFftThreads, 2 * m * sizeof(float2), s>>>(
+    rows_forward_kernel<<<dim3(2 * c.nodes, c.count), kFftThreads, padded(2 * m) * sizeof(float2), s>>>(
         d.d_inst, c.members, c.grid, c.nodes, c.log_fft, c.twiddle, d.cur, c.rows, c.krows);
     FE_LAUNCH("rows_forward_kernel");
-    columns_convolve_kernel<<<dim3(c.col_blocks, c.count), kFftThreads, 3 * c.cols_per_block * m * sizeof(float2),
-                              s>>>(c.rows, c.krows, c.nodes, c.log_fft, c.cols_per_block, c.twiddle, c.zpart);
+    columns_convolve_kernel<<<dim3(c.col_blocks, c.count), kFftThreads,
+                              padded(3 * c.cols_per_block * m) * sizeof(float2), s>>>(c.rows, c.krows, c.nodes, c.log_fft, c.cols_per_block, c.twiddle, c.zpart);
     FE_LAUNCH("columns_convolve_kernel");
-    rows_inverse_kernel<<<dim3(c.nodes, c.count), kFftThreads, 2 * m * sizeof(float2), s>>>(
+    rows_inverse_kernel<<<dim3(c.nodes, c.count), kFftThreads, padded(2 * m) * sizeof(float2), s>>>(
         c.rows, d.d_inst, c.members, c.grid, c.nodes, c.log_fft, c.twiddle, c.zpart, c.col_blocks, d.cur);
     FE_LAUNCH("rows_inverse_kernel");
   }
