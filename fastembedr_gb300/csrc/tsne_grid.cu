@@ -31,6 +31,7 @@ namespace fe {
 
 constexpr int kStepThreads = 256;
 constexpr int kFftThreads = 256;
+constexpr int kColThreads = 512;  // the column pass holds 110 KB of shared memory: 2 blocks per SM
 
 // ---------------------------------------------------------------- stencils
 template <int TAPS>
@@ -489,11 +490,11 @@ rows_forward_kernel(const TsneInstance* __restrict__ inst, const int* __restrict
 // spectra Kq + i Kq2) and the two charge planes, accumulate sum |F_mass|^2 Kq (Parseval form
 // of sum_nodes mass * (mass conv q), i.e. Z + n up to the 1/M^2 scale), multiply the charge
 // spectra by Kq2 and transform back. Only rows < nodes of the result are written.
-__global__ void __launch_bounds__(kFftThreads)
+__global__ void __launch_bounds__(kColThreads)
 columns_convolve_kernel(float2* __restrict__ rows, const float2* __restrict__ krows, int nodes, int logm, int cc,
                         const float2* __restrict__ tw, double* __restrict__ zpart) {
   extern __shared__ float2 sbuf[];  // [2 cc charge sequences][cc kernel sequences]
-  __shared__ double s_z[kFftThreads / 32];
+  __shared__ double s_z[kColThreads / 32];
   const int m = 1 << logm;
   const int half = m >> 1;
   rows += (long long)blockIdx.y * 2 * nodes * m;
@@ -1079,7 +1080,7 @@ void tsne_grid_stage(TsneDevice& d, cudaStream_t s) {
     rows_forward_kernel<<<dim3(2 * c.nodes, c.count), kFftThreads, padded(2 * m) * sizeof(float2), s>>>(
         d.d_inst, c.members, c.grid, c.nodes, c.log_fft, c.twiddle, d.cur, c.rows, c.krows);
     FE_LAUNCH("rows_forward_kernel");
-    columns_convolve_kernel<<<dim3(c.col_blocks, c.count), kFftThreads,
+    columns_convolve_kernel<<<dim3(c.col_blocks, c.count), m >= 2048 ? kColThreads : kFftThreads,
                               padded(3 * c.cols_per_block * m) * sizeof(float2), s>>>(c.rows, c.krows, c.nodes, c.log_fft, c.cols_per_block, c.twiddle, c.zpart);
     FE_LAUNCH("columns_convolve_kernel");
     rows_inverse_kernel<<<dim3(c.nodes, c.count), kFftThreads, padded(2 * m) * sizeof(float2), s>>>(
