@@ -43,6 +43,8 @@ SIGNATURES = {
     "fastembedr_cuda_tsne_exact_repulsion_noalloc": (I, [vp, I, vp, vp, vp]),
     "fastembedr_cuda_transform_tsne": (I, [vp, I, vp, vp, I, I, vp, I, C.c_char_p, D, I, I, D, D, D, D, D, D, D, I, I,
                                            I, vp]),
+    "fastembedr_cuda_landmark_tsne_from_device_knn": (I, [vp, vp, I, vp, vp, vp, I, I, I, I, F, I, I, F, F, F, F, F,
+                                                          F, F, I, I, U, I, F, F, vp]),
     "fastembedr_transform_server_create": (I, [vp, I, D, I, I, D, D, D, D, D, D, D, I, I, I, C.c_char_p, C.c_ulonglong,
                                                I, C.POINTER(vp)]),
     "fastembedr_transform_server_submit": (I, [vp, vp, vp, I, I, C.POINTER(C.c_ulonglong)]),

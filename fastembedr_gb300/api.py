@@ -635,3 +635,34 @@ def umap_knn_batch(knns, inits, seed=42, n_epochs=500, min_dist=0.01, negative_s
     _lib.check(st, "CUDA UMAP batch")
     lays = np.split(out, np.cumsum(sizes)[:-1])
     return (lays, ms.value) if return_time else lays
+
+
+def landmark_tsne_transform(reference_data, query_data, reference_layout, indices, distances, perplexity=5.0,
+                            n_iter=250, early_exaggeration_iter=0, learning_rate=0.1, early_exaggeration=4.0,
+                            exaggeration=1.5, initial_momentum=0.8, final_momentum=0.8, max_grad_norm=0.25,
+                            max_step_norm=math.inf, n_negatives=256, exact_repulsion_threshold=4096, seed=4,
+                            affine_neighbors=8, affine_ridge=1e-3, max_extrapolation=1.5):
+    """Landmark t-SNE projection through fastembedr_cuda_landmark_tsne_from_device_knn: the query
+    KNN (n_query, k) into the landmarks goes to the device first, as in the reference's
+    device-KNN route; the data matrices and the landmark layout are host arrays."""
+    import torch
+
+    idx = np.asarray(indices)
+    n_query, k = idx.shape
+    off = 1 if idx.min() >= 1 and idx.max() <= np.asarray(reference_layout).shape[0] else 0
+    d_idx = torch.as_tensor(np.ascontiguousarray(idx.T, np.int32), device="cuda")
+    d_dist = torch.as_tensor(np.ascontiguousarray(np.asarray(distances, np.float32).T), device="cuda")
+    torch.cuda.current_stream().synchronize()
+    X = _colmajor(reference_data, np.float32)
+    Q = _colmajor(query_data, np.float32)
+    L = _colmajor(reference_layout, np.float32)
+    out = np.zeros((n_query, 2), np.float32)
+    lib = _lib.require_gpu()
+    st = lib.fastembedr_cuda_landmark_tsne_from_device_knn(
+        d_idx.data_ptr(), d_dist.data_ptr(), off, X.ctypes.data, Q.ctypes.data, L.ctypes.data, L.shape[0], n_query,
+        X.shape[1], k, float(perplexity), int(n_iter), int(early_exaggeration_iter), float(learning_rate),
+        float(early_exaggeration), float(exaggeration), float(initial_momentum), float(final_momentum),
+        float(max_grad_norm), float(max_step_norm), int(n_negatives), int(exact_repulsion_threshold),
+        int(seed) & 0xFFFFFFFF, int(affine_neighbors), float(affine_ridge), float(max_extrapolation), out.ctypes.data)
+    _lib.check(st, "CUDA landmark t-SNE")
+    return out

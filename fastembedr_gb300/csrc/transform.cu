@@ -310,7 +310,22 @@ transform_iterate_kernel(const float2* __restrict__ ref, const TransformSegment*
     const float exg = early ? tp.early_exag : tp.exag;
     const float mom = early ? tp.m0 : tp.m1;
     float fz = 0.0f, fx = 0.0f, fy = 0.0f;
-    if (MODE == 0) {
+    if (MODE == 0 && tp.hash_sampler) {
+      // landmark_reference_sample of the reference's landmark transform
+      // (src/embedding_cuda_kernels.cpp:511-521): an independent hash per sample
+      const std::uint32_t base = (std::uint32_t)tp.seed ^ ((std::uint32_t)(it + 1) * 0x9e3779b9u) ^
+                                 ((std::uint32_t)(i + 1) * 0x85ebca6bu);
+#pragma unroll 4
+      for (int m = lane; m < tp.n_negatives; m += 32) {
+        std::uint32_t x = base ^ ((std::uint32_t)(m + 1) * 0xc2b2ae35u);
+        x ^= x >> 16u;
+        x *= 0x7feb352du;
+        x ^= x >> 15u;
+        x *= 0x846ca68bu;
+        x ^= x >> 16u;
+        repulse(__ldg(&ref[x % (std::uint32_t)tp.n_ref]), yhx, yhy, ylx, yly, fz, fx, fy);
+      }
+    } else if (MODE == 0) {
       const std::uint32_t iter_seed = (std::uint32_t)tp.seed + 65537u * (std::uint32_t)(it + 1);
       std::uint32_t s = gf2_apply(sjump, lane, mix_u32(iter_seed ^ salt));
 #pragma unroll 4

@@ -22,6 +22,7 @@ struct TransformParams {
   int early_iter = 0;
   int init_mode = 1;      // 0 supplied, 1 median, 2 weighted
   int seed = 0;
+  int hash_sampler = 0;   // 1: samples by the landmark path's per-(iteration, query, sample) hash
   float lr = 0.1f, early_exag = 4.0f, exag = 1.5f, m0 = 0.8f, m1 = 0.8f;
   float max_grad = 0.25f, max_step = 3.4e38f;
   double perplexity = 5.0;

@@ -168,6 +168,27 @@ int fastembedr_cuda_transform_tsne(const double* reference_layout, int n_referen
                                    double max_grad_norm, double max_step_norm, int n_negatives,
                                    int exact_repulsion_threshold, int seed, double* out);
 
+/* replaces fastembedr_cuda_landmark_tsne_from_device_knn, src/embedding_cuda_kernels.cpp:3572-3686
+ * (project_landmark_model's CUDA route, landmark_tsne_transform_cuda_gpu_cpp,
+ * src/embedding_cuda_bridge.cpp:584-612). device_indices / device_distances: device pointers,
+ * column-major n_query x k (k <= 128); reference_data (n_reference x n_features), query_data
+ * (n_query x n_features) and reference_layout (n_reference x 2): host, column-major float.
+ * Each query starts at the ridge-regularised local affine projection of its first
+ * affine_neighbors (3..12) landmarks, displacement bounded by max_extrapolation times their
+ * layout radius, then runs the fixed-reference iterations with the landmark hash sampler
+ * (n_negatives per query and iteration; exact when n_reference <= exact_repulsion_threshold).
+ * out: host, row-major n_query x 2 floats. */
+int fastembedr_cuda_landmark_tsne_from_device_knn(const int* device_indices, const float* device_distances,
+                                                  int index_offset, const float* reference_data,
+                                                  const float* query_data, const float* reference_layout,
+                                                  int n_reference, int n_query, int n_features, int k,
+                                                  float perplexity, int n_iter, int early_exaggeration_iter,
+                                                  float learning_rate, float early_exaggeration, float exaggeration,
+                                                  float initial_momentum, float final_momentum, float max_grad_norm,
+                                                  float max_step_norm, int n_negatives, int exact_repulsion_threshold,
+                                                  unsigned int seed, int affine_neighbors, float affine_ridge,
+                                                  float max_extrapolation, float* out);
+
 /* ---------------------------------------------------------------- transform serving loop
  * No counterpart in the reference: fastembedr_cuda_landmark_tsne_from_device_knn
  * (src/embedding_cuda_kernels.cpp:3572-3686) uploads the reference and rebuilds its state on
