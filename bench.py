@@ -42,6 +42,24 @@ def dist_env():
     return rank, world, local
 
 
+def replica_time_ms(ms, world, device):
+    """The job's time over N replicas is the slowest replica's: max over ranks (all_reduce MAX
+    on the process group; gloo on CPU tensors, NCCL on CUDA tensors)."""
+    import torch
+
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    if world > 1:
+        import torch.distributed as tdist
+
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_rate(steps, ms, world):
+    """Whole-job rate: every replica ran `steps` units in at most `ms` milliseconds."""
+    return world * steps / (ms / 1e3)
+
+
 def make_inputs(device, n=N_POINTS):
     """The 1M-point mixture (or the same generator at n points, for profiling captures) and its
     exact KNN (torch brute force on the GPU: setup only)."""
@@ -201,7 +219,7 @@ def run_gpu(args):
     info = plan.info()
     lr = n / 12.0
     # untimed early-exaggeration phase, as in a real run, then the warm-up steps: at least two
-    # 25-iteration chunks, so that the CUDA graphs of both CSR buffers of the reorder exist
+    # 25-iteration chunks, so that the timed chunks' CUDA graph is captured before timing
     plan.run(250, 12.0, lr)
     plan.run(max(args.warmup, 50), 1.0, lr)
     plan.synchronize()
@@ -225,12 +243,9 @@ def run_gpu(args):
     # dominant kernel, timed alone with CUDA events on the plan's stream over the same number of steps
     prof = plan.profile(args.steps, 1.0, lr)
     kl = plan.kl() if not args.no_kl else None
-    t_ms = torch.tensor([ms], device=device)
-    if world > 1:
-        tdist.all_reduce(t_ms, op=tdist.ReduceOp.MAX)
-    ms = float(t_ms.item())
+    ms = replica_time_ms(ms, world, device)
     plan.close()
-    value = world * args.steps / (ms / 1e3)
+    value = aggregate_rate(args.steps, ms, world)
 
     # the same instance under the adaptive box count (grid sizes chosen from the layout every 25
     # iterations), timed the same way; its KL is taken after as many iterations as the main plan's
