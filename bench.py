@@ -33,6 +33,7 @@ N_POINTS = 1_000_000
 K = 90
 PERPLEXITY = 30.0
 WORKLOAD = "tsne_knn_1M_k90_perp30"
+GRADIENT_SEED = 2026  # seed of the gradient-check sample
 
 
 def dist_env():
@@ -153,6 +154,15 @@ def cpu_baseline(idx_cpu, dist_cpu, iters):
     return iters / dt, threads, dt
 
 
+def gradient_summary(plan, args):
+    """Grid gradient of the final layout against exact FP64-summed repulsion (all-pairs Z) at a
+    seeded sample of points."""
+    c = plan.gradient_check(sample=args.check_sample, seed=GRADIENT_SEED)
+    return {"sample": int(c["rows"].shape[0]), "seed": GRADIENT_SEED, "grid_size": plan.info()["grid_size"],
+            "gradient_rel_l2": c["gradient_rel_l2"], "repulsion_rel_l2": c["repulsion_rel_l2"],
+            "repulsion_max_rel": c["repulsion_max_rel"], "z_rel_err": c["z_rel_err"]}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -243,6 +253,7 @@ def run_gpu(args):
     # dominant kernel, timed alone with CUDA events on the plan's stream over the same number of steps
     prof = plan.profile(args.steps, 1.0, lr)
     kl = plan.kl() if not args.no_kl else None
+    gcheck = gradient_summary(plan, args) if not args.no_kl else None
     ms = replica_time_ms(ms, world, device)
     plan.close()
     value = aggregate_rate(args.steps, ms, world)
@@ -267,12 +278,13 @@ def run_gpu(args):
             ms2 = a0.elapsed_time(a1)
             plan2.run(args.steps, 1.0, lr)  # as many iterations as the main plan's profiling pass
             kl2 = plan2.kl() if not args.no_kl else None
+            gcheck2 = gradient_summary(plan2, args) if not args.no_kl else None
             g2 = plan2.info()["grid_size"]
             plan2.close()
         finally:
             del os.environ["FASTEMBEDR_TSNE_FFT_GRID"]
         adaptive = {"value": world * args.steps / (ms2 / 1e3), "unit": "iter/s", "ms_per_step": ms2 / args.steps,
-                    "grid_at_end": g2, "kl_after_run": kl2,
+                    "grid_at_end": g2, "kl_after_run": kl2, "gradient_check": gcheck2,
                     "policy": "adaptive box count: node spacing <= 0.7 over the current layout, >= 128 nodes, "
                               "re-chosen every 25 iterations"}
 
@@ -333,6 +345,8 @@ def run_gpu(args):
     }
     if kl is not None:
         line["kl_after_run"] = kl
+    if gcheck is not None:
+        line["gradient_check"] = gcheck
     if adaptive is not None:
         line["adaptive_grid"] = adaptive
     if rank == 0 and not args.no_cpu:
@@ -790,7 +804,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-iters", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--no-kl", action="store_true")
+    ap.add_argument("--no-kl", action="store_true", help="skip the exact KL and the gradient check")
+    ap.add_argument("--check-sample", type=int, default=20000, help="points of the gradient check")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adaptive", action="store_true", help="skip the adaptive-grid run of the 1M instance")
     ap.add_argument("--n", type=int, default=N_POINTS, help="points (profiling captures use a smaller case)")

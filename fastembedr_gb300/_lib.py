@@ -60,6 +60,7 @@ SIGNATURES = {
     "fastembedr_tsne_plan_layout": (I, [vp, vp]),
     "fastembedr_tsne_plan_info": (I, [vp, C.POINTER(L), C.POINTER(I), C.POINTER(I), C.POINTER(I), C.POINTER(I)]),
     "fastembedr_tsne_plan_kl": (I, [vp, C.POINTER(D)]),
+    "fastembedr_tsne_plan_gradient_check": (I, [vp, vp, I, F, vp, vp, vp, C.POINTER(D), C.POINTER(D)]),
     "fastembedr_tsne_plan_destroy": (None, [vp]),
     "fastembedr_tsne_batch_create": (I, [I, vp, vp, vp, vp, I, F, I, I, I, U, C.POINTER(vp)]),
     "fastembedr_tsne_batch_run": (I, [vp, I, I, F, F, F, F, F, F, F]),

@@ -235,6 +235,31 @@ class TsnePlan:
         _lib.check(self.lib.fastembedr_tsne_plan_kl(self.h, C.byref(v)), "t-SNE plan KL")
         return v.value
 
+    def gradient_check(self, sample=20000, seed=0, exaggeration=1.0):
+        """Grid gradient of the current layout against the exact FP64-summed repulsion at a seeded
+        sample of points (``sample`` ids drawn without replacement, or an array of ids)."""
+        if np.ndim(sample) == 0:
+            rows = np.sort(np.random.default_rng(seed).choice(self.n, min(int(sample), self.n), replace=False))
+        else:
+            rows = np.asarray(sample)
+        rows = np.ascontiguousarray(rows, np.int32)
+        m = rows.shape[0]
+        attr = np.zeros((m, 2), np.float32)
+        rep = np.zeros((m, 2), np.float32)
+        rex = np.zeros((m, 2), np.float64)
+        zg, ze = C.c_double(), C.c_double()
+        _lib.check(self.lib.fastembedr_tsne_plan_gradient_check(self.h, rows.ctypes.data, m, float(exaggeration),
+                                                                attr.ctypes.data, rep.ctypes.data, rex.ctypes.data,
+                                                                C.byref(zg), C.byref(ze)), "t-SNE gradient check")
+        g_grid = attr.astype(np.float64) + rep
+        g_exact = attr.astype(np.float64) + rex
+        rel = lambda a, b: float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+        return dict(rows=rows, attractive=attr, repulsive_grid=rep, repulsive_exact=rex, z_grid=zg.value,
+                    z_exact=ze.value, z_rel_err=(zg.value - ze.value) / ze.value,
+                    repulsion_rel_l2=rel(rep, rex), gradient_rel_l2=rel(g_grid, g_exact),
+                    repulsion_max_rel=float(np.max(np.linalg.norm(rep - rex, axis=1))
+                                            / max(np.max(np.linalg.norm(rex, axis=1)), 1e-300)))
+
     def close(self):
         if getattr(self, "h", None):
             self.lib.fastembedr_tsne_plan_destroy(self.h)

@@ -60,6 +60,17 @@ __global__ void append_csr_kernel(const int* __restrict__ rp, const int* __restr
     col_out[t] = col[t] + first;
 }
 
+// out[r] = full[inv[rows[r]]] for the two float2 force fields of a diagnostic.
+__global__ void gather_rows_kernel(const float2* __restrict__ a, const float2* __restrict__ b,
+                                   const int* __restrict__ rows, const int* __restrict__ inv, int n_rows,
+                                   float2* __restrict__ a_out, float2* __restrict__ b_out) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rows; r += gridDim.x * blockDim.x) {
+    const int si = inv[rows[r]];
+    a_out[r] = a[si];
+    b_out[r] = b[si];
+  }
+}
+
 // Optimizer state of one t-SNE instance (or a batch of instances) resident on the device.
 struct TsneJob {
   DeviceCsr P;
@@ -636,6 +647,65 @@ int fastembedr_tsne_plan_kl(fastembedr_tsne_plan* plan, double* kl) {
     fe::exact_kl(J.P, reinterpret_cast<const float*>(J.D.y), J.D.inv, d_zrow, d_work, d_sc, s);
     FE_CUDA(cudaMemcpyAsync(kl, d_sc + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
     FE_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int fastembedr_tsne_plan_gradient_check(fastembedr_tsne_plan* plan, const int* rows, int n_rows,
+                                        float exaggeration, float* attractive, float* repulsive_grid,
+                                        double* repulsive_exact, double* z_grid, double* z_exact) {
+  return fe::guarded([&] {
+    if (!plan || !rows || !attractive || !repulsive_grid || !repulsive_exact)
+      throw fe::Error("null CUDA t-SNE gradient check pointer");
+    fe::TsneJob& J = plan->job;
+    const int n = J.D.n;
+    if (n_rows < 1 || n_rows > n || !(exaggeration > 0.0f)) throw fe::Error("invalid CUDA t-SNE gradient check");
+    for (int r = 0; r < n_rows; ++r)
+      if (rows[r] < 0 || rows[r] >= n) throw fe::Error("gradient check row out of range");
+    if (J.D.inst.size() != 1) throw fe::Error("gradient check needs a single-instance plan");
+    cudaStream_t s = J.stream.s;
+    const int slices = fe::exact_rows_slices(n, n_rows);
+    int* d_rows = nullptr;
+    float2* d_attr = nullptr;
+    float2* d_rep = nullptr;
+    float2* d_attr_rows = nullptr;
+    float2* d_rep_rows = nullptr;
+    double* d_part = nullptr;
+    double* d_out = nullptr;
+    double* d_zrow = nullptr;
+    double* d_sc = nullptr;
+    fe::Arena a;
+    a.reserve(&d_rows, n_rows);
+    a.reserve(&d_attr, n);
+    a.reserve(&d_rep, n);
+    a.reserve(&d_attr_rows, n_rows);
+    a.reserve(&d_rep_rows, n_rows);
+    a.reserve(&d_part, (std::size_t)slices * 3 * n_rows);
+    a.reserve(&d_out, 3 * (std::size_t)n_rows);
+    a.reserve(&d_zrow, n);
+    a.reserve(&d_sc, 2);
+    a.commit("t-SNE gradient check");
+    FE_CUDA(cudaMemcpyAsync(d_rows, rows, sizeof(int) * n_rows, cudaMemcpyHostToDevice, s));
+    // the grid forces of the current layout (the optimizer state is left as it was)
+    fe::tsne_forces(J.D, J.P, exaggeration, reinterpret_cast<float*>(d_attr), reinterpret_cast<float*>(d_rep), s);
+    FE_CUDA(cudaMemcpyAsync(d_sc + 1, &J.D.cur->z, sizeof(double), cudaMemcpyDeviceToDevice, s));
+    fe::gather_rows_kernel<<<std::max(1, std::min(fe::ceil_div(n_rows, 256), fe::sm_count() * 4)), 256, 0, s>>>(
+        d_attr, d_rep, d_rows, J.D.inv, n_rows, d_attr_rows, d_rep_rows);
+    FE_LAUNCH("gather_rows_kernel");
+    fe::exact_repulsion_rows(reinterpret_cast<const float*>(J.D.y), n, d_rows, J.D.inv, n_rows, d_part, d_out, d_zrow,
+                             d_sc, s);
+    std::vector<double> ex(3 * (std::size_t)n_rows);
+    double zs[2] = {0.0, 0.0};
+    FE_CUDA(cudaMemcpyAsync(attractive, d_attr_rows, sizeof(float2) * n_rows, cudaMemcpyDeviceToHost, s));
+    FE_CUDA(cudaMemcpyAsync(repulsive_grid, d_rep_rows, sizeof(float2) * n_rows, cudaMemcpyDeviceToHost, s));
+    FE_CUDA(cudaMemcpyAsync(ex.data(), d_out, sizeof(double) * ex.size(), cudaMemcpyDeviceToHost, s));
+    FE_CUDA(cudaMemcpyAsync(zs, d_sc, sizeof(zs), cudaMemcpyDeviceToHost, s));
+    FE_CUDA(cudaStreamSynchronize(s));
+    for (int r = 0; r < n_rows; ++r) {
+      repulsive_exact[2 * (std::size_t)r] = ex[r] / zs[0];
+      repulsive_exact[2 * (std::size_t)r + 1] = ex[(std::size_t)n_rows + r] / zs[0];
+    }
+    if (z_exact) *z_exact = zs[0];
+    if (z_grid) *z_grid = zs[1];
   });
 }
 

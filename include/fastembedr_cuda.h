@@ -256,6 +256,16 @@ int fastembedr_tsne_plan_info(fastembedr_tsne_plan* plan, long long* nnz, int* g
                               int* launches_per_iteration, int* launches_per_reorder);
 /* exact KL of the current layout (all-pairs Z on the GPU) */
 int fastembedr_tsne_plan_kl(fastembedr_tsne_plan* plan, double* kl);
+/* Gradient check of the plan's current layout at selected points (the force part of
+ * opentsne_force_diagnostic_cpp, src/tsne_neighbors.cpp:1698-1817, evaluated in place on a resident
+ * run so that an instance too large for the all-pairs diagnostic can still be checked). rows: n_rows
+ * 0-based point ids (host). Writes row-major n_rows x 2 arrays: the attractive force
+ * (exaggeration-scaled), the grid repulsion divided by the grid Z, and the exact repulsion of each
+ * selected point against all n points (FP32 pair terms, FP64 sums) divided by the exact all-pairs
+ * Z; z_grid / z_exact (may be NULL) receive both Z. The optimizer state is not changed. */
+int fastembedr_tsne_plan_gradient_check(fastembedr_tsne_plan* plan, const int* rows, int n_rows,
+                                        float exaggeration, float* attractive, float* repulsive_grid,
+                                        double* repulsive_exact, double* z_grid, double* z_exact);
 void fastembedr_tsne_plan_destroy(fastembedr_tsne_plan* plan);
 
 /* ---------------------------------------------------------------- batched t-SNE

@@ -238,3 +238,39 @@ def test_spatial_reorder_preserves_results(small, monkeypatch):
     rp, col, val, _ = O.tsne_csr(idx, dist, 15.0)
     for y, kv in zip(outs, kls):
         assert kv == pytest.approx(O.kl(rp, col, val, y), rel=1e-5)
+
+
+def test_plan_gradient_check_matches_diagnostic_and_oracle(c1):
+    """Gradient check of a resident run at a seeded sample: the exact part against the FP64 oracle
+    on the plan's layout, the grid part and the attraction against the force diagnostic on the
+    same layout and grid, and the size of the grid approximation error."""
+    import torch
+
+    idx, dist, _ = c1
+    n, k = idx.shape
+    d_idx = torch.as_tensor(np.ascontiguousarray(idx.T), device="cuda")
+    d_dist = torch.as_tensor(np.ascontiguousarray(dist.T), device="cuda")
+    plan = api.TsnePlan(d_idx, d_dist, n, k, 30.0, init=synthetic.tsne_init(n, 5))
+    plan.run(250, 12.0, n / 12.0)
+    plan.run(100, 1.0, n / 12.0)
+    chk = plan.gradient_check(sample=2000, seed=1)
+    y = plan.layout()
+    grid = plan.info()["grid_size"]
+    # the check leaves the optimizer state alone: the next iterations continue as before
+    plan.run(5, 1.0, n / 12.0)
+    assert np.all(np.isfinite(plan.layout()))
+    plan.close()
+    rows = chk["rows"]
+    assert rows.shape == (2000,) and np.all(np.diff(rows) > 0)
+    ex64, z64 = O.exact_rep_f64(y)
+    assert chk["z_exact"] == pytest.approx(z64, rel=1e-6)
+    assert rel_l2(chk["repulsive_exact"], ex64[rows]) < 1e-5
+    d = api.tsne_force_diagnostic(idx, dist, y, 30.0, grid_size=grid, exact=False, kl=False)
+    assert rel_l2(chk["attractive"], d["attractive_force"][rows].astype(np.float64)) < 1e-5
+    assert rel_l2(chk["repulsive_grid"], d["repulsive_force_fft"][rows].astype(np.float64)) < 1e-3
+    assert chk["z_grid"] == pytest.approx(d["z_grid"], rel=1e-4)
+    # grid approximation error: the gradient is a small difference of attraction and repulsion
+    # once the layout has settled, so its relative error is several times the repulsion's
+    assert abs(chk["z_rel_err"]) < 1e-2
+    assert chk["repulsion_rel_l2"] < 0.05, chk["repulsion_rel_l2"]
+    assert chk["gradient_rel_l2"] < 0.25, chk["gradient_rel_l2"]
