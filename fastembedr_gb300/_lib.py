@@ -60,6 +60,14 @@ SIGNATURES = {
     "fastembedr_tsne_plan_layout": (I, [vp, vp]),
     "fastembedr_tsne_plan_info": (I, [vp, C.POINTER(L), C.POINTER(I), C.POINTER(I), C.POINTER(I), C.POINTER(I)]),
     "fastembedr_tsne_plan_kl": (I, [vp, C.POINTER(D)]),
+    "fastembedr_cuda_umap_spectral_init_from_knn": (I, [vp, vp, I, I, I, I, D, I, vp]),
+    "fastembedr_cuda_umap_spectral_init_csr": (I, [vp, vp, vp, I, I, D, I, vp]),
+    "fastembedr_cuda_umap_knn_spectral": (I, [vp, vp, I, I, I, I, I, F, F, F, I, D, U, vp]),
+    "fastembedr_umap_find_ab_params": (None, [D, D, C.POINTER(D), C.POINTER(D)]),
+    "fastembedr_cuda_spectral_init_from_knn": (I, [vp, vp, I, I, I, U, I, vp]),
+    "fastembedr_cuda_umap_from_knn_spectral": (I, [vp, vp, I, I, I, I, F, F, F, F, I, U, I, I, vp]),
+    "fastembedr_cuda_umap_from_knn_spectral_float": (I, [vp, vp, I, I, I, I, F, F, F, F, I, U, I, I, vp]),
+    "fastembedr_cuda_umap_from_device_knn_spectral_float": (I, [vp, vp, I, I, I, I, F, F, F, F, I, U, I, I, I, vp]),
     "fastembedr_tsne_plan_gradient_check": (I, [vp, vp, I, F, vp, vp, vp, C.POINTER(D), C.POINTER(D)]),
     "fastembedr_tsne_plan_destroy": (None, [vp]),
     "fastembedr_tsne_batch_create": (I, [I, vp, vp, vp, vp, I, F, I, I, I, U, C.POINTER(vp)]),

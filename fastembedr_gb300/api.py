@@ -432,12 +432,77 @@ def umap_optimize_coo(heads, tails, weights, epochs_per_sample, init, n_epochs, 
     return out
 
 
-def umap_knn(indices, distances, init, n_components=2, seed=42, n_epochs=None, min_dist=0.01,
-             negative_sample_rate=5, learning_rate=1.0, repulsion_strength=1.0, backend="cuda") -> UmapFit:
+def umap_ab_params(min_dist, spread=1.0):
+    """Curve parameters a, b (find_ab_params, src/fast_knn_umap.cpp:437-497; host code)."""
+    a, b = C.c_double(), C.c_double()
+    _lib.load().fastembedr_umap_find_ab_params(float(spread), float(min_dist), C.byref(a), C.byref(b))
+    return a.value, b.value
+
+
+def umap_spectral_n_iter(n, k):
+    """Diffusion rounds of the package size policy (umap_size_defaults, R/fast_knn_umap.R:947-965)."""
+    if n >= 10000:
+        return 30 if k <= 15 else 20
+    return 60 if n >= 500 else 50
+
+
+def umap_spectral_init(indices, distances, spectral_n_iter=50, seed=42, index_offset=None):
+    """GPU diffusion start of spectral_knn_init(backend = "cuda") (R/fast_knn_umap.R:1309-1341,
+    through fastembedr_cuda_spectral_init_from_knn): row-major (n, 2) float32, whitened."""
+    idx = np.asarray(indices)
+    n, k = idx.shape
+    off = knn_index_offset(idx) if index_offset is None else int(index_offset)
+    idx_cm, dist_cm = _colmajor(idx, np.int32), _colmajor(distances, np.float64)
+    out = np.zeros((n, 2), np.float32)
+    st = _lib.require_gpu().fastembedr_cuda_spectral_init_from_knn(idx_cm.ctypes.data, dist_cm.ctypes.data, n, k,
+                                                                   int(spectral_n_iter), int(seed) & 0xFFFFFFFF, off,
+                                                                   out.ctypes.data)
+    _lib.check(st, "CUDA spectral initialization")
+    return out
+
+
+def umap_spectral_start(indices, distances, spectral_n_iter=50, seed=42, init_scale=float("nan"),
+                        index_offset=None):
+    """The reference CPU spectral start (spectral_knn_init(backend = "cpu"), R/fast_knn_umap.R:1343-1365)
+    computed on the GPU: (n, 2) float64, equal to the CPU start to rounding."""
+    idx = np.asarray(indices)
+    n, k = idx.shape
+    off = knn_index_offset(idx) if index_offset is None else int(index_offset)
+    idx_cm, dist_cm = _colmajor(idx, np.int32), _colmajor(distances, np.float32)
+    out = np.zeros(2 * n)
+    st = _lib.require_gpu().fastembedr_cuda_umap_spectral_init_from_knn(idx_cm.ctypes.data, dist_cm.ctypes.data, n,
+                                                                        k, off, int(spectral_n_iter),
+                                                                        float(init_scale), int(seed), out.ctypes.data)
+    _lib.check(st, "CUDA spectral start")
+    return out.reshape(2, n).T.copy()
+
+
+def umap_spectral_start_csr(offsets, neighbors, weights, spectral_n_iter=50, seed=42, init_scale=float("nan")):
+    """The reference CPU spectral start of a symmetric CSR graph (umap_init_from_csr_graph,
+    R/fast_knn_umap.R:665-689) computed on the GPU: (n, 2) float64."""
+    off = np.ascontiguousarray(offsets, np.int32)
+    nb = np.ascontiguousarray(neighbors, np.int32)
+    w = np.ascontiguousarray(weights, np.float32)
+    n = off.size - 1
+    out = np.zeros(2 * n)
+    st = _lib.require_gpu().fastembedr_cuda_umap_spectral_init_csr(off.ctypes.data, nb.ctypes.data, w.ctypes.data, n,
+                                                                   int(spectral_n_iter), float(init_scale), int(seed),
+                                                                   out.ctypes.data)
+    _lib.check(st, "CUDA spectral start")
+    return out.reshape(2, n).T.copy()
+
+
+def umap_knn(indices, distances, init="spectral", n_components=2, seed=42, n_epochs=None, min_dist=0.01,
+             negative_sample_rate=5, learning_rate=1.0, repulsion_strength=1.0, backend="cuda",
+             spectral_n_iter=None, graph_mode="fuzzy", init_scale=float("nan")) -> UmapFit:
     """UMAP from a supplied KNN graph (R/fast_knn_umap.R:1444-1462 with the package policy of
     fast_knn_umap_config, :1008-1032: 200 epochs at n >= 10k else 500, min_dist 0.01, negative
-    rate 5, lr 1, repulsion 1). The initial layout is supplied by the caller (the reference feeds
-    the same CPU spectral initialisation to every backend)."""
+    rate 5, lr 1, repulsion 1). ``init``: "spectral" (default) computes the reference's CPU
+    spectral start (what umap_knn feeds every backend, R/umap_core_helpers.R:205-243) on the GPU
+    and runs graph -> start -> SGD in one call; "diffusion" is the fused GPU path of
+    knn_umap_cuda_fused_impl (src/embedding_cuda_impl.cpp:1716-1770) with its diffusion start and
+    the "fuzzy" or "binary" (unit weights) graph; an (n, 2) array is used as given.
+    ``spectral_n_iter`` defaults to the package size policy."""
     if backend != "cuda":
         raise ValueError("fastembedr_gb300 implements backend = 'cuda' only")
     if int(n_components) != 2:
@@ -445,6 +510,47 @@ def umap_knn(indices, distances, init, n_components=2, seed=42, n_epochs=None, m
     idx = np.asarray(indices)
     n, k = idx.shape
     epochs = (200 if n >= 10000 else 500) if n_epochs is None else int(n_epochs)
+    if isinstance(init, str) and init == "spectral":
+        rounds = umap_spectral_n_iter(n, k) if spectral_n_iter is None else int(spectral_n_iter)
+        out = np.zeros((n, 2), np.float32)
+        idx_cm, dist_cm = _colmajor(idx, np.int32), _colmajor(distances, np.float32)
+        st = _lib.require_gpu().fastembedr_cuda_umap_knn_spectral(
+            idx_cm.ctypes.data, dist_cm.ctypes.data, n, k, knn_index_offset(idx), epochs, int(negative_sample_rate),
+            float(learning_rate), float(min_dist), float(repulsion_strength), rounds, float(init_scale),
+            int(seed) & 0xFFFFFFFF, out.ctypes.data)
+        _lib.check(st, "CUDA UMAP")
+        config = dict(method="umap", backend="cuda", n=n, k=k, n_epochs=epochs, min_dist=float(min_dist),
+                      negative_sample_rate=int(negative_sample_rate), learning_rate=float(learning_rate),
+                      repulsion_strength=float(repulsion_strength), graph_mode="native_csr_graph",
+                      init_backend="cuda_spectral_csr", spectral_n_iter=rounds,
+                      graph_prep_backend="cuda_fuzzy_csr", optimizer_math="coo_atomic_edge_sampler_philox",
+                      seed=int(seed))
+        return UmapFit(out, config)
+    if isinstance(init, str):
+        if init != "diffusion":
+            raise ValueError("init must be an (n, 2) array, 'spectral' or 'diffusion'")
+        if graph_mode not in ("fuzzy", "binary"):
+            raise ValueError("graph_mode must be 'fuzzy' or 'binary'")
+        rounds = umap_spectral_n_iter(n, k) if spectral_n_iter is None else int(spectral_n_iter)
+        a, b = umap_ab_params(min_dist)
+        import torch
+
+        d_idx = torch.as_tensor(_colmajor(idx, np.int32), device="cuda")
+        d_dist = torch.as_tensor(_colmajor(distances, np.float32), device="cuda")
+        _settle(d_idx, d_dist)
+        out = np.zeros((n, 2), np.float32)
+        st = _lib.require_gpu().fastembedr_cuda_umap_from_device_knn_spectral_float(
+            d_idx.data_ptr(), d_dist.data_ptr(), n, k, epochs, int(negative_sample_rate), float(learning_rate),
+            float(a), float(b), float(repulsion_strength), rounds, int(seed) & 0xFFFFFFFF, knn_index_offset(idx), 0,
+            int(graph_mode == "binary"), out.ctypes.data)
+        _lib.check(st, "fused CUDA UMAP")
+        config = dict(method="umap", backend="cuda", n=n, k=k, n_epochs=epochs, min_dist=float(min_dist),
+                      negative_sample_rate=int(negative_sample_rate), learning_rate=float(learning_rate),
+                      repulsion_strength=float(repulsion_strength), graph_mode=graph_mode,
+                      init_backend="cuda_diffusion", spectral_n_iter=rounds,
+                      graph_prep_backend="cuda_fuzzy_csr", optimizer_math="coo_atomic_edge_sampler_philox",
+                      seed=int(seed))
+        return UmapFit(out, config)
     y0 = np.ascontiguousarray(init, np.float32)
     if y0.shape != (n, 2):
         raise ValueError("init row count must match the KNN graph")

@@ -15,16 +15,20 @@
 // t-SNE P; the epoch is one persistent grid-stride kernel over head-sorted COO edges with float2
 // vector atomics, negative samples drawn from per-(edge, epoch) Philox4x32-10 streams, and the
 // epoch counter lives on the device so a captured CUDA graph of 25 epochs replays unchanged.
+#include <algorithm>
 #include <cfloat>
 #include <climits>
 #include <cmath>
 #include <map>
 #include <memory>
+#include <type_traits>
+#include <vector>
 
 #include "../../include/fastembedr_cuda.h"
 #include "philox.cuh"
 #include "sort.cuh"
 #include "tsne.cuh"
+#include "umap_spectral.cuh"
 
 namespace fe {
 
@@ -627,12 +631,276 @@ __global__ void umap_offset_edges_kernel(const int* __restrict__ heads, const in
   }
 }
 
+// ---------------------------------------------------------------- diffusion start
+// The reference's GPU spectral start (fastembedr_cuda_spectral_init_from_knn,
+// src/embedding_cuda_kernels.cpp:4801-4960; kernels :1178-1335), stated for the CPU by the
+// reference as initialize_layout_csr_cuda_diffusion (src/fast_knn_umap.cpp:2597-2652): a hashed
+// start in [-1, 1]^2 (deterministic_unit, :522-530), whitened (normalize_cuda_like_init,
+// :2541-2595: centred, x scaled to unit norm, y made orthogonal to x and scaled to unit norm),
+// then rounds of weighted neighbour averaging over the fuzzy graph, whitened after each. Each
+// row's average is summed in CSR order in float with separately rounded products, as the CPU
+// statement does; the whitening moments are FP64 sums of exact products, reduced in a fixed
+// block order, and the whitening arithmetic is FP64 without contraction.
+constexpr int kInitThreads = 256;
+constexpr int kInitMomentBlocks = 1024;
+
+__device__ __forceinline__ unsigned init_hash(unsigned x) {
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
+  return x;
+}
+
+__device__ __forceinline__ float init_unit(unsigned seed, int row, int col) {
+  unsigned x = seed;
+  x ^= (unsigned)(row + 1) * 0x9e3779b9u;
+  x ^= (unsigned)(col + 1) * 0x85ebca6bu;
+  return __fsub_rn(__fdiv_rn((float)(init_hash(x) & 0x00ffffffu), 8388607.5f), 1.0f);
+}
+
+__global__ void diffusion_start_kernel(float2* __restrict__ y, int n, unsigned seed) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    y[i] = make_float2(init_unit(seed, i, 0), init_unit(seed, i, 1));
+}
+
+__global__ void diffusion_round_kernel(const int* __restrict__ offsets, const int* __restrict__ neighbors,
+                                       const float* __restrict__ weights, int n, const float2* __restrict__ cur,
+                                       float2* __restrict__ next) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float sx = 0.0f, sy = 0.0f, sw = 0.0f;
+    for (int p = offsets[i]; p < offsets[i + 1]; ++p) {
+      const int nb = neighbors[p];
+      const float w = weights[p];
+      if (nb < 0 || nb >= n || nb == i || !(w > 0.0f) || !isfinite(w)) continue;
+      const float2 c = cur[nb];
+      sx = __fadd_rn(sx, __fmul_rn(w, c.x));
+      sy = __fadd_rn(sy, __fmul_rn(w, c.y));
+      sw = __fadd_rn(sw, w);
+    }
+    next[i] = sw <= 0.0f ? cur[i] : make_float2(__fdiv_rn(sx, sw), __fdiv_rn(sy, sw));
+  }
+}
+
+// Block partial moments (sum x, sum y, sum x^2, sum xy, sum y^2) of the layout.
+__global__ void __launch_bounds__(kInitThreads)
+whiten_moments_kernel(const float2* __restrict__ y, int n, double* __restrict__ partial) {
+  __shared__ double sm[5][kInitThreads];
+  double a[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double x = y[i].x, v = y[i].y;
+    a[0] += x;
+    a[1] += v;
+    a[2] += x * x;  // products of floats are exact in double
+    a[3] += x * v;
+    a[4] += v * v;
+  }
+#pragma unroll
+  for (int c = 0; c < 5; ++c) sm[c][threadIdx.x] = a[c];
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w)
+#pragma unroll
+      for (int c = 0; c < 5; ++c) sm[c][threadIdx.x] += sm[c][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x < 5) partial[blockIdx.x * 5 + threadIdx.x] = sm[threadIdx.x][0];
+}
+
+// stats = (mean_x, mean_y, 1 / |x|, projection of y on x, 1 / |y residual|), one thread.
+__global__ void whiten_finish_kernel(const double* __restrict__ partial, int blocks, int n, double* __restrict__ st) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double m[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int b = 0; b < blocks; ++b)
+    for (int c = 0; c < 5; ++c) m[c] += partial[b * 5 + c];
+  const double dn = (double)n;
+  const double xss = fmax(__dsub_rn(m[2], __ddiv_rn(__dmul_rn(m[0], m[0]), dn)), 1.0e-24);
+  const double yss = fmax(__dsub_rn(m[4], __ddiv_rn(__dmul_rn(m[1], m[1]), dn)), 1.0e-24);
+  const double xy = __dsub_rn(m[3], __ddiv_rn(__dmul_rn(m[0], m[1]), dn));
+  const double nx = __dsqrt_rn(xss);
+  const double proj = __ddiv_rn(xy, nx);
+  st[0] = __ddiv_rn(m[0], dn);
+  st[1] = __ddiv_rn(m[1], dn);
+  st[2] = __ddiv_rn(1.0, nx);
+  st[3] = proj;
+  st[4] = __ddiv_rn(1.0, __dsqrt_rn(fmax(__dsub_rn(yss, __dmul_rn(proj, proj)), 1.0e-24)));
+}
+
+__global__ void whiten_apply_kernel(float2* __restrict__ y, int n, const double* __restrict__ st) {
+  const double mx = st[0], my = st[1], inx = st[2], proj = st[3], iny = st[4];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float2 v = y[i];
+    const double x = __dmul_rn(__dsub_rn((double)v.x, mx), inx);
+    const double r = __dmul_rn(__dsub_rn(__dsub_rn((double)v.y, my), __dmul_rn(proj, x)), iny);
+    y[i] = make_float2((float)x, (float)r);
+  }
+}
+
+__global__ void umap_double_to_float_kernel(const double* __restrict__ in, float* __restrict__ out, long long m) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < m; t += (long long)gridDim.x * blockDim.x)
+    out[t] = (float)in[t];
+}
+
+// Unit weights and sampling periods on the fuzzy graph's structure (the binary graph mode of
+// the reference's fused path, binary_graph_weights_kernel, src/embedding_cuda_kernels.cpp:1115).
+__global__ void umap_binary_weights_kernel(float* __restrict__ weights, float* __restrict__ eps, long long nnz) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nnz; t += (long long)gridDim.x * blockDim.x) {
+    weights[t] = 1.0f;
+    eps[t] = 1.0f;
+  }
+}
+
+void whiten(float2* y, int n, double* partial, double* stats, cudaStream_t s) {
+  const int blocks = std::max(1, std::min(ceil_div(n, kInitThreads), kInitMomentBlocks));
+  whiten_moments_kernel<<<blocks, kInitThreads, 0, s>>>(y, n, partial);
+  FE_LAUNCH("whiten_moments_kernel");
+  whiten_finish_kernel<<<1, 32, 0, s>>>(partial, blocks, n, stats);
+  FE_LAUNCH("whiten_finish_kernel");
+  whiten_apply_kernel<<<std::max(1, std::min(ceil_div(n, kInitThreads), sm_count() * 8)), kInitThreads, 0, s>>>(
+      y, n, stats);
+  FE_LAUNCH("whiten_apply_kernel");
+}
+
+// Diffusion start over g into y (n float2); 4 launches per round.
+void umap_diffusion_start(const UmapGraph& g, int n_iter, unsigned seed, float2* y, cudaStream_t s) {
+  const int n = g.n;
+  float2* tmp = nullptr;
+  double* partial = nullptr;
+  double* stats = nullptr;
+  Arena w;
+  w.reserve(&tmp, n);
+  w.reserve(&partial, 5 * kInitMomentBlocks);
+  w.reserve(&stats, 5);
+  w.commit("UMAP diffusion start");
+  const int blocks = std::max(1, std::min(ceil_div(n, kInitThreads), sm_count() * 8));
+  diffusion_start_kernel<<<blocks, kInitThreads, 0, s>>>(y, n, seed);
+  FE_LAUNCH("diffusion_start_kernel");
+  whiten(y, n, partial, stats, s);
+  float2* cur = y;
+  float2* nxt = tmp;
+  for (int it = 0; it < n_iter; ++it) {
+    diffusion_round_kernel<<<blocks, kInitThreads, 0, s>>>(g.offsets, g.neighbors, g.weights, n, cur, nxt);
+    FE_LAUNCH("diffusion_round_kernel");
+    whiten(nxt, n, partial, stats, s);
+    std::swap(cur, nxt);
+  }
+  if (cur != y) FE_CUDA(cudaMemcpyAsync(y, cur, sizeof(float2) * n, cudaMemcpyDeviceToDevice, s));
+  FE_CUDA(cudaStreamSynchronize(s));
+}
+
+// KNN on the device (float distances) -> fuzzy graph (optionally unit-weighted) -> diffusion
+// start -> n_epochs of SGD; result row-major n x 2 floats to the host.
+void umap_spectral_job(const int* d_idx, const float* d_dist, int n, int k, int n_epochs, int nsr, float lr, float a,
+                       float b, float rep, int spectral_n_iter, unsigned seed, int offset, bool binary, float* out) {
+  UmapJob job;
+  job.alloc(n);
+  cudaStream_t s = job.stream.s;
+  order_after_legacy_stream(s);  // d_idx / d_dist may be the caller's device buffers
+  validate_knn(d_idx, d_dist, n, k, offset, s);
+  UmapGraph g;
+  umap_build_graph(d_idx, d_dist, n, k, offset, g, s);
+  if (binary) {
+    umap_binary_weights_kernel<<<std::max(1, std::min(ceil_div(g.nnz, 256), sm_count() * 8)), 256, 0, s>>>(
+        g.weights, g.eps, g.nnz);
+    FE_LAUNCH("umap_binary_weights_kernel");
+  }
+  umap_diffusion_start(g, spectral_n_iter, seed, job.y, s);
+  const UmapParams p{n, n_epochs, nsr, seed, lr, a, b, rep};
+  job.run(g.heads, g.neighbors, g.eps, g.nnz, p);
+  FE_CUDA(cudaMemcpyAsync(out, job.y, sizeof(float) * 2 * (std::size_t)n, cudaMemcpyDeviceToHost, s));
+  FE_CUDA(cudaStreamSynchronize(s));
+}
+
+__global__ void umap_start_to_layout_kernel(const double* __restrict__ emb, int n, float2* __restrict__ y) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    y[i] = make_float2((float)emb[i], (float)emb[(long long)n + i]);
+}
+
+// KNN on the device -> fuzzy graph -> the reference CPU spectral start (block subspace
+// iteration) -> optionally n_epochs of SGD from it. emb_out (host, column-major n x 2 doubles)
+// receives the start, y_out (host, row-major n x 2 floats) the optimised layout; either may be
+// null (n_epochs must be 0 when y_out is).
+void umap_knn_spectral_job(const int* d_idx, const float* d_dist, int n, int k, int offset, int n_epochs, int nsr,
+                           float lr, float min_dist, float rep, int spectral_n_iter, double init_scale,
+                           unsigned seed, double* emb_out, float* y_out) {
+  UmapJob job;
+  job.alloc(n);
+  cudaStream_t s = job.stream.s;
+  order_after_legacy_stream(s);
+  validate_knn(d_idx, d_dist, n, k, offset, s);
+  UmapGraph g;
+  umap_build_graph(d_idx, d_dist, n, k, offset, g, s);
+  double* emb = nullptr;
+  Arena a;
+  a.reserve(&emb, 2 * (std::size_t)n);
+  a.commit("UMAP spectral start output");
+  umap_spectral_start(g.offsets, g.neighbors, g.weights, n, g.nnz, spectral_n_iter, init_scale, (int)seed, emb, s);
+  if (emb_out) FE_CUDA(cudaMemcpyAsync(emb_out, emb, sizeof(double) * 2 * (std::size_t)n, cudaMemcpyDeviceToHost, s));
+  if (y_out) {
+    umap_start_to_layout_kernel<<<std::max(1, std::min(ceil_div(n, 256), sm_count() * 8)), 256, 0, s>>>(emb, n,
+                                                                                                      job.y);
+    FE_LAUNCH("umap_start_to_layout_kernel");
+    if (n_epochs > 0) {
+      double av = 0.0, bv = 0.0;
+      umap_ab_params(1.0, min_dist, &av, &bv);
+      const UmapParams p{n, n_epochs, nsr, seed, lr, (float)av, (float)bv, rep};
+      job.run(g.heads, g.neighbors, g.eps, g.nnz, p);
+    }
+    FE_CUDA(cudaMemcpyAsync(y_out, job.y, sizeof(float) * 2 * (std::size_t)n, cudaMemcpyDeviceToHost, s));
+  }
+  FE_CUDA(cudaStreamSynchronize(s));
+}
+
+void check_spectral_job(int n, int k, int n_epochs, int nsr, float lr, int spectral_n_iter, int optimizer_mode) {
+  if (n < 2 || k < 1 || k > 256 || n_epochs < 1 || nsr < 0 || !(lr > 0.0f) || spectral_n_iter < 1)
+    throw Error("invalid fused CUDA UMAP dimensions or parameters");
+  if (optimizer_mode != 0)
+    throw Error("optimizer_mode 1 (batched delta) is not provided; the package policy uses mode 0");
+}
+
 void check_umap_params(int n, long long n_edges, int n_epochs, int nsr, float lr, float rep) {
   if (n < 2 || n_edges < 1 || n_epochs < 1 || nsr < 0 || !(lr > 0.0f) || !(rep > 0.0f))
     throw Error("invalid CUDA COO UMAP optimization parameters");
 }
 
 }  // namespace fe
+
+namespace {
+template <typename DistT>
+int umap_spectral_host(const int* indices, const DistT* distances, int n, int k, int n_epochs, int nsr, float lr,
+                       float a, float b, float rep, int spectral_n_iter, unsigned seed, int index_offset,
+                       int optimizer_mode, float* out) {
+  return fe::guarded([&] {
+    if (!indices || !distances || !out) throw fe::Error("null host pointer");
+    fe::check_spectral_job(n, k, n_epochs, nsr, lr, spectral_n_iter, optimizer_mode);
+    fe::Stream st;
+    cudaStream_t s = st.s;
+    const std::size_t items = (std::size_t)n * k;
+    int* d_idx = nullptr;
+    DistT* d_raw = nullptr;
+    float* d_dist = nullptr;
+    fe::Arena in;
+    in.reserve(&d_idx, items);
+    if (!std::is_same<DistT, float>::value) in.reserve(&d_raw, items);
+    in.reserve(&d_dist, items);
+    in.commit("fused CUDA UMAP input");
+    FE_CUDA(cudaMemcpyAsync(d_idx, indices, sizeof(int) * items, cudaMemcpyHostToDevice, s));
+    if constexpr (std::is_same<DistT, float>::value) {
+      FE_CUDA(cudaMemcpyAsync(d_dist, distances, sizeof(float) * items, cudaMemcpyHostToDevice, s));
+    } else {
+      FE_CUDA(cudaMemcpyAsync(d_raw, distances, sizeof(double) * items, cudaMemcpyHostToDevice, s));
+      fe::umap_double_to_float_kernel<<<std::max(1, std::min(fe::ceil_div((long long)items, 256),
+                                                              fe::sm_count() * 8)),
+                                        256, 0, s>>>(d_raw, d_dist, (long long)items);
+      FE_LAUNCH("umap_double_to_float_kernel");
+    }
+    FE_CUDA(cudaStreamSynchronize(s));
+    fe::umap_spectral_job(d_idx, d_dist, n, k, n_epochs, nsr, lr, a, b, rep, spectral_n_iter, seed, index_offset,
+                          false, out);
+  });
+}
+}  // namespace
 
 extern "C" {
 
@@ -832,6 +1100,183 @@ int fastembedr_cuda_umap_batch_from_knn(int n_instances, const int* sizes, const
     cudaEventElapsedTime(&ms, ev[0], ev[1]);
     for (auto& e : ev) cudaEventDestroy(e);
     if (sgd_ms) *sgd_ms = ms;
+  });
+}
+
+void fastembedr_umap_find_ab_params(double spread, double min_dist, double* a, double* b) {
+  double av = 0.0, bv = 0.0;
+  fe::umap_ab_params(spread, min_dist, &av, &bv);
+  if (a) *a = av;
+  if (b) *b = bv;
+}
+
+int fastembedr_cuda_umap_spectral_init_from_knn(const int* indices, const float* distances, int n, int k,
+                                                int index_offset, int spectral_n_iter, double init_scale, int seed,
+                                                double* out) {
+  return fe::guarded([&] {
+    if (!indices || !distances || !out) throw fe::Error("null host pointer");
+    if (n < 2 || k < 1 || spectral_n_iter < 1) throw fe::Error("invalid spectral initialization parameters");
+    fe::Stream st;
+    const std::size_t items = (std::size_t)n * k;
+    int* d_idx = nullptr;
+    float* d_dist = nullptr;
+    fe::Arena a;
+    a.reserve(&d_idx, items);
+    a.reserve(&d_dist, items);
+    a.commit("UMAP spectral start input");
+    FE_CUDA(cudaMemcpyAsync(d_idx, indices, sizeof(int) * items, cudaMemcpyHostToDevice, st.s));
+    FE_CUDA(cudaMemcpyAsync(d_dist, distances, sizeof(float) * items, cudaMemcpyHostToDevice, st.s));
+    FE_CUDA(cudaStreamSynchronize(st.s));
+    fe::umap_knn_spectral_job(d_idx, d_dist, n, k, index_offset, 0, 0, 1.0f, 0.01f, 1.0f, spectral_n_iter,
+                              init_scale, (unsigned)seed, out, nullptr);
+  });
+}
+
+int fastembedr_cuda_umap_spectral_init_csr(const int* offsets, const int* neighbors, const float* weights, int n,
+                                           int spectral_n_iter, double init_scale, int seed, double* out) {
+  return fe::guarded([&] {
+    if (!offsets || !neighbors || !weights || !out) throw fe::Error("null host pointer");
+    if (n < 1 || spectral_n_iter < 1) throw fe::Error("invalid spectral initialization parameters");
+    // validate_csr_inputs (src/fast_knn_umap.cpp:747-785), plus the symmetry the GPU start relies on
+    if (offsets[0] != 0) throw fe::Error("First CSR offset must be zero");
+    for (int i = 1; i <= n; ++i)
+      if (offsets[i] < offsets[i - 1]) throw fe::Error("CSR offsets must be non-decreasing");
+    const long long nnz = offsets[n];
+    int lo = INT_MAX, hi = INT_MIN;
+    for (long long p = 0; p < nnz; ++p) {
+      lo = std::min(lo, neighbors[p]);
+      hi = std::max(hi, neighbors[p]);
+    }
+    const int off = (nnz > 0 && lo >= 1 && hi <= n) ? 1 : 0;
+    std::vector<int> nb0((std::size_t)std::max<long long>(nnz, 1));
+    for (int r = 0; r < n; ++r) {
+      int last = -1;
+      for (int p = offsets[r]; p < offsets[r + 1]; ++p) {
+        const int j = neighbors[p] - off;
+        if (j < 0 || j >= n) throw fe::Error("CSR neighbor index out of range");
+        if (j == r) throw fe::Error("CSR graph must not contain self-neighbors");
+        if (j < last) throw fe::Error("CSR neighbors must be sorted within each row");
+        last = j;
+        if (!std::isfinite(weights[p]) || !(weights[p] > 0.0f)) throw fe::Error("CSR weights must be positive and finite");
+        nb0[p] = j;
+      }
+    }
+    for (int r = 0; r < n; ++r)
+      for (int p = offsets[r]; p < offsets[r + 1]; ++p) {
+        const int j = nb0[p];
+        const int* b = nb0.data() + offsets[j];
+        const int* e = nb0.data() + offsets[j + 1];
+        const int* it = std::lower_bound(b, e, r);
+        if (it == e || *it != r || weights[offsets[j] + (it - b)] != weights[p])
+          throw fe::Error("the GPU spectral start needs a symmetric CSR graph (w_ij == w_ji)");
+      }
+    fe::Stream st;
+    cudaStream_t s = st.s;
+    int *d_off = nullptr, *d_nb = nullptr;
+    float* d_w = nullptr;
+    double* d_out = nullptr;
+    fe::Arena a;
+    a.reserve(&d_off, n + 1);
+    a.reserve(&d_nb, (std::size_t)std::max<long long>(nnz, 1));
+    a.reserve(&d_w, (std::size_t)std::max<long long>(nnz, 1));
+    a.reserve(&d_out, 2 * (std::size_t)n);
+    a.commit("UMAP spectral start (CSR)");
+    FE_CUDA(cudaMemcpyAsync(d_off, offsets, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s));
+    if (nnz > 0) {
+      FE_CUDA(cudaMemcpyAsync(d_nb, nb0.data(), sizeof(int) * nnz, cudaMemcpyHostToDevice, s));
+      FE_CUDA(cudaMemcpyAsync(d_w, weights, sizeof(float) * nnz, cudaMemcpyHostToDevice, s));
+    }
+    fe::umap_spectral_start(d_off, d_nb, d_w, n, nnz, spectral_n_iter, init_scale, seed, d_out, s);
+    FE_CUDA(cudaMemcpyAsync(out, d_out, sizeof(double) * 2 * (std::size_t)n, cudaMemcpyDeviceToHost, s));
+    FE_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int fastembedr_cuda_umap_knn_spectral(const int* indices, const float* distances, int n, int k, int index_offset,
+                                      int n_epochs, int negative_sample_rate, float learning_rate, float min_dist,
+                                      float repulsion_strength, int spectral_n_iter, double init_scale,
+                                      unsigned int seed, float* out) {
+  return fe::guarded([&] {
+    if (!indices || !distances || !out) throw fe::Error("null host pointer");
+    if (n < 2 || k < 1 || n_epochs < 1 || negative_sample_rate < 0 || !(learning_rate > 0.0f) || min_dist < 0.0f ||
+        !(repulsion_strength > 0.0f) || spectral_n_iter < 1)
+      throw fe::Error("invalid CUDA UMAP parameters");
+    fe::Stream st;
+    const std::size_t items = (std::size_t)n * k;
+    int* d_idx = nullptr;
+    float* d_dist = nullptr;
+    fe::Arena a;
+    a.reserve(&d_idx, items);
+    a.reserve(&d_dist, items);
+    a.commit("UMAP input");
+    FE_CUDA(cudaMemcpyAsync(d_idx, indices, sizeof(int) * items, cudaMemcpyHostToDevice, st.s));
+    FE_CUDA(cudaMemcpyAsync(d_dist, distances, sizeof(float) * items, cudaMemcpyHostToDevice, st.s));
+    FE_CUDA(cudaStreamSynchronize(st.s));
+    fe::umap_knn_spectral_job(d_idx, d_dist, n, k, index_offset, n_epochs, negative_sample_rate, learning_rate,
+                              min_dist, repulsion_strength, spectral_n_iter, init_scale, seed, nullptr, out);
+  });
+}
+
+int fastembedr_cuda_spectral_init_from_knn(const int* indices, const double* distances, int n, int k,
+                                           int spectral_n_iter, unsigned int seed, int index_offset, float* out) {
+  return fe::guarded([&] {
+    if (!indices || !distances || !out) throw fe::Error("null host pointer");
+    if (n < 2 || k < 1 || k > 256 || spectral_n_iter < 1)
+      throw fe::Error("invalid spectral initialization dimensions or parameters");
+    fe::Stream st;
+    cudaStream_t s = st.s;
+    const std::size_t items = (std::size_t)n * k;
+    int* d_idx = nullptr;
+    double* d_dd = nullptr;
+    float* d_dist = nullptr;
+    float2* d_y = nullptr;
+    fe::Arena a;
+    a.reserve(&d_idx, items);
+    a.reserve(&d_dd, items);
+    a.reserve(&d_dist, items);
+    a.reserve(&d_y, n);
+    a.commit("CUDA spectral initialization");
+    FE_CUDA(cudaMemcpyAsync(d_idx, indices, sizeof(int) * items, cudaMemcpyHostToDevice, s));
+    FE_CUDA(cudaMemcpyAsync(d_dd, distances, sizeof(double) * items, cudaMemcpyHostToDevice, s));
+    fe::umap_double_to_float_kernel<<<std::max(1, std::min(fe::ceil_div((long long)items, 256), fe::sm_count() * 8)),
+                                      256, 0, s>>>(d_dd, d_dist, (long long)items);
+    FE_LAUNCH("umap_double_to_float_kernel");
+    fe::validate_knn(d_idx, d_dist, n, k, index_offset, s);
+    fe::UmapGraph g;
+    fe::umap_build_graph(d_idx, d_dist, n, k, index_offset, g, s);
+    fe::umap_diffusion_start(g, spectral_n_iter, seed, d_y, s);
+    FE_CUDA(cudaMemcpyAsync(out, d_y, sizeof(float) * 2 * (std::size_t)n, cudaMemcpyDeviceToHost, s));
+    FE_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int fastembedr_cuda_umap_from_knn_spectral(const int* indices, const double* distances, int n, int k, int n_epochs,
+                                           int negative_sample_rate, float learning_rate, float a, float b,
+                                           float repulsion_strength, int spectral_n_iter, unsigned int seed,
+                                           int index_offset, int optimizer_mode, float* out) {
+  return umap_spectral_host(indices, distances, n, k, n_epochs, negative_sample_rate, learning_rate, a, b,
+                            repulsion_strength, spectral_n_iter, seed, index_offset, optimizer_mode, out);
+}
+
+int fastembedr_cuda_umap_from_knn_spectral_float(const int* indices, const float* distances, int n, int k,
+                                                 int n_epochs, int negative_sample_rate, float learning_rate, float a,
+                                                 float b, float repulsion_strength, int spectral_n_iter,
+                                                 unsigned int seed, int index_offset, int optimizer_mode, float* out) {
+  return umap_spectral_host(indices, distances, n, k, n_epochs, negative_sample_rate, learning_rate, a, b,
+                            repulsion_strength, spectral_n_iter, seed, index_offset, optimizer_mode, out);
+}
+
+int fastembedr_cuda_umap_from_device_knn_spectral_float(const int* device_indices, const float* device_distances,
+                                                        int n, int k, int n_epochs, int negative_sample_rate,
+                                                        float learning_rate, float a, float b,
+                                                        float repulsion_strength, int spectral_n_iter,
+                                                        unsigned int seed, int index_offset, int optimizer_mode,
+                                                        int binary_graph, float* out) {
+  return fe::guarded([&] {
+    if (!device_indices || !device_distances || !out) throw fe::Error("null device pointer");
+    fe::check_spectral_job(n, k, n_epochs, negative_sample_rate, learning_rate, spectral_n_iter, optimizer_mode);
+    fe::umap_spectral_job(device_indices, device_distances, n, k, n_epochs, negative_sample_rate, learning_rate, a,
+                          b, repulsion_strength, spectral_n_iter, seed, index_offset, binary_graph != 0, out);
   });
 }
 

@@ -1,0 +1,477 @@
+// Spectral start of UMAP on the GPU.
+//
+// Restates initialize_layout_csr (src/fast_knn_umap.cpp:2231-2528), as optimize_layout_csr
+// (:3088-3205) calls it for spectral_knn_init(backend = "cpu") / umap_init: the symmetric
+// normalised adjacency D^-1/2 W D^-1/2 of the fuzzy graph, a block of 8 vectors drawn from the
+// reference's std::mt19937 / normal(0, 1e-4) x 1e4 stream, spectral_n_iter rounds of
+// multiply + modified Gram-Schmidt against the trivial eigenvector sqrt(deg) / |sqrt(deg)| and
+// the earlier columns, a Rayleigh-Ritz step (the 8 x 8 projected matrix, diagonalised by the
+// reference's largest-off-diagonal Jacobi rotations), the two leading Ritz vectors centred,
+// scaled to max |y| = 10 and jittered by the stream's normal(0, 1e-4) draws
+// (scale_embedding_max_abs_and_jitter, :2705-2730), then the optional scale_embedding_sdev
+// (:2681-2703).
+//
+// The random draws are made on the host in the reference's order (the column redraw of a
+// vanishing Gram-Schmidt column included) and uploaded; every arithmetic step runs on the GPU in
+// FP64 with the reference's operation order and no contraction (__d*_rn). Sums over points are
+// reduced in a fixed block order, so results are deterministic and differ from the sequential
+// CPU sums by rounding only.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <random>
+#include <vector>
+
+#include "umap_spectral.cuh"
+
+namespace fe {
+namespace {
+
+constexpr int kSpThreads = 256;
+constexpr int kSpMaxBlocks = 1024;
+constexpr int kSpBlock = 8;                           // block size of the reference for 2 components
+constexpr int kSpPairs = kSpBlock * (kSpBlock + 1) / 2;  // upper triangle of the projected matrix
+
+int sp_blocks(int n) { return std::max(1, std::min(ceil_div(n, kSpThreads), kSpMaxBlocks)); }
+
+// Fixed-order sum of `count` partials, valid in every thread of the block (all threads call).
+__device__ double sum_partials(const double* __restrict__ part, int count) {
+  __shared__ double s_total;
+  if (threadIdx.x < 32) {
+    double s = 0.0;
+    for (int b = threadIdx.x; b < count; b += 32) s = __dadd_rn(s, part[b]);
+    s = warp_sum(s);
+    if (threadIdx.x == 0) s_total = s;
+  }
+  __syncthreads();
+  const double r = s_total;
+  __syncthreads();
+  return r;
+}
+
+// Block sum of v into part[blockIdx.x] (fixed order: warp trees, then warps in order).
+__device__ void block_partial(double v, double* __restrict__ part) {
+  __shared__ double s_w[kSpThreads / 32];
+  v = warp_sum(v);
+  if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t = __dadd_rn(t, s_w[w]);
+    part[blockIdx.x] = t;
+  }
+}
+
+// deg[r] = float(sum of row r's weights in double)
+__global__ void sp_degree_kernel(const int* __restrict__ offsets, const float* __restrict__ w, int n,
+                                 float* __restrict__ deg) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int p = offsets[r]; p < offsets[r + 1]; ++p) s = __dadd_rn(s, (double)w[p]);
+    deg[r] = (float)s;
+  }
+}
+
+// nw[p] = float(w / sqrt(max(deg_r deg_j, 1e-24))); triv[r] = sqrt(max(deg_r, 0)); partials of
+// sum triv^2. One thread per row, grid-stride with a fixed row-to-block assignment.
+__global__ void __launch_bounds__(kSpThreads)
+sp_adjacency_kernel(const int* __restrict__ offsets, const int* __restrict__ nb, const float* __restrict__ w,
+                    const float* __restrict__ deg, int n, float* __restrict__ nw, double* __restrict__ triv,
+                    double* __restrict__ part) {
+  double acc = 0.0;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    const double dr = (double)deg[r];
+    for (int p = offsets[r]; p < offsets[r + 1]; ++p) {
+      const double den = __dsqrt_rn(fmax(__dmul_rn(dr, (double)deg[nb[p]]), 1e-24));
+      nw[p] = (float)__ddiv_rn((double)w[p], den);
+    }
+    const double t = __dsqrt_rn(fmax(dr, 0.0));
+    triv[r] = t;
+    acc = __dadd_rn(acc, __dmul_rn(t, t));
+  }
+  block_partial(acc, part);
+}
+
+__global__ void sp_normalise_trivial_kernel(double* __restrict__ triv, int n, const double* __restrict__ part,
+                                            int nparts) {
+  const double nrm = __dsqrt_rn(fmax(sum_partials(part, nparts), 1e-12));
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
+    triv[r] = __ddiv_rn(triv[r], nrm);
+}
+
+// Gram-Schmidt steps. A column whose norm vanished sets *flag to its index; the later steps of
+// the same pass see the flag and do nothing, and the host redraws that column and resumes.
+__global__ void __launch_bounds__(kSpThreads)
+gs_dot_kernel(const double* __restrict__ a, const double* __restrict__ b, int n, double* __restrict__ part,
+              const int* __restrict__ flag) {
+  if (*flag >= 0) return;
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    acc = __dadd_rn(acc, __dmul_rn(a[i], b[i]));
+  block_partial(acc, part);
+}
+
+// qc -= (sum of part_in) * u; then partials of sum qc * v (v may be qc)
+__global__ void __launch_bounds__(kSpThreads)
+gs_sub_dot_kernel(double* qc, const double* __restrict__ u, const double* __restrict__ part_in, int nparts,
+                  const double* v, int n, double* __restrict__ part_out, const int* __restrict__ flag) {
+  if (*flag >= 0) return;
+  const double d = sum_partials(part_in, nparts);
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double x = __dsub_rn(qc[i], __dmul_rn(d, u[i]));
+    qc[i] = x;
+    acc = __dadd_rn(acc, __dmul_rn(x, v == qc ? x : v[i]));
+  }
+  block_partial(acc, part_out);
+}
+
+__global__ void gs_scale_kernel(double* __restrict__ qc, const double* __restrict__ part_in, int nparts, int n,
+                                int col, int* __restrict__ flag) {
+  if (*flag >= 0) return;
+  const double nrm = __dsqrt_rn(sum_partials(part_in, nparts));
+  if (nrm < 1e-10) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *flag = col;
+    return;
+  }
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    qc[i] = __ddiv_rn(qc[i], nrm);
+}
+
+// y[:, c] = A x[:, c] for the B columns; one thread per row, neighbours in CSR order.
+__global__ void sp_multiply_kernel(const int* __restrict__ offsets, const int* __restrict__ nb,
+                                   const float* __restrict__ nw, int n, int B, const double* __restrict__ x,
+                                   double* __restrict__ y) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    double s[kSpBlock];
+#pragma unroll
+    for (int c = 0; c < kSpBlock; ++c) s[c] = 0.0;
+    for (int p = offsets[r]; p < offsets[r + 1]; ++p) {
+      const double w = (double)nw[p];
+      const long long j = nb[p];
+#pragma unroll
+      for (int c = 0; c < kSpBlock; ++c)
+        if (c < B) s[c] = __dadd_rn(s[c], __dmul_rn(w, x[(long long)c * n + j]));
+    }
+#pragma unroll
+    for (int c = 0; c < kSpBlock; ++c)
+      if (c < B) y[(long long)c * n + r] = s[c];
+  }
+}
+
+// Block partials of q[:, a] . z[:, b] for a <= b (pair index in row-major upper-triangle order).
+__global__ void __launch_bounds__(kSpThreads)
+sp_project_kernel(const double* __restrict__ q, const double* __restrict__ z, int n, int B,
+                  double* __restrict__ part) {
+  __shared__ double s_w[kSpThreads / 32][kSpPairs];
+  double acc[kSpPairs];
+#pragma unroll
+  for (int t = 0; t < kSpPairs; ++t) acc[t] = 0.0;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    int t = 0;
+#pragma unroll
+    for (int a = 0; a < kSpBlock; ++a) {
+      const double qv = a < B ? q[(long long)a * n + r] : 0.0;
+#pragma unroll
+      for (int b = a; b < kSpBlock; ++b, ++t)
+        if (b < B) acc[t] = __dadd_rn(acc[t], __dmul_rn(qv, z[(long long)b * n + r]));
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < kSpPairs; ++t) {
+    const double v = warp_sum(acc[t]);
+    if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5][t] = v;
+  }
+  __syncthreads();
+  if ((int)threadIdx.x < kSpPairs) {
+    double s = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s = __dadd_rn(s, s_w[w][threadIdx.x]);
+    part[(long long)blockIdx.x * kSpPairs + threadIdx.x] = s;
+  }
+}
+
+// One thread: the projected matrix from the partials, the reference's Jacobi rotations (at most
+// 80, each on the largest off-diagonal entry), Ritz values sorted descending; coef[c * 8 + b]
+// = component c's coefficients on the basis.
+__global__ void sp_ritz_kernel(const double* __restrict__ part, int nparts, int B, double* __restrict__ coef) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double P[kSpBlock][kSpBlock], V[kSpBlock][kSpBlock];
+  int t = 0;
+  for (int a = 0; a < kSpBlock; ++a)
+    for (int b = a; b < kSpBlock; ++b, ++t) {
+      double s = 0.0;
+      for (int k = 0; k < nparts; ++k) s = __dadd_rn(s, part[(long long)k * kSpPairs + t]);
+      P[a][b] = s;
+      P[b][a] = s;
+    }
+  for (int i = 0; i < kSpBlock; ++i)
+    for (int j = 0; j < kSpBlock; ++j) V[i][j] = i == j ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 80; ++sweep) {
+    int p = 0, q = 1;
+    double mx = 0.0;
+    for (int i = 0; i < B; ++i)
+      for (int j = i + 1; j < B; ++j) {
+        const double v = fabs(P[i][j]);
+        if (v > mx) {
+          mx = v;
+          p = i;
+          q = j;
+        }
+      }
+    if (mx < 1e-10) break;
+    const double app = P[p][p], aqq = P[q][q], apq = P[p][q];
+    const double tau = __ddiv_rn(__dsub_rn(aqq, app), __dmul_rn(2.0, apq));
+    const double tt = __ddiv_rn(tau >= 0.0 ? 1.0 : -1.0,
+                                __dadd_rn(fabs(tau), __dsqrt_rn(__dadd_rn(1.0, __dmul_rn(tau, tau)))));
+    const double cs = __ddiv_rn(1.0, __dsqrt_rn(__dadd_rn(1.0, __dmul_rn(tt, tt))));
+    const double sn = __dmul_rn(tt, cs);
+    for (int k = 0; k < B; ++k) {
+      if (k == p || k == q) continue;
+      const double akp = P[k][p], akq = P[k][q];
+      P[k][p] = __dsub_rn(__dmul_rn(cs, akp), __dmul_rn(sn, akq));
+      P[p][k] = P[k][p];
+      P[k][q] = __dadd_rn(__dmul_rn(sn, akp), __dmul_rn(cs, akq));
+      P[q][k] = P[k][q];
+    }
+    const double cc = __dmul_rn(cs, cs), ss = __dmul_rn(sn, sn);
+    const double cross = __dmul_rn(__dmul_rn(__dmul_rn(2.0, sn), cs), apq);
+    P[p][p] = __dadd_rn(__dsub_rn(__dmul_rn(cc, app), cross), __dmul_rn(ss, aqq));
+    P[q][q] = __dadd_rn(__dadd_rn(__dmul_rn(ss, app), cross), __dmul_rn(cc, aqq));
+    P[p][q] = 0.0;
+    P[q][p] = 0.0;
+    for (int k = 0; k < B; ++k) {
+      const double vp = V[k][p], vq = V[k][q];
+      V[k][p] = __dsub_rn(__dmul_rn(cs, vp), __dmul_rn(sn, vq));
+      V[k][q] = __dadd_rn(__dmul_rn(sn, vp), __dmul_rn(cs, vq));
+    }
+  }
+  int order[kSpBlock];
+  for (int i = 0; i < B; ++i) {
+    int j = i;
+    while (j > 0 && P[i][i] > P[order[j - 1]][order[j - 1]]) {
+      order[j] = order[j - 1];
+      --j;
+    }
+    order[j] = i;
+  }
+  for (int c = 0; c < 2; ++c)
+    for (int b = 0; b < kSpBlock; ++b) coef[c * kSpBlock + b] = b < B ? V[b][order[c]] : 0.0;
+}
+
+// emb[:, c] = q coef_c (basis order), with block partials of each column's sum.
+__global__ void __launch_bounds__(kSpThreads)
+sp_embed_kernel(const double* __restrict__ q, const double* __restrict__ coef, int n, int B,
+                double* __restrict__ emb, double* __restrict__ part) {
+  double acc0 = 0.0, acc1 = 0.0;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    double v0 = 0.0, v1 = 0.0;
+    for (int b = 0; b < B; ++b) {
+      const double x = q[(long long)b * n + r];
+      v0 = __dadd_rn(v0, __dmul_rn(x, coef[b]));
+      v1 = __dadd_rn(v1, __dmul_rn(x, coef[kSpBlock + b]));
+    }
+    emb[r] = v0;
+    emb[(long long)n + r] = v1;
+    acc0 = __dadd_rn(acc0, v0);
+    acc1 = __dadd_rn(acc1, v1);
+  }
+  block_partial(acc0, part);
+  __syncthreads();
+  block_partial(acc1, part + gridDim.x);
+}
+
+// emb[:, c] -= mean_c (sums in part[c * nparts ...]); block maxima of |emb| into pmax.
+__global__ void __launch_bounds__(kSpThreads)
+sp_centre_kernel(double* __restrict__ emb, int n, const double* __restrict__ part, int nparts,
+                 double* __restrict__ pmax) {
+  __shared__ double s_w[kSpThreads / 32];
+  const double m0 = __ddiv_rn(sum_partials(part, nparts), (double)n);
+  const double m1 = __ddiv_rn(sum_partials(part + nparts, nparts), (double)n);
+  double mx = 0.0;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    const double a = __dsub_rn(emb[r], m0), b = __dsub_rn(emb[(long long)n + r], m1);
+    emb[r] = a;
+    emb[(long long)n + r] = b;
+    if (isfinite(a)) mx = fmax(mx, fabs(a));
+    if (isfinite(b)) mx = fmax(mx, fabs(b));
+  }
+  mx = warp_max(mx);
+  if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t = fmax(t, s_w[w]);
+    pmax[blockIdx.x] = t;
+  }
+}
+
+// emb = emb * (10 / max|emb|) + jitter, unless the maximum is zero or not finite.
+__global__ void sp_expand_kernel(double* __restrict__ emb, int n, const double* __restrict__ pmax, int nparts,
+                                 const double* __restrict__ jitter) {
+  __shared__ double s_mx;
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int b = 0; b < nparts; ++b) t = fmax(t, pmax[b]);
+    s_mx = t;
+  }
+  __syncthreads();
+  const double mx = s_mx;
+  if (!isfinite(mx) || mx <= 0.0) return;
+  const double ex = __ddiv_rn(10.0, mx);
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < 2LL * n;
+       t += (long long)gridDim.x * blockDim.x)
+    emb[t] = __dadd_rn(__dmul_rn(emb[t], ex), jitter[t]);
+}
+
+// scale_embedding_sdev: column c -> (x - mean) * (target / sd), sd over n - 1.
+__global__ void __launch_bounds__(kSpThreads)
+sp_column_sum_kernel(const double* __restrict__ col, int n, const double* __restrict__ mean_part, int nparts,
+                     double* __restrict__ part) {
+  const double mean = mean_part ? __ddiv_rn(sum_partials(mean_part, nparts), (double)n) : 0.0;
+  double acc = 0.0;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    if (mean_part) {
+      const double d = __dsub_rn(col[r], mean);
+      acc = __dadd_rn(acc, __dmul_rn(d, d));
+    } else {
+      acc = __dadd_rn(acc, col[r]);
+    }
+  }
+  block_partial(acc, part);
+}
+
+__global__ void sp_rescale_kernel(double* __restrict__ col, int n, const double* __restrict__ mean_part,
+                                  const double* __restrict__ ss_part, int nparts, double target) {
+  const double mean = __ddiv_rn(sum_partials(mean_part, nparts), (double)n);
+  const double sd = __dsqrt_rn(__ddiv_rn(sum_partials(ss_part, nparts), (double)(n - 1)));
+  if (!isfinite(sd) || sd <= 0.0) return;
+  const double sc = __ddiv_rn(target, sd);
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
+    col[r] = __dmul_rn(__dsub_rn(col[r], mean), sc);
+}
+
+}  // namespace
+
+void umap_spectral_start(const int* offsets, const int* neighbors, const float* weights, int n, long long nnz,
+                         int spectral_n_iter, double init_scale, int seed, double* out, cudaStream_t s) {
+  if (n < 1 || spectral_n_iter < 1) throw Error("invalid spectral initialization parameters");
+  std::mt19937 rng((std::uint32_t)seed);
+  std::normal_distribution<double> normal(0.0, 0.0001);
+  std::uniform_real_distribution<double> uniform(-10.0, 10.0);
+  const int B = std::min(n - 1, kSpBlock);
+  const int nb = sp_blocks(n);
+  const int gb = std::max(1, std::min(ceil_div(n, kSpThreads), sm_count() * 8));
+  std::vector<double> host;
+  if (nnz < 1 || B < 2) {
+    // the reference's fallback: uniform(-10, 10) coordinates, column after column
+    host.resize(2 * (std::size_t)n);
+    for (double& v : host) v = uniform(rng);
+    FE_CUDA(cudaMemcpyAsync(out, host.data(), sizeof(double) * host.size(), cudaMemcpyHostToDevice, s));
+  } else {
+    float *deg = nullptr, *nw = nullptr;
+    double *triv = nullptr, *q = nullptr, *z = nullptr, *pa = nullptr, *pb = nullptr, *pc = nullptr;
+    double *coef = nullptr, *jit = nullptr;
+    int* flag = nullptr;
+    Arena w;
+    w.reserve(&deg, n);
+    w.reserve(&nw, (std::size_t)nnz);
+    w.reserve(&triv, n);
+    w.reserve(&q, (std::size_t)n * B);
+    w.reserve(&z, (std::size_t)n * B);
+    w.reserve(&pa, kSpMaxBlocks * kSpPairs);
+    w.reserve(&pb, kSpMaxBlocks * 2);
+    w.reserve(&pc, kSpMaxBlocks * 2);
+    w.reserve(&coef, 2 * kSpBlock);
+    w.reserve(&jit, 2 * (std::size_t)n);
+    w.reserve(&flag, 1);
+    w.commit("UMAP spectral start");
+    sp_degree_kernel<<<gb, kSpThreads, 0, s>>>(offsets, weights, n, deg);
+    FE_LAUNCH("sp_degree_kernel");
+    sp_adjacency_kernel<<<nb, kSpThreads, 0, s>>>(offsets, neighbors, weights, deg, n, nw, triv, pa);
+    FE_LAUNCH("sp_adjacency_kernel");
+    sp_normalise_trivial_kernel<<<gb, kSpThreads, 0, s>>>(triv, n, pa, nb);
+    FE_LAUNCH("sp_normalise_trivial_kernel");
+    FE_CUDA(cudaMemsetAsync(flag, 0xff, sizeof(int), s));  // -1: no vanished column
+
+    // column c of the block in `m`, orthonormalised from column `from` on; the host redraws a
+    // vanished column from the stream and resumes there
+    auto orthonormalise = [&](double* m, int from) {
+      for (;;) {
+        for (int c = from; c < B; ++c) {
+          double* qc = m + (std::size_t)c * n;
+          double* in = pb;
+          double* outp = pc;
+          gs_dot_kernel<<<nb, kSpThreads, 0, s>>>(qc, triv, n, in, flag);
+          FE_LAUNCH("gs_dot_kernel");
+          for (int j = 0; j <= c; ++j) {
+            const double* u = j == 0 ? triv : m + (std::size_t)(j - 1) * n;
+            const double* v = j < c ? m + (std::size_t)j * n : qc;
+            gs_sub_dot_kernel<<<nb, kSpThreads, 0, s>>>(qc, u, in, nb, v, n, outp, flag);
+            FE_LAUNCH("gs_sub_dot_kernel");
+            std::swap(in, outp);
+          }
+          gs_scale_kernel<<<nb, kSpThreads, 0, s>>>(qc, in, nb, n, c, flag);
+          FE_LAUNCH("gs_scale_kernel");
+        }
+        int f = -1;
+        FE_CUDA(cudaMemcpyAsync(&f, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+        FE_CUDA(cudaStreamSynchronize(s));
+        if (f < 0) return;
+        host.resize(n);
+        for (double& v : host) v = normal(rng) * 10000.0;
+        FE_CUDA(cudaMemcpyAsync(m + (std::size_t)f * n, host.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+        FE_CUDA(cudaMemsetAsync(flag, 0xff, sizeof(int), s));
+        FE_CUDA(cudaStreamSynchronize(s));
+        from = f;
+      }
+    };
+
+    host.resize((std::size_t)n * B);
+    for (double& v : host) v = normal(rng) * 10000.0;
+    FE_CUDA(cudaMemcpyAsync(q, host.data(), sizeof(double) * host.size(), cudaMemcpyHostToDevice, s));
+    orthonormalise(q, 0);
+    for (int it = 0; it < spectral_n_iter; ++it) {
+      sp_multiply_kernel<<<gb, kSpThreads, 0, s>>>(offsets, neighbors, nw, n, B, q, z);
+      FE_LAUNCH("sp_multiply_kernel");
+      orthonormalise(z, 0);
+      std::swap(q, z);
+    }
+    sp_multiply_kernel<<<gb, kSpThreads, 0, s>>>(offsets, neighbors, nw, n, B, q, z);
+    FE_LAUNCH("sp_multiply_kernel");
+    sp_project_kernel<<<nb, kSpThreads, 0, s>>>(q, z, n, B, pa);
+    FE_LAUNCH("sp_project_kernel");
+    sp_ritz_kernel<<<1, 32, 0, s>>>(pa, nb, B, coef);
+    FE_LAUNCH("sp_ritz_kernel");
+    sp_embed_kernel<<<nb, kSpThreads, 0, s>>>(q, coef, n, B, out, pb);
+    FE_LAUNCH("sp_embed_kernel");
+    sp_centre_kernel<<<nb, kSpThreads, 0, s>>>(out, n, pb, nb, pc);
+    FE_LAUNCH("sp_centre_kernel");
+    // jitter: a fresh normal(0, 1e-4) distribution on the same stream, column after column
+    std::normal_distribution<double> jitter(0.0, 1e-4);
+    host.resize(2 * (std::size_t)n);
+    for (double& v : host) v = jitter(rng);
+    FE_CUDA(cudaMemcpyAsync(jit, host.data(), sizeof(double) * host.size(), cudaMemcpyHostToDevice, s));
+    sp_expand_kernel<<<gb, kSpThreads, 0, s>>>(out, n, pc, nb, jit);
+    FE_LAUNCH("sp_expand_kernel");
+    FE_CUDA(cudaStreamSynchronize(s));
+  }
+  if (std::isfinite(init_scale) && init_scale > 0.0 && n >= 2) {
+    double *pm = nullptr, *ps = nullptr;
+    Arena w;
+    w.reserve(&pm, kSpMaxBlocks);
+    w.reserve(&ps, kSpMaxBlocks);
+    w.commit("UMAP start rescale");
+    for (int c = 0; c < 2; ++c) {
+      double* col = out + (std::size_t)c * n;
+      sp_column_sum_kernel<<<nb, kSpThreads, 0, s>>>(col, n, nullptr, nb, pm);
+      FE_LAUNCH("sp_column_sum_kernel");
+      sp_column_sum_kernel<<<nb, kSpThreads, 0, s>>>(col, n, pm, nb, ps);
+      FE_LAUNCH("sp_column_sum_kernel");
+      sp_rescale_kernel<<<gb, kSpThreads, 0, s>>>(col, n, pm, ps, nb, init_scale);
+      FE_LAUNCH("sp_rescale_kernel");
+    }
+    FE_CUDA(cudaStreamSynchronize(s));
+  }
+}
+
+}  // namespace fe

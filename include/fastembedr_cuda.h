@@ -93,6 +93,68 @@ int fastembedr_cuda_umap_graph_from_knn(const int* indices, const float* distanc
                                         int* offsets, int* neighbors, float* weights, float* epochs_per_sample,
                                         long long capacity, long long* nnz, float* max_weight);
 
+/* No reference counterpart (the reference computes this start on the CPU even for the CUDA
+ * backend: spectral_knn_init(backend = "cpu"), R/fast_knn_umap.R:1343-1365, used by
+ * initialize_umap_gpu_host_knn, R/umap_core_helpers.R:205-243). GPU twin of fast_knn_umap_range_cpp
+ * with n_epochs = 0 (src/fast_knn_umap.cpp:4461-4501): the fuzzy graph of the column-major n x k
+ * KNN, then initialize_layout_csr (:2231-2528) with the reference's std::mt19937(seed) draws and
+ * scale_embedding_sdev(init_scale) when init_scale is finite and > 0 (:2681-2703). out: host,
+ * column-major n x 2 doubles (an R NumericMatrix). Sums over points are reduced in a fixed block
+ * order instead of sequentially, so results equal the CPU start to rounding. */
+int fastembedr_cuda_umap_spectral_init_from_knn(const int* indices, const float* distances, int n, int k,
+                                                int index_offset, int spectral_n_iter, double init_scale, int seed,
+                                                double* out);
+/* The same start from a CSR graph (host arrays): the GPU twin of fast_knn_umap_csr_cpp with
+ * n_epochs = 0 (src/fast_knn_umap.cpp:5291-5321, as umap_init_from_csr_graph calls it,
+ * R/fast_knn_umap.R:665-689). Inputs are checked as validate_csr_inputs does (:747-785; 0- or
+ * 1-based neighbours) and must be symmetric (w_ij == w_ji, as every UMAP fuzzy or binary graph
+ * is). out: host, column-major n x 2 doubles. */
+int fastembedr_cuda_umap_spectral_init_csr(const int* offsets, const int* neighbors, const float* weights, int n,
+                                           int spectral_n_iter, double init_scale, int seed, double* out);
+/* No reference counterpart: umap_knn(backend = "cuda") with the start above computed on the GPU
+ * instead of the CPU (R/umap_core_helpers.R:205-243 then fastembedr_cuda_umap_optimize_coo): KNN ->
+ * fuzzy graph -> spectral start -> n_epochs SGD epochs (min_dist through find_ab_params), one
+ * seed for both as in the reference. out: row-major n x 2 host floats. */
+int fastembedr_cuda_umap_knn_spectral(const int* indices, const float* distances, int n, int k, int index_offset,
+                                      int n_epochs, int negative_sample_rate, float learning_rate, float min_dist,
+                                      float repulsion_strength, int spectral_n_iter, double init_scale,
+                                      unsigned int seed, float* out);
+
+/* find_ab_params (src/fast_knn_umap.cpp:437-497), the curve a, b that the reference's bridges
+ * compute on the host before calling the fused UMAP entry points below (host code, no GPU). */
+void fastembedr_umap_find_ab_params(double spread, double min_dist, double* a, double* b);
+
+/* replaces fastembedr_cuda_spectral_init_from_knn, src/embedding_cuda_kernels.cpp:4801-4960
+ * (bound by spectral_knn_init_cuda_impl, src/embedding_cuda_impl.cpp:1589-1628): the diffusion
+ * start of initialize_layout_csr_cuda_diffusion (src/fast_knn_umap.cpp:2597-2652) over the fuzzy
+ * graph of the column-major n x k KNN (the graph of fastembedr_cuda_umap_graph_from_knn, every
+ * union entry kept). out: row-major n x 2 floats, whitened (zero mean, unit-norm x, y orthogonal
+ * to x with unit norm). Requires 2 <= n, 1 <= k <= 256, spectral_n_iter >= 1. */
+int fastembedr_cuda_spectral_init_from_knn(const int* indices, const double* distances, int n, int k,
+                                           int spectral_n_iter, unsigned int seed, int index_offset, float* out);
+
+/* replace fastembedr_cuda_umap_from_knn_spectral / _float (src/embedding_cuda_kernels.cpp:5360-5449,
+ * bound by knn_umap_cuda_fused_impl / _float_impl / _gpu_impl, src/embedding_cuda_impl.cpp:1716-1900)
+ * and fastembedr_cuda_umap_from_device_knn_spectral_float
+ * (:5462-5481, device KNN pointers): KNN -> fuzzy graph (unit weights with binary_graph) ->
+ * diffusion start (spectral_n_iter rounds, seed) -> n_epochs SGD epochs with curve a, b, all on
+ * the GPU. out: row-major n x 2 host floats. Only optimizer_mode 0 (the package policy) is
+ * provided. */
+int fastembedr_cuda_umap_from_knn_spectral(const int* indices, const double* distances, int n, int k, int n_epochs,
+                                           int negative_sample_rate, float learning_rate, float a, float b,
+                                           float repulsion_strength, int spectral_n_iter, unsigned int seed,
+                                           int index_offset, int optimizer_mode, float* out);
+int fastembedr_cuda_umap_from_knn_spectral_float(const int* indices, const float* distances, int n, int k,
+                                                 int n_epochs, int negative_sample_rate, float learning_rate, float a,
+                                                 float b, float repulsion_strength, int spectral_n_iter,
+                                                 unsigned int seed, int index_offset, int optimizer_mode, float* out);
+int fastembedr_cuda_umap_from_device_knn_spectral_float(const int* device_indices, const float* device_distances,
+                                                        int n, int k, int n_epochs, int negative_sample_rate,
+                                                        float learning_rate, float a, float b,
+                                                        float repulsion_strength, int spectral_n_iter,
+                                                        unsigned int seed, int index_offset, int optimizer_mode,
+                                                        int binary_graph, float* out);
+
 /* No reference counterpart (the reference builds the graph on the host): KNN -> fuzzy graph ->
  * SGD entirely on the GPU, with a/b from the package's min_dist policy (spread 1). */
 int fastembedr_cuda_umap_from_knn(const int* indices, const float* distances, const float* init, int n, int k,

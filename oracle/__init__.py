@@ -80,6 +80,8 @@ def orc() -> C.CDLL:
             "orc_umap_powf_fast": (F, [F, F]),
             "orc_umap_pow": (D, [D, D]),
             "orc_umap_sgd_serial": (V, [I, i32p, i32p, f32p, f64p, I, D, D, I, D, D, I]),
+            "orc_umap_diffusion_init": (V, [i32p, i32p, f32p, I, I, I, I, f32p]),
+            "orc_umap_spectral_init": (V, [i32p, i32p, f32p, I, I, D, I, f64p]),
             "orc_umap_sgd_coo_schedule": (V, [I, I, i32p, i32p, f32p, f32p, I, F, F, I, F, F, C.c_uint]),
             "orc_transform_tsne": (I, [f64p, I, i32p, f64p, I, I, C.c_void_p, I, D, I, I, D, D, D, D, D,
                                        D, D, I, I, I, f64p]),
@@ -118,6 +120,12 @@ def ref() -> C.CDLL:
                                        C.POINTER(D)]
         lib.ref_umap_sgd.restype = I
         lib.ref_umap_sgd.argtypes = [i32p, i32p, f64p, f64p, I, L, I, D, I, D, D, I, I, f64p]
+        lib.ref_umap_diffusion_init.restype = I
+        lib.ref_umap_diffusion_init.argtypes = [i32p, i32p, f64p, I, L, I, I, f64p]
+        lib.ref_umap_spectral_init.restype = I
+        lib.ref_umap_spectral_init.argtypes = [i32p, i32p, f64p, I, L, I, D, I, f64p]
+        lib.ref_umap_spectral_knn.restype = I
+        lib.ref_umap_spectral_knn.argtypes = [i32p, f64p, I, I, I, I, f64p]
         _REF = lib
     return _REF
 
@@ -267,6 +275,26 @@ def umap_ab(min_dist=0.01, spread=1.0, cuda_host=False):
     fn = orc().orc_umap_ab_cuda_host if cuda_host else orc().orc_umap_ab
     fn(float(spread), float(min_dist), C.byref(a), C.byref(b))
     return a.value, b.value
+
+
+def umap_diffusion_init(offsets, neighbors, weights, n_iter, seed, index_offset=0):
+    """The reference's diffusion start over a CSR graph (row-major n x 2 float32)."""
+    n = len(offsets) - 1
+    out = np.zeros((n, 2), np.float32)
+    orc().orc_umap_diffusion_init(np.ascontiguousarray(offsets, np.int32), np.ascontiguousarray(neighbors, np.int32),
+                                  np.ascontiguousarray(weights, np.float32), n, int(index_offset), int(n_iter),
+                                  int(seed), out.ravel())
+    return out
+
+
+def umap_spectral_init(offsets, neighbors, weights, n_iter, seed, init_scale=float("nan")):
+    """The reference CPU spectral start over a CSR graph (row-major n x 2 float64)."""
+    n = len(offsets) - 1
+    out = np.zeros(2 * n)
+    orc().orc_umap_spectral_init(np.ascontiguousarray(offsets, np.int32), np.ascontiguousarray(neighbors, np.int32),
+                                 np.ascontiguousarray(weights, np.float32), n, int(n_iter), float(init_scale),
+                                 int(seed), out)
+    return out.reshape(2, n).T.copy()
 
 
 def umap_sgd_coo(n, heads, tails, eps, init, n_epochs, a, b, nsr=5, lr=1.0, gamma=1.0, seed=42):

@@ -80,6 +80,10 @@ void orc_umap_sgd_serial(int n, const int* offsets, const int* neighbors, const 
                          double* emb_colmajor, int n_epochs, double a, double b,
                          int negative_sample_rate, double learning_rate,
                          double repulsion_strength, int seed);
+void orc_umap_diffusion_init(const int* offsets, const int* neighbors, const float* weights, int n,
+                             int index_offset, int n_iter, int seed, float* out);
+void orc_umap_spectral_init(const int* offsets, const int* neighbors, const float* weights, int n,
+                            int n_iter, double init_scale, int seed, double* out);
 void orc_umap_sgd_coo_schedule(int n, int n_edges, const int* heads, const int* tails,
                                const float* epochs_per_sample, float* y, int n_epochs,
                                float a, float b, int negative_sample_rate, float learning_rate,

@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <limits>
 #include <string>
 
 using Rcpp::IntegerMatrix;
@@ -15,7 +16,7 @@ using Rcpp::NumericMatrix;
 using Rcpp::NumericVector;
 
 // prototypes of the reference exports (src/tsne_neighbors.cpp:1656, :1698, :1871, :2124;
-// src/fast_knn_umap.cpp:3996, :4547)
+// src/fast_knn_umap.cpp:3996, :4461, :4525, :4547, :5291)
 double opentsne_kl_diagnostic_cpp(IntegerMatrix, SEXP, SEXP, double, int);
 List opentsne_force_diagnostic_cpp(IntegerMatrix, SEXP, SEXP, double, double, int, int);
 List knn_tsne_opentsne_float_cpp(IntegerMatrix, SEXP, NumericMatrix, bool, int, double, double, int,
@@ -27,6 +28,11 @@ List transform_tsne_cpp(NumericMatrix, IntegerMatrix, NumericMatrix, NumericMatr
 Rcpp::List umap_graph_csr_float_cpp(IntegerMatrix, SEXP, int, int, int, int);
 NumericMatrix fast_knn_umap_csr_init_cpp(IntegerVector, IntegerVector, SEXP, NumericMatrix, int, double,
                                          int, double, double, int, int, bool);
+NumericMatrix umap_cuda_diffusion_init_csr_cpp(IntegerVector, IntegerVector, SEXP, int, int, int);
+NumericMatrix fast_knn_umap_csr_cpp(IntegerVector, IntegerVector, SEXP, int, int, double, int, double, double, int,
+                                    int, double, int, bool);
+NumericMatrix fast_knn_umap_range_cpp(IntegerMatrix, NumericMatrix, int, int, int, int, double, int, double, double,
+                                      int, int, double, int, bool);
 
 namespace {
 thread_local std::string last_error;
@@ -181,6 +187,64 @@ int ref_umap_sgd(const int* offsets, const int* neighbors, const double* weights
     NumericMatrix r = fast_knn_umap_csr_init_cpp(o, nb, w, num_matrix(init, n, 2), n_epochs, min_dist, nsr,
                                                  learning_rate, gamma, threads, seed, false);
     copy_out(r, out);
+    return 0;
+  } catch (const std::exception& e) {
+    last_error = e.what();
+    return 1;
+  }
+}
+
+// umap_cuda_diffusion_init_csr_cpp (the CPU statement of the GPU diffusion start) with one
+// worker; out row-major n x 2.
+int ref_umap_diffusion_init(const int* offsets, const int* neighbors, const double* weights, int n, long long nnz,
+                            int n_iter, int seed, double* out) {
+  try {
+    IntegerVector o(offsets, offsets + n + 1);
+    IntegerVector nb(neighbors, neighbors + nnz);
+    NumericVector w(weights, weights + nnz);
+    NumericMatrix r = umap_cuda_diffusion_init_csr_cpp(o, nb, w, n_iter, 1, seed);
+    for (int i = 0; i < n; ++i) {
+      out[2 * i] = r(i, 0);
+      out[2 * i + 1] = r(i, 1);
+    }
+    return 0;
+  } catch (const std::exception& e) {
+    last_error = e.what();
+    return 1;
+  }
+}
+
+// fast_knn_umap_csr_cpp with n_epochs = 0 (the CPU spectral start, as umap_init_from_csr_graph
+// calls it) with one worker; out row-major n x 2.
+int ref_umap_spectral_init(const int* offsets, const int* neighbors, const double* weights, int n, long long nnz,
+                           int n_iter, double init_scale, int seed, double* out) {
+  try {
+    IntegerVector o(offsets, offsets + n + 1);
+    IntegerVector nb(neighbors, neighbors + nnz);
+    NumericVector w(weights, weights + nnz);
+    NumericMatrix r = fast_knn_umap_csr_cpp(o, nb, w, 2, 0, 0.01, 0, 1.0, 1.0, n_iter, 1, init_scale, seed, false);
+    for (int i = 0; i < n; ++i) {
+      out[2 * i] = r(i, 0);
+      out[2 * i + 1] = r(i, 1);
+    }
+    return 0;
+  } catch (const std::exception& e) {
+    last_error = e.what();
+    return 1;
+  }
+}
+
+// spectral_knn_init(backend = "cpu") (R/fast_knn_umap.R:1343-1365): fast_knn_umap_range_cpp over
+// all k columns with n_epochs = 0, one worker; idx / dist column-major n x k, out row-major n x 2.
+int ref_umap_spectral_knn(const int* idx, const double* dist, int n, int k, int n_iter, int seed, double* out) {
+  try {
+    NumericMatrix r = fast_knn_umap_range_cpp(int_matrix(idx, n, k), num_matrix(dist, n, k), 0, k, 2, 0, 0.01, 0,
+                                              1.0, 1.0, n_iter, 1, std::numeric_limits<double>::quiet_NaN(), seed,
+                                              false);
+    for (int i = 0; i < n; ++i) {
+      out[2 * i] = r(i, 0);
+      out[2 * i + 1] = r(i, 1);
+    }
     return 0;
   } catch (const std::exception& e) {
     last_error = e.what();

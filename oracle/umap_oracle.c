@@ -471,3 +471,75 @@ void orc_umap_sgd_coo_schedule(int n, int n_edges, const int* heads, const int* 
       }
   }
 }
+
+/* deterministic_unit, src/fast_knn_umap.cpp:522-530: a value in [-1, 1] from (seed, row, col) */
+static float det_unit(int seed, int row, int col) {
+  uint32_t x = (uint32_t)seed;
+  x ^= (uint32_t)(row + 1) * 0x9e3779b9u;
+  x ^= (uint32_t)(col + 1) * 0x85ebca6bu;
+  return (float)(mix_seed(x) & 0x00ffffffu) / 8388607.5f - 1.0f;
+}
+
+/* normalize_cuda_like_init, src/fast_knn_umap.cpp:2541-2595 with one worker (sequential sums):
+ * centre both columns, scale x to unit norm, remove x's projection from y and scale it to unit
+ * norm (row-major n x 2 floats in place). */
+static void whiten_pair(float* v, int n) {
+  double sx = 0.0, sy = 0.0, sx2 = 0.0, sxy = 0.0, sy2 = 0.0;
+  for (int i = 0; i < n; ++i) {
+    const double x = v[2 * i], y = v[2 * i + 1];
+    sx += x;
+    sy += y;
+    sx2 += x * x;
+    sxy += x * y;
+    sy2 += y * y;
+  }
+  const double dn = (double)n;
+  const double mx = sx / dn, my = sy / dn;
+  const double xss = fmax(sx2 - sx * sx / dn, 1.0e-24), yss = fmax(sy2 - sy * sy / dn, 1.0e-24);
+  const double xy = sxy - sx * sy / dn;
+  const double nx = sqrt(xss), inx = 1.0 / nx, proj = xy / nx;
+  const double iny = 1.0 / sqrt(fmax(yss - proj * proj, 1.0e-24));
+  for (int i = 0; i < n; ++i) {
+    const double x = ((double)v[2 * i] - mx) * inx;
+    const double y = (((double)v[2 * i + 1] - my) - proj * x) * iny;
+    v[2 * i] = (float)x;
+    v[2 * i + 1] = (float)y;
+  }
+}
+
+/* initialize_layout_csr_cuda_diffusion, src/fast_knn_umap.cpp:2597-2652 (the CPU statement of
+ * the reference's GPU spectral start): hashed start, whitened, then n_iter rounds of weighted
+ * neighbour averaging over the CSR graph, whitened after each. out: row-major n x 2. */
+void orc_umap_diffusion_init(const int* offsets, const int* neighbors, const float* weights, int n,
+                             int index_offset, int n_iter, int seed, float* out) {
+  float* cur = out;
+  float* nxt = (float*)malloc(sizeof(float) * 2 * (size_t)n);
+  for (int i = 0; i < n; ++i) {
+    cur[2 * i] = det_unit(seed, i, 0);
+    cur[2 * i + 1] = det_unit(seed, i, 1);
+  }
+  whiten_pair(cur, n);
+  for (int it = 0; it < n_iter; ++it) {
+    for (int i = 0; i < n; ++i) {
+      float sx = 0.0f, sy = 0.0f, sw = 0.0f;
+      for (int p = offsets[i]; p < offsets[i + 1]; ++p) {
+        const int nb = neighbors[p] - index_offset;
+        const float w = weights[p];
+        if (nb < 0 || nb >= n || nb == i || w <= 0.0f || !isfinite(w)) continue;
+        sx += w * cur[2 * nb];
+        sy += w * cur[2 * nb + 1];
+        sw += w;
+      }
+      if (sw <= 0.0f) {
+        nxt[2 * i] = cur[2 * i];
+        nxt[2 * i + 1] = cur[2 * i + 1];
+      } else {
+        nxt[2 * i] = sx / sw;
+        nxt[2 * i + 1] = sy / sw;
+      }
+    }
+    whiten_pair(nxt, n);
+    memcpy(cur, nxt, sizeof(float) * 2 * (size_t)n);
+  }
+  free(nxt);
+}

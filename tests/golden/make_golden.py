@@ -4,6 +4,7 @@ Runs fastEmbedR's src/tsne_neighbors.cpp and src/fast_knn_umap.cpp, compiled whe
 they lie against the test-only Rcpp shim (``make -C oracle ref``), on small seeded
 inputs and stores inputs + outputs. The fixtures travel with the repository; the
 reference sources do not. Re-run with:  python tests/golden/make_golden.py
+(or ``python tests/golden/make_golden.py umap_diffusion`` for one case).
 """
 from __future__ import annotations
 
@@ -93,6 +94,69 @@ def umap_case():
                         y=out.reshape(2, n).T, n_epochs=200, seed=42)
 
 
+def umap_diffusion_case():
+    """The reference's CPU statement of its GPU diffusion start (umap_cuda_diffusion_init_csr_cpp,
+    one worker) over the reference fuzzy graph of the umap_3k workload (20 rounds, the pilot
+    default for k <= 15), and over a small two-cluster graph with k = 5 (3 rounds)."""
+    R = O.ref()
+    out = {}
+    cases = (("3k", S.mixture(3000, 20, 6, 12, centre_sd=3.0, lognormal_sizes=True, anisotropic=True)[0], 15, 20, 42),
+             ("200", np.vstack([np.random.default_rng(8).normal(-3, 1, (100, 4)),
+                                np.random.default_rng(9).normal(3, 1, (100, 4))]).astype(np.float32), 5, 3, 7))
+    for tag, x, k, iters, seed in cases:
+        idx, dist = S.exact_knn_numpy(x, k)
+        n = idx.shape[0]
+        cap = 2 * n * k
+        off = np.zeros(n + 1, np.int32)
+        nb = np.zeros(cap, np.int32)
+        w, e = np.zeros(cap), np.zeros(cap)
+        nnz, mw = C.c_longlong(), C.c_double()
+        st = R.ref_umap_graph(cm(idx, np.int32), cm(dist, np.float64), n, k, 1, off, nb, w, e, cap, C.byref(nnz),
+                              C.byref(mw))
+        assert st == 0, R.ref_last_error()
+        m = nnz.value
+        y = np.zeros(2 * n)
+        st = R.ref_umap_diffusion_init(off, nb[:m].copy(), w[:m].copy(), n, m, iters, seed, y)
+        assert st == 0, R.ref_last_error()
+        out.update({f"idx_{tag}": idx, f"dist_{tag}": dist, f"init_{tag}": y.reshape(n, 2),
+                    f"iters_{tag}": iters, f"seed_{tag}": seed})
+    np.savez_compressed(os.path.join(OUT, "umap_diffusion.npz"), **out)
+
+
+def umap_spectral_case():
+    """spectral_knn_init(backend = "cpu") of the reference (fast_knn_umap_range_cpp with n_epochs = 0,
+    one worker) on the umap_3k KNN (30 rounds) and on a 40-point KNN (5 rounds); the second also
+    through fast_knn_umap_csr_cpp with init_scale 2 on the reference graph."""
+    R = O.ref()
+    out = {}
+    x3k = S.mixture(3000, 20, 6, 12, centre_sd=3.0, lognormal_sizes=True, anisotropic=True)[0]
+    x40 = np.random.default_rng(41).normal(size=(40, 5)).astype(np.float32)
+    for tag, x, k, iters, seed in (("3k", x3k, 15, 30, 42), ("40", x40, 8, 5, 9)):
+        idx, dist = S.exact_knn_numpy(x, k)
+        n = idx.shape[0]
+        y = np.zeros(2 * n)
+        st = R.ref_umap_spectral_knn(cm(idx, np.int32), cm(dist, np.float64), n, k, iters, seed, y)
+        assert st == 0, R.ref_last_error()
+        out.update({f"idx_{tag}": idx, f"dist_{tag}": dist, f"start_{tag}": y.reshape(n, 2),
+                    f"iters_{tag}": iters, f"seed_{tag}": seed})
+    idx, dist = out["idx_40"], out["dist_40"]
+    n, k = idx.shape
+    cap = 2 * n * k
+    off = np.zeros(n + 1, np.int32)
+    nb = np.zeros(cap, np.int32)
+    w, e = np.zeros(cap), np.zeros(cap)
+    nnz, mw = C.c_longlong(), C.c_double()
+    st = R.ref_umap_graph(cm(idx, np.int32), cm(dist, np.float64), n, k, 1, off, nb, w, e, cap, C.byref(nnz),
+                          C.byref(mw))
+    assert st == 0, R.ref_last_error()
+    m = nnz.value
+    y = np.zeros(2 * n)
+    st = R.ref_umap_spectral_init(off, nb[:m].copy(), w[:m].copy(), n, m, 5, 2.0, 9, y)
+    assert st == 0, R.ref_last_error()
+    out["start_40_scaled"] = y.reshape(n, 2)
+    np.savez_compressed(os.path.join(OUT, "umap_spectral.npz"), **out)
+
+
 def transform_case():
     R = O.ref()
     xr, _ = S.mixture(2500, 20, 5, 13, centre_sd=4.0, within_sd=1.0)
@@ -116,6 +180,11 @@ def transform_case():
 
 def main():
     O.build(ref=True)
+    if len(sys.argv) > 1:
+        for name in sys.argv[1:]:
+            globals()[name + "_case"]()
+        print("golden fixtures written to", OUT)
+        return
     force_case("n48", 701, 48, 6, 15, 5.0, 64, 0.3)
     force_case("n300", 7011, 300, 6, 15, 5.0, 64, 0.3)
     # pathological inputs of tests/testthat/test-tsne-numerics.R:120-160

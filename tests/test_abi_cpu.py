@@ -26,7 +26,9 @@ def test_header_declares_the_reference_abi():
     syms = declared_symbols()
     for ref in ("fastembedr_cuda_available", "fastembedr_cuda_embedding_last_error",
                 "fastembedr_cuda_opentsne_fft_grid_size", "fastembedr_cuda_opentsne_fft_from_knn_float",
-                "fastembedr_cuda_opentsne_fft_from_knn", "fastembedr_cuda_opentsne_fft_from_device_knn_float"):
+                "fastembedr_cuda_opentsne_fft_from_knn", "fastembedr_cuda_opentsne_fft_from_device_knn_float",
+                "fastembedr_cuda_spectral_init_from_knn", "fastembedr_cuda_umap_from_knn_spectral",
+                "fastembedr_cuda_umap_from_knn_spectral_float", "fastembedr_cuda_umap_from_device_knn_spectral_float"):
         assert ref in syms
 
 
@@ -61,3 +63,36 @@ def test_no_device_is_an_error_not_a_fallback():
 def test_index_offset_detection():
     assert api.knn_index_offset(np.array([[2, 3], [1, 3], [1, 2]])) == 1
     assert api.knn_index_offset(np.array([[1, 2], [0, 2], [0, 1]])) == 0
+
+
+@pytest.mark.parametrize("min_dist", [0.01, 0.1, 0.25, 0.5, 0.05])
+def test_umap_curve_parameters_match_the_oracle(min_dist):
+    """find_ab_params is host code in the library; the oracle restates the reference's."""
+    import oracle as O
+
+    a, b = api.umap_ab_params(min_dist)
+    ra, rb = O.umap_ab(min_dist)
+    assert a == pytest.approx(ra, rel=1e-12) and b == pytest.approx(rb, rel=1e-12)
+
+
+def test_spectral_start_csr_checks_its_graph_before_any_device_work():
+    """Host-side checks of fastembedr_cuda_umap_spectral_init_csr (validate_csr_inputs plus the
+    symmetry the GPU start needs) report errors without a GPU."""
+    lib = _lib.load()
+    out = np.zeros(6)
+
+    def call(off, nb, w):
+        off, nb, w = (np.ascontiguousarray(off, np.int32), np.ascontiguousarray(nb, np.int32),
+                      np.ascontiguousarray(w, np.float32))
+        st = lib.fastembedr_cuda_umap_spectral_init_csr(off.ctypes.data, nb.ctypes.data, w.ctypes.data, 3, 5, 0.0,
+                                                        1, out.ctypes.data)
+        return st, lib.fastembedr_cuda_embedding_last_error().decode()
+
+    st, msg = call([0, 1, 2, 3], [1, 2, 0], [1.0, 1.0, 1.0])  # 0->1, 1->2, 2->0: not symmetric
+    assert st != 0 and "symmetric" in msg
+    st, msg = call([0, 1, 2, 2], [1, 1, 0], [1.0, 1.0, 1.0])  # row 1 holds itself
+    assert st != 0 and "self-neighbors" in msg
+    st, msg = call([0, 2, 3, 4], [2, 1, 0, 0], [1.0, 1.0, 1.0, 1.0])
+    assert st != 0 and "sorted" in msg
+    st, msg = call([0, 1, 2, 2], [1, 0, 0], [1.0, -1.0, 1.0])
+    assert st != 0 and "positive and finite" in msg

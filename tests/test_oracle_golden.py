@@ -52,6 +52,27 @@ def test_umap_graph_and_serial_sgd_match_reference(golden):
     np.testing.assert_array_equal(emb.reshape(2, n).T, g["y"])
 
 
+@pytest.mark.parametrize("tag", ["3k", "200"])
+def test_umap_diffusion_start_matches_reference(golden, tag):
+    """initialize_layout_csr_cuda_diffusion (one worker) over the reference fuzzy graph."""
+    g = golden("umap_diffusion")
+    off, nb, w, _, _ = O.umap_graph(g["idx_" + tag], g["dist_" + tag])
+    y = O.umap_diffusion_init(off, nb, w, int(g["iters_" + tag]), int(g["seed_" + tag]))
+    np.testing.assert_array_equal(y.astype(np.float64), g["init_" + tag])
+
+
+@pytest.mark.parametrize("tag", ["3k", "40"])
+def test_umap_spectral_start_matches_reference(golden, tag):
+    """initialize_layout_csr through spectral_knn_init(backend = "cpu"), one worker."""
+    g = golden("umap_spectral")
+    off, nb, w, _, _ = O.umap_graph(g["idx_" + tag], g["dist_" + tag])
+    y = O.umap_spectral_init(off, nb, w, int(g["iters_" + tag]), int(g["seed_" + tag]))
+    np.testing.assert_array_equal(y, g["start_" + tag])
+    if tag == "40":
+        ys = O.umap_spectral_init(off, nb, w, 5, 9, init_scale=2.0)
+        np.testing.assert_array_equal(ys, g["start_40_scaled"])
+
+
 @pytest.mark.parametrize("tag,nneg,thr", [("exact", 256, 4096), ("sampled", 64, 10)])
 def test_transform_matches_reference(golden, tag, nneg, thr):
     g = golden("transform_2k")

@@ -108,3 +108,143 @@ def test_batched_umap_matches_each_instance_alone():
         pb = O.knn_preservation(lay, idx, keep=keep, preserve_k=15)
         assert np.all(np.isfinite(lay)) and np.abs(lay).max() <= 16.0
         assert abs(pa - pb) < 0.01, (n, pa, pb)
+
+
+@pytest.mark.parametrize("tag", ["3k", "200"])
+def test_diffusion_start_matches_reference_golden(golden, tag):
+    """fastembedr_cuda_spectral_init_from_knn against the reference's CPU statement of its GPU
+    diffusion start (golden), and against the oracle on this build's own graph."""
+    g = golden("umap_diffusion")
+    idx, dist = g["idx_" + tag], g["dist_" + tag]
+    iters, seed = int(g["iters_" + tag]), int(g["seed_" + tag])
+    got = api.umap_spectral_init(idx, dist, iters, seed)
+    want = g["init_" + tag]
+    scale = np.abs(want).max()
+    # graph weights agree with the reference builder to 2e-6; averaging keeps that size
+    assert np.abs(got - want).max() <= 2e-5 * scale
+    gr = api.umap_graph(idx, dist)
+    orc = O.umap_diffusion_init(gr["offsets"], gr["neighbors"], gr["weights"], iters, seed)
+    # same graph: rows are summed exactly as the restatement; only the whitening moments are
+    # reduced in another order
+    assert np.abs(got - orc).max() <= 1e-6 * scale
+    y = got.astype(np.float64)
+    assert np.abs(y.mean(0)).max() < 1e-6
+    assert np.linalg.norm(y[:, 0]) == pytest.approx(1.0, rel=1e-5)
+    assert np.linalg.norm(y[:, 1]) == pytest.approx(1.0, rel=1e-5)
+    assert abs(y[:, 0] @ y[:, 1]) < 1e-5
+
+
+def test_fused_umap_entry_points_match_reference_cpu_sgd():
+    """The three fused entry points (host double, host float, device float KNN) run graph ->
+    diffusion start -> SGD on the GPU; from the same start the reference CPU SGD reaches the
+    same 15-NN preservation within 0.015."""
+    x, _ = synthetic.mixture(20000, 30, 12, 44, centre_sd=3.0, lognormal_sizes=True, anisotropic=True)
+    idx, dist = synthetic.exact_knn_numpy(x, 15)
+    n, k = idx.shape
+    rounds, epochs = 30, 200
+    start = api.umap_spectral_init(idx, dist, rounds, 42)
+    off, nb, w, e, mw = O.umap_graph(idx, dist)
+    a, b = api.umap_ab_params(0.01)
+    emb = np.ascontiguousarray(start.T.astype(np.float64)).ravel().copy()
+    O.orc().orc_umap_sgd_serial(n, off, nb, w, emb, epochs, a, b, 5, 1.0, 1.0, 42)
+    cpu = emb.reshape(2, n).T.astype(np.float32)
+    keep = np.arange(0, n, 4, dtype=np.int32)
+    pc = O.knn_preservation(cpu, idx, keep=keep, preserve_k=15)
+    p0 = O.knn_preservation(start, idx, keep=keep, preserve_k=15)
+    lib = _lib.require_gpu()
+    icm = np.asfortranarray(idx.astype(np.int32))
+    outs = {}
+    for tag, dcm in (("double", np.asfortranarray(dist.astype(np.float64))),
+                     ("float", np.asfortranarray(dist.astype(np.float32)))):
+        out = np.zeros((n, 2), np.float32)
+        fn = lib.fastembedr_cuda_umap_from_knn_spectral if tag == "double" else \
+            lib.fastembedr_cuda_umap_from_knn_spectral_float
+        st = fn(icm.ctypes.data, dcm.ctypes.data, n, k, epochs, 5, 1.0, a, b, 1.0, rounds, 42, 0, 0, out.ctypes.data)
+        _lib.check(st, "fused UMAP " + tag)
+        outs[tag] = out
+    outs["device"] = api.umap_knn(idx, dist, init="diffusion", n_epochs=epochs, spectral_n_iter=rounds, seed=42).layout
+    # the reference starts SGD from the whitened start itself (coordinates ~1/sqrt(n)), so the
+    # first epochs scatter the layout; both sides do the same
+    for tag, y in outs.items():
+        assert np.all(np.isfinite(y)) and np.abs(y).max() <= 16.0, tag
+        pg = O.knn_preservation(y, idx, keep=keep, preserve_k=15)
+        assert abs(pg - pc) < 0.015, (tag, pg, pc, p0)
+    binary = api.umap_knn(idx, dist, init="diffusion", n_epochs=epochs, spectral_n_iter=rounds, seed=42,
+                          graph_mode="binary").layout
+    assert np.all(np.isfinite(binary)) and np.abs(binary).max() <= 16.0
+
+
+def test_fused_umap_rejects_invalid_arguments():
+    x, _ = synthetic.mixture(500, 8, 3, 45, centre_sd=3.0)
+    idx, dist = synthetic.exact_knn_numpy(x, 10)
+    lib = _lib.require_gpu()
+    icm = np.asfortranarray(idx.astype(np.int32))
+    dcm = np.asfortranarray(dist.astype(np.float32))
+    out = np.zeros((500, 2), np.float32)
+    assert lib.fastembedr_cuda_umap_from_knn_spectral_float(icm.ctypes.data, dcm.ctypes.data, 500, 10, 0, 5, 1.0, 1.9,
+                                                            0.8, 1.0, 10, 1, 0, 0, out.ctypes.data) != 0
+    assert b"invalid fused CUDA UMAP" in lib.fastembedr_cuda_embedding_last_error()
+    assert lib.fastembedr_cuda_umap_from_knn_spectral_float(icm.ctypes.data, dcm.ctypes.data, 500, 10, 10, 5, 1.0,
+                                                            1.9, 0.8, 1.0, 10, 1, 0, 1, out.ctypes.data) != 0
+    assert b"optimizer_mode" in lib.fastembedr_cuda_embedding_last_error()
+    with pytest.raises(_lib.CudaEmbeddingError, match="invalid spectral initialization"):
+        api.umap_spectral_init(idx, dist, 0)
+
+
+@pytest.mark.parametrize("tag", ["3k", "40"])
+def test_spectral_start_matches_reference_golden(golden, tag):
+    """The reference CPU spectral start (spectral_knn_init(backend = "cpu")) computed on the GPU:
+    against the reference's own output, and against the oracle on this build's graph."""
+    g = golden("umap_spectral")
+    idx, dist = g["idx_" + tag], g["dist_" + tag]
+    iters, seed = int(g["iters_" + tag]), int(g["seed_" + tag])
+    want = g["start_" + tag]
+    # on the reference's own graph (the oracle's, bit-identical to it) the GPU start differs from
+    # the reference only by the order of the FP64 sums over points. The start is ill-conditioned
+    # in the graph (a 1e-7 relative change of the weights moves the 3k start by 0.7 on its scale
+    # of 10), so it is compared on the same graph, not on this build's graph (weights within 2e-6)
+    off, nb, w, _, _ = O.umap_graph(idx, dist)
+    on_ref_graph = api.umap_spectral_start_csr(off, nb, w, iters, seed)
+    assert np.abs(on_ref_graph - want).max() <= 1e-4, np.abs(on_ref_graph - want).max()
+    # the KNN entry point builds the graph on the GPU: against the oracle on that graph
+    got = api.umap_spectral_start(idx, dist, iters, seed)
+    gr = api.umap_graph(idx, dist)
+    orc = O.umap_spectral_init(gr["offsets"], gr["neighbors"], gr["weights"], iters, seed)
+    assert np.abs(got - orc).max() <= 1e-4, np.abs(got - orc).max()
+    if tag == "40":
+        scaled = api.umap_spectral_start_csr(off, nb, w, 5, 9, init_scale=2.0)
+        assert np.abs(scaled - g["start_40_scaled"]).max() <= 1e-4
+        assert np.std(scaled, axis=0, ddof=1) == pytest.approx([2.0, 2.0], rel=1e-9)
+
+
+def test_spectral_start_matches_oracle_20k():
+    x, _ = synthetic.mixture(20000, 30, 12, 46, centre_sd=3.0, lognormal_sizes=True, anisotropic=True)
+    idx, dist = synthetic.exact_knn_numpy(x, 15)
+    got = api.umap_spectral_start(idx, dist, 30, 7)
+    gr = api.umap_graph(idx, dist)
+    orc = O.umap_spectral_init(gr["offsets"], gr["neighbors"], gr["weights"], 30, 7)
+    assert np.abs(got - orc).max() <= 1e-4, np.abs(got - orc).max()
+    assert np.abs(got).max() == pytest.approx(10.0, abs=1e-3)
+
+
+def test_umap_knn_with_gpu_spectral_start_matches_reference_cpu():
+    """umap_knn's default path (graph -> spectral start -> SGD, all on the GPU) against the
+    reference CPU SGD from the same start: 15-NN preservation within 0.01."""
+    x, _ = synthetic.mixture(20000, 30, 12, 47, centre_sd=3.0, lognormal_sizes=True, anisotropic=True)
+    idx, dist = synthetic.exact_knn_numpy(x, 15)
+    n = idx.shape[0]
+    off, nb, w, e, mw = O.umap_graph(idx, dist)
+    start = api.umap_spectral_start(idx, dist, 30, 42)  # deterministic: the start umap_knn computes
+    a, b = O.umap_ab(0.01)
+    emb = np.ascontiguousarray(start.T).ravel().copy()
+    O.orc().orc_umap_sgd_serial(n, off, nb, w, emb, 200, a, b, 5, 1.0, 1.0, 42)
+    cpu = emb.reshape(2, n).T.astype(np.float32)
+    fit = api.umap_knn(idx, dist, n_epochs=200, seed=42)
+    assert fit.config["init_backend"] == "cuda_spectral_csr" and fit.config["spectral_n_iter"] == 30
+    keep = np.arange(0, n, 4, dtype=np.int32)
+    pc = O.knn_preservation(cpu, idx, keep=keep, preserve_k=15)
+    pg = O.knn_preservation(fit.layout, idx, keep=keep, preserve_k=15)
+    p0 = O.knn_preservation(start.astype(np.float32), idx, keep=keep, preserve_k=15)
+    assert np.all(np.isfinite(fit.layout)) and np.abs(fit.layout).max() <= 16.0
+    assert abs(pg - pc) < 0.01, (pg, pc)
+    assert pg > p0 + 0.02, (pg, p0)
