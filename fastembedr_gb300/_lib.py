@@ -64,6 +64,11 @@ SIGNATURES = {
     "fastembedr_cuda_umap_spectral_init_csr": (I, [vp, vp, vp, I, I, D, I, vp]),
     "fastembedr_cuda_umap_knn_spectral": (I, [vp, vp, I, I, I, I, I, F, F, F, I, D, U, vp]),
     "fastembedr_umap_find_ab_params": (None, [D, D, C.POINTER(D), C.POINTER(D)]),
+    "fastembedr_cuda_opentsne_fft_from_device_knn_float_pca_double": (I, [vp, vp, vp, I, I, I, I, F, I, I, F, F, F, I,
+                                                                       F, F, F, F, U, I, vp]),
+    "fastembedr_cuda_opentsne_fft_from_device_knn_float_pca_float": (I, [vp, vp, vp, I, I, I, I, F, I, I, F, F, F, I,
+                                                                      F, F, F, F, U, I, vp]),
+    "fastembedr_cuda_tsne_pca_init": (I, [vp, I, I, I, vp]),
     "fastembedr_cuda_spectral_init_from_knn": (I, [vp, vp, I, I, I, U, I, vp]),
     "fastembedr_cuda_umap_from_knn_spectral": (I, [vp, vp, I, I, I, I, F, F, F, F, I, U, I, I, vp]),
     "fastembedr_cuda_umap_from_knn_spectral_float": (I, [vp, vp, I, I, I, I, F, F, F, F, I, U, I, I, vp]),

@@ -127,6 +127,21 @@ def tsne_knn(indices, distances, n_neighbors=None, perplexity=None, n_components
     return TsneFit(out, config)
 
 
+def tsne_pca_init(data):
+    """PCA start of t-SNE computed on the GPU (make_cuda_opentsne_pca_init, R/tsne_pca_init.R:28-50,
+    and normalize_opentsne_pca_scores, R/tsne_control.R:515-540): the two leading principal
+    components of the centred data, each signed so its largest-magnitude score is positive,
+    centred and scaled so the larger standard deviation is 1e-4. (n, 2) float32."""
+    x = np.asarray(data)
+    is_double = x.dtype != np.float32
+    xc = np.asfortranarray(x, np.float64 if is_double else np.float32)
+    n, p = xc.shape
+    out = np.zeros((n, 2), np.float32)
+    st = _lib.require_gpu().fastembedr_cuda_tsne_pca_init(xc.ctypes.data, int(is_double), n, p, out.ctypes.data)
+    _lib.check(st, "CUDA PCA initialization")
+    return out
+
+
 def tsne_affinities(indices, distances, perplexity, index_offset=None):
     """Symmetrised CSR P and directed P / entropies from the GPU (diagnostic)."""
     idx = np.asarray(indices)

@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "../../include/fastembedr_cuda.h"
+#include "pca.cuh"
 #include "philox.cuh"
 #include "tsne_exact.cuh"
 #include "tsne_grid.cuh"
@@ -328,17 +329,53 @@ void check_tsne_args(const void* idx, const void* dist, const float* init, int h
     throw Error("invalid CUDA openTSNE FFT-grid dimensions or parameters");
 }
 
+// The PCA start of host data (column-major n x p, float or double) on the GPU, as a host
+// row-major n x 2 init.
+std::vector<float> pca_start(const void* values, bool is_double, int n, int p, cudaStream_t s) {
+  const std::size_t items = (std::size_t)n * p;
+  float* X = nullptr;
+  double* raw = nullptr;
+  float2* init = nullptr;
+  Arena a;
+  a.reserve(&X, items);
+  if (is_double) a.reserve(&raw, items);
+  a.reserve(&init, n);
+  a.commit("device PCA input");
+  if (is_double) {
+    FE_CUDA(cudaMemcpyAsync(raw, values, sizeof(double) * items, cudaMemcpyHostToDevice, s));
+    double_to_float_kernel<<<std::max(1, std::min(ceil_div((long long)items, 256), sm_count() * 8)), 256, 0, s>>>(
+        raw, X, (long long)items);
+    FE_LAUNCH("double_to_float_kernel");
+  } else {
+    FE_CUDA(cudaMemcpyAsync(X, values, sizeof(float) * items, cudaMemcpyHostToDevice, s));
+  }
+  pca_tsne_start(X, n, p, init, s);
+  std::vector<float> h(2 * (std::size_t)n);
+  FE_CUDA(cudaMemcpyAsync(h.data(), init, sizeof(float) * h.size(), cudaMemcpyDeviceToHost, s));
+  FE_CUDA(cudaStreamSynchronize(s));
+  return h;
+}
+
 template <typename DistT>
 int run_tsne_from_knn(const int* indices, const DistT* distances, bool on_device, const float* init, int has_init,
                       int n, int k, int n_components, float perplexity, int early_iter, int n_iter, float early_exag,
                       float exag, float lr, int lr_auto, float m0, float m1, float min_gain, float max_step,
-                      unsigned seed, int offset, float* out) {
+                      unsigned seed, int offset, float* out, const void* pca_values = nullptr,
+                      bool pca_double = false, int pca_p = 0) {
   return guarded([&] {
     check_tsne_args(indices, distances, init, has_init, n, k, n_components, perplexity, early_iter, n_iter,
                     early_exag, exag, lr, lr_auto, m0, m1, min_gain, out);
+    if (!has_init && pca_values && pca_p < n_components)
+      throw Error("invalid CUDA openTSNE FFT-grid dimensions or parameters");
     auto job = std::make_unique<TsneJob>();
     cudaStream_t s = job->stream.s;
     if (on_device) order_after_legacy_stream(s);
+    std::vector<float> pca_init;
+    if (!has_init && pca_values) {
+      pca_init = pca_start(pca_values, pca_double, n, pca_p, s);
+      init = pca_init.data();
+      has_init = 1;
+    }
     const std::size_t items = (std::size_t)n * k;
     int* d_idx = nullptr;
     float* d_dist = nullptr;
@@ -433,6 +470,35 @@ int fastembedr_cuda_opentsne_fft_from_device_knn_float(const int* indices, const
   return fe::run_tsne_from_knn<float>(indices, distances, true, init, has_init, n, k, n_components, perplexity,
                                       early_iter, n_iter, early_exag, exag, lr, lr_auto, m0, m1, min_gain, max_step,
                                       seed, index_offset, out);
+}
+
+int fastembedr_cuda_opentsne_fft_from_device_knn_float_pca_double(
+    const int* indices, const float* distances, const double* pca_init_values, int pca_init_p, int n, int k,
+    int n_components, float perplexity, int early_iter, int n_iter, float early_exag, float exag, float lr,
+    int lr_auto, float m0, float m1, float min_gain, float max_step, unsigned int seed, int index_offset, float* out) {
+  if (!pca_init_values) return fe::guarded([] { throw fe::Error("null CUDA openTSNE input pointer"); });
+  return fe::run_tsne_from_knn<float>(indices, distances, true, nullptr, 0, n, k, n_components, perplexity,
+                                      early_iter, n_iter, early_exag, exag, lr, lr_auto, m0, m1, min_gain, max_step,
+                                      seed, index_offset, out, pca_init_values, true, pca_init_p);
+}
+
+int fastembedr_cuda_opentsne_fft_from_device_knn_float_pca_float(
+    const int* indices, const float* distances, const float* pca_init_values, int pca_init_p, int n, int k,
+    int n_components, float perplexity, int early_iter, int n_iter, float early_exag, float exag, float lr,
+    int lr_auto, float m0, float m1, float min_gain, float max_step, unsigned int seed, int index_offset, float* out) {
+  if (!pca_init_values) return fe::guarded([] { throw fe::Error("null CUDA openTSNE input pointer"); });
+  return fe::run_tsne_from_knn<float>(indices, distances, true, nullptr, 0, n, k, n_components, perplexity,
+                                      early_iter, n_iter, early_exag, exag, lr, lr_auto, m0, m1, min_gain, max_step,
+                                      seed, index_offset, out, pca_init_values, false, pca_init_p);
+}
+
+int fastembedr_cuda_tsne_pca_init(const void* values, int is_double, int n, int p, float* out) {
+  return fe::guarded([&] {
+    if (!values || !out) throw fe::Error("null host pointer");
+    fe::Stream st;
+    const std::vector<float> h = fe::pca_start(values, is_double != 0, n, p, st.s);
+    std::copy(h.begin(), h.end(), out);
+  });
 }
 
 int fastembedr_cuda_tsne_affinities(const int* indices, const float* distances, int n, int k, float perplexity,

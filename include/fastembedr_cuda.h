@@ -72,6 +72,28 @@ int fastembedr_cuda_opentsne_fft_from_device_knn_float(const int* indices, const
                                                        float min_gain, float max_step_norm, unsigned int seed,
                                                        int index_offset, float* out);
 
+/* replace fastembedr_cuda_opentsne_fft_from_device_knn_float_pca_double / _pca_float
+ * (src/embedding_cuda_kernels.cpp:6265-6321, bound by src/embedding_cuda_impl.cpp:2480-2570): the
+ * device-KNN entry above with the start computed on the GPU from the data: pca_init_values is a
+ * HOST column-major n x pca_init_p matrix (double or float). The two leading principal components
+ * (covariance of the centred data, Jacobi eigendecomposition in FP64; the reference calls RAPIDS
+ * RAFT's tsvd_fit_transform with the covariance-eigen solver) give the scores; each score column is
+ * signed so its largest-magnitude entry is positive, centred, and both are scaled by 1e-4 / the
+ * larger standard deviation (src/embedding_cuda_kernels.cpp:1337-1420). pca_init_p <= 1024. */
+int fastembedr_cuda_opentsne_fft_from_device_knn_float_pca_double(
+    const int* indices, const float* distances, const double* pca_init_values, int pca_init_p, int n, int k,
+    int n_components, float perplexity, int early_exaggeration_iter, int n_iter, float early_exaggeration,
+    float exaggeration, float learning_rate, int learning_rate_auto, float initial_momentum, float final_momentum,
+    float min_gain, float max_step_norm, unsigned int seed, int index_offset, float* out);
+int fastembedr_cuda_opentsne_fft_from_device_knn_float_pca_float(
+    const int* indices, const float* distances, const float* pca_init_values, int pca_init_p, int n, int k,
+    int n_components, float perplexity, int early_exaggeration_iter, int n_iter, float early_exaggeration,
+    float exaggeration, float learning_rate, int learning_rate_auto, float initial_momentum, float final_momentum,
+    float min_gain, float max_step_norm, unsigned int seed, int index_offset, float* out);
+/* The PCA start alone (no reference counterpart as an entry point): host column-major n x p data
+ * (is_double: double, else float) -> out, host row-major n x 2 floats. */
+int fastembedr_cuda_tsne_pca_init(const void* values, int is_double, int n, int p, float* out);
+
 /* ---------------------------------------------------------------- UMAP */
 
 /* replaces fastembedr_cuda_umap_optimize_coo, src/embedding_cuda_kernels.cpp:5483-5608.
