@@ -465,14 +465,22 @@ umap_epoch_kernel(float2* __restrict__ y, const int* __restrict__ heads, const i
     }
     const int h = __ldg(heads + e), t = __ldg(tails + e);
     if (h < v0 || h >= v0 + nv || t < v0 || t >= v0 + nv || h == t) continue;
+    // The head's own moves go to a register copy and reach memory in one atomic at the end of
+    // the edge; later samples of the edge see them, as every sample of the serial reference
+    // sees the previous ones. Moves of other threads land through their atomics (Hogwild).
+    float2 yh = y[h];
+    float mx = 0.0f, my = 0.0f;
     for (int s = 0; s < ps; ++s) {
-      const float2 yh = y[h], yt = y[t];
+      const float2 yt = y[t];
       const float dx = yh.x - yt.x, dy = yh.y - yt.y;
       const float d2 = fmaxf(fe, dx * dx + dy * dy);
       const float d2b = schraudolph_pow(d2, p.b);
       const float c = -2.0f * p.a * p.b * (d2b / d2) / (p.a * d2b + 1.0f);
       const float gx = clip4(c * dx) * alpha, gy = clip4(c * dy) * alpha;
-      atomicAdd(y + h, make_float2(gx, gy));
+      yh.x += gx;
+      yh.y += gy;
+      mx += gx;
+      my += gy;
       atomicAdd(y + t, make_float2(-gx, -gy));
     }
     const int ns = umap_negative_samples(period, p.negative_sample_rate, epoch);
@@ -484,13 +492,18 @@ umap_epoch_kernel(float2* __restrict__ y, const int* __restrict__ heads, const i
       const unsigned draw = (s & 3) == 0 ? r.x : ((s & 3) == 1 ? r.y : ((s & 3) == 2 ? r.z : r.w));
       const int neg = v0 + (int)bounded(draw, (unsigned)nv);
       if (neg == h || neg == t) continue;
-      const float2 yh = y[h], yn = y[neg];
+      const float2 yn = y[neg];
       const float dx = yh.x - yn.x, dy = yh.y - yn.y;
       const float d2 = fmaxf(fe, dx * dx + dy * dy);
       const float d2b = schraudolph_pow(d2, p.b);
       const float rc = p.repulsion_strength * 2.0f * p.b / ((0.001f + d2) * (p.a * d2b + 1.0f));
-      atomicAdd(y + h, make_float2(clip4(rc * dx) * alpha, clip4(rc * dy) * alpha));
+      const float gx = clip4(rc * dx) * alpha, gy = clip4(rc * dy) * alpha;
+      yh.x += gx;
+      yh.y += gy;
+      mx += gx;
+      my += gy;
     }
+    atomicAdd(y + h, make_float2(mx, my));
   }
 }
 
