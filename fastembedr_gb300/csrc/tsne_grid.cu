@@ -31,7 +31,8 @@ namespace fe {
 
 constexpr int kStepThreads = 256;
 constexpr int kFftThreads = 256;
-constexpr int kColThreads = 512;  // the column pass holds 110 KB of shared memory: 2 blocks per SM
+constexpr int kColThreads = 256;  // the column pass holds 104 KB of shared memory: 2 blocks per SM;
+                                  // 256 threads take its 3 x 256 radix-16 work items in 3 rounds
 
 // ---------------------------------------------------------------- stencils
 template <int TAPS>
@@ -317,15 +318,17 @@ scatter_kernel(const float2* __restrict__ y, const TsneInstance* __restrict__ in
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
-// Shared-memory index with one pad slot after every 8 complex values: the radix-2^3 passes with
-// small butterfly strides (1, 8) touch elements 8 or 64 apart from consecutive threads, which
-// would otherwise land on the same banks.
-__device__ __forceinline__ int sidx(int i) { return i + (i >> 3); }
-__host__ __device__ constexpr int padded(int count) { return count + count / 8; }
+// Shared-memory index with one pad slot after every 16 complex values: the radix-2^4 passes with
+// small butterfly strides (1, 16) touch elements 16 or 256 apart from consecutive threads, which
+// would otherwise land on the same banks (with this padding every pass of M = 512 .. 2048 is
+// free of bank conflicts for 64-bit accesses).
+__device__ __forceinline__ int sidx(int i) { return i + (i >> 4); }
+__host__ __device__ constexpr int padded(int count) { return count + count / 16; }
 
 // Radix-2 FFTs over `count` sequences of length M = 2^logm stored at buf + seq * M, with R
-// consecutive radix-2 stages fused per shared-memory pass (R <= 3): each work item keeps the
-// 2^R elements i0 + t * 2^s of one butterfly group in registers. tw[t] = exp(-2 pi i t / M).
+// consecutive radix-2 stages fused per shared-memory pass (R <= 4, so M = 2048 takes three
+// passes): each work item keeps the 2^R elements i0 + t * 2^s of one butterfly group in
+// registers. tw[t] = exp(-2 pi i t / M).
 __device__ __forceinline__ float2 twiddle(const float2* __restrict__ tw, int x, int shift, bool inverse) {
   float2 w = tw[x << shift];
   if (inverse) w.y = -w.y;
@@ -401,8 +404,9 @@ __device__ __forceinline__ void dif_pass(float2* buf, int count, int logm, int s
 
 __device__ void fft_dit(float2* buf, int count, int logm, const float2* __restrict__ tw, bool inverse) {
   for (int s = 0; s < logm;) {
-    const int r = min(3, logm - s);
-    if (r == 3) dit_pass<3>(buf, count, logm, s, tw, inverse);
+    const int r = min(4, logm - s);
+    if (r == 4) dit_pass<4>(buf, count, logm, s, tw, inverse);
+    else if (r == 3) dit_pass<3>(buf, count, logm, s, tw, inverse);
     else if (r == 2) dit_pass<2>(buf, count, logm, s, tw, inverse);
     else dit_pass<1>(buf, count, logm, s, tw, inverse);
     __syncthreads();
@@ -412,9 +416,10 @@ __device__ void fft_dit(float2* buf, int count, int logm, const float2* __restri
 
 __device__ void fft_dif(float2* buf, int count, int logm, const float2* __restrict__ tw, bool inverse) {
   for (int top = logm - 1; top >= 0;) {
-    const int r = min(3, top + 1);
+    const int r = min(4, top + 1);
     const int s = top - r + 1;
-    if (r == 3) dif_pass<3>(buf, count, logm, s, tw, inverse);
+    if (r == 4) dif_pass<4>(buf, count, logm, s, tw, inverse);
+    else if (r == 3) dif_pass<3>(buf, count, logm, s, tw, inverse);
     else if (r == 2) dif_pass<2>(buf, count, logm, s, tw, inverse);
     else dif_pass<1>(buf, count, logm, s, tw, inverse);
     __syncthreads();
@@ -431,7 +436,7 @@ __device__ void fft_dif(float2* buf, int count, int logm, const float2* __restri
 // Blocks [nodes, 2 nodes): kernel row dy = r - nodes -> forward FFT of (q + i q^2), all M
 // spectral positions kept.
 // blockIdx.y selects the instance members[blockIdx.y] of the grid class.
-__global__ void __launch_bounds__(kFftThreads)
+__global__ void __launch_bounds__(kFftThreads, 4)
 rows_forward_kernel(const TsneInstance* __restrict__ inst, const int* __restrict__ members, int grid, int nodes,
                     int logm, const float2* __restrict__ tw, const GridState* __restrict__ cur,
                     float2* __restrict__ rows, float2* __restrict__ krows) {
@@ -549,7 +554,7 @@ columns_convolve_kernel(float2* __restrict__ rows, const float2* __restrict__ kr
 
 // Inverse row pass -> potentials (phi_q2, phi_x, phi_y) per node; block 0 also finalises
 // Z = sum_k |F_mass|^2 Kq / M^2 - n (the reference's sum_i q_grid(y_i) - n).
-__global__ void __launch_bounds__(kFftThreads)
+__global__ void __launch_bounds__(kFftThreads, 4)
 rows_inverse_kernel(const float2* __restrict__ rows, const TsneInstance* __restrict__ inst,
                     const int* __restrict__ members, int grid, int nodes, int logm, const float2* __restrict__ tw,
                     const double* __restrict__ zpart, int zblocks, GridState* __restrict__ cur) {
