@@ -225,12 +225,19 @@ def run_gpu(args):
     d_idx = idx.T.contiguous()
     d_dist = dist.T.contiguous()
     init = S.tsne_init(n)
+    torch.cuda.synchronize()
+    t_setup = time.perf_counter()
     plan = api.TsnePlan(d_idx, d_dist, n, K, PERPLEXITY, init=init)
+    setup_s = time.perf_counter() - t_setup  # validation, bisection, symmetrised P, state (synchronous)
     info = plan.info()
     lr = n / 12.0
-    # untimed early-exaggeration phase, as in a real run, then the warm-up steps: at least two
-    # 25-iteration chunks, so that the timed chunks' CUDA graph is captured before timing
+    # the early-exaggeration phase, as in a real run (timed apart, CUDA graph captures included),
+    # then the warm-up steps: at least two 25-iteration chunks, so that the timed chunks' CUDA
+    # graph is captured before timing
+    t_early = time.perf_counter()
     plan.run(250, 12.0, lr)
+    plan.synchronize()
+    early_s = time.perf_counter() - t_early
     plan.run(max(args.warmup, 50), 1.0, lr)
     plan.synchronize()
 
@@ -342,6 +349,8 @@ def run_gpu(args):
                    "parallelism": f"replicas x{world}"},
         "clocks": clk, "e2e": e2e, "roofline": roofline, "gpu_launches": launches,
         "stage_ms_per_step": {k_: v / args.steps for k_, v in prof.items()},
+        "setup": {"affinities_and_state_s": setup_s, "early_phase_ms_per_iter": early_s * 1e3 / 250,
+                  "note": "device KNN -> P and optimizer state; 250 early-exaggeration iterations incl. graph capture"},
     }
     if kl is not None:
         line["kl_after_run"] = kl

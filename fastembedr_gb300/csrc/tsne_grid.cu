@@ -326,9 +326,10 @@ __device__ __forceinline__ int sidx(int i) { return i + (i >> 4); }
 __host__ __device__ constexpr int padded(int count) { return count + count / 16; }
 
 // Radix-2 FFTs over `count` sequences of length M = 2^logm stored at buf + seq * M, with R
-// consecutive radix-2 stages fused per shared-memory pass (R <= 4, so M = 2048 takes three
-// passes): each work item keeps the 2^R elements i0 + t * 2^s of one butterfly group in
-// registers. tw[t] = exp(-2 pi i t / M).
+// consecutive radix-2 stages fused per shared-memory pass (R <= MAXR <= 4; with 4, M = 2048 takes
+// three passes): each work item keeps the 2^R elements i0 + t * 2^s of one butterfly group in
+// registers. tw[t] = exp(-2 pi i t / M). The forward row pass uses MAXR = 3: its kernel-row blocks
+// transform one sequence, whose 128 radix-16 work items would leave half of 256 threads idle.
 __device__ __forceinline__ float2 twiddle(const float2* __restrict__ tw, int x, int shift, bool inverse) {
   float2 w = tw[x << shift];
   if (inverse) w.y = -w.y;
@@ -402,9 +403,10 @@ __device__ __forceinline__ void dif_pass(float2* buf, int count, int logm, int s
   }
 }
 
+template <int MAXR = 4>
 __device__ void fft_dit(float2* buf, int count, int logm, const float2* __restrict__ tw, bool inverse) {
   for (int s = 0; s < logm;) {
-    const int r = min(4, logm - s);
+    const int r = min(MAXR, logm - s);
     if (r == 4) dit_pass<4>(buf, count, logm, s, tw, inverse);
     else if (r == 3) dit_pass<3>(buf, count, logm, s, tw, inverse);
     else if (r == 2) dit_pass<2>(buf, count, logm, s, tw, inverse);
@@ -414,9 +416,10 @@ __device__ void fft_dit(float2* buf, int count, int logm, const float2* __restri
   }
 }
 
+template <int MAXR = 4>
 __device__ void fft_dif(float2* buf, int count, int logm, const float2* __restrict__ tw, bool inverse) {
   for (int top = logm - 1; top >= 0;) {
-    const int r = min(4, top + 1);
+    const int r = min(MAXR, top + 1);
     const int s = top - r + 1;
     if (r == 4) dif_pass<4>(buf, count, logm, s, tw, inverse);
     else if (r == 3) dif_pass<3>(buf, count, logm, s, tw, inverse);
@@ -436,7 +439,7 @@ __device__ void fft_dif(float2* buf, int count, int logm, const float2* __restri
 // Blocks [nodes, 2 nodes): kernel row dy = r - nodes -> forward FFT of (q + i q^2), all M
 // spectral positions kept.
 // blockIdx.y selects the instance members[blockIdx.y] of the grid class.
-__global__ void __launch_bounds__(kFftThreads, 4)
+__global__ void __launch_bounds__(kFftThreads)
 rows_forward_kernel(const TsneInstance* __restrict__ inst, const int* __restrict__ members, int grid, int nodes,
                     int logm, const float2* __restrict__ tw, const GridState* __restrict__ cur,
                     float2* __restrict__ rows, float2* __restrict__ krows) {
@@ -462,7 +465,7 @@ rows_forward_kernel(const TsneInstance* __restrict__ inst, const int* __restrict
       sbuf[sidx(m + c)] = b;
     }
     __syncthreads();
-    fft_dif(sbuf, 2, logm, tw, false);
+    fft_dif<3>(sbuf, 2, logm, tw, false);
     float2* outa = rows + (long long)r * m;
     float2* outb = rows + (long long)(nodes + r) * m;
     for (int c = threadIdx.x; c < m; c += blockDim.x) {
@@ -485,7 +488,7 @@ rows_forward_kernel(const TsneInstance* __restrict__ inst, const int* __restrict
       sbuf[sidx(c)] = v;
     }
     __syncthreads();
-    fft_dif(sbuf, 1, logm, tw, false);
+    fft_dif<3>(sbuf, 1, logm, tw, false);
     float2* out = krows + (long long)kr * m;
     for (int c = threadIdx.x; c < m; c += blockDim.x) out[c] = sbuf[sidx(c)];
   }
