@@ -76,6 +76,7 @@ SIGNATURES = {
     "fastembedr_tsne_plan_gradient_check": (I, [vp, vp, I, F, vp, vp, vp, C.POINTER(D), C.POINTER(D)]),
     "fastembedr_tsne_plan_destroy": (None, [vp]),
     "fastembedr_tsne_batch_create": (I, [I, vp, vp, vp, vp, I, F, I, I, I, U, C.POINTER(vp)]),
+    "fastembedr_tsne_batch_create_rows": (I, [I, vp, vp, vp, vp, I, F, I, I, I, U, C.POINTER(vp)]),
     "fastembedr_tsne_batch_run": (I, [vp, I, I, F, F, F, F, F, F, F]),
     "fastembedr_tsne_batch_iterate": (I, [vp, I, F, F, F, F, F]),
     "fastembedr_tsne_batch_synchronize": (I, [vp]),

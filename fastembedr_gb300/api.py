@@ -315,18 +315,18 @@ class TsneBatch:
             raise ValueError("every instance needs the same number of neighbours")
         self.k = ks.pop()
         self.sizes = np.array([np.asarray(i).shape[0] for i, _ in knns], np.int32)
-        offs = {knn_index_offset(i) for i, _ in knns}
-        off = 1 if offs == {1} else 0
-        idx, dist = _concat_knn(knns)
-        init = None
-        if inits is not None:
-            init = np.concatenate([np.ascontiguousarray(y, np.float32).ravel() for y in inits])
+        # one row-major array per instance, passed by pointer (no concatenated copy); each
+        # instance's 0- or 1-based labels are detected on the device
+        idx = [np.ascontiguousarray(i, np.int32) for i, _ in knns]
+        dist = [np.ascontiguousarray(d, np.float32) for _, d in knns]
+        ys = None if inits is None else [np.ascontiguousarray(y, np.float32) for y in inits]
+        ptrs = lambda arrs: (C.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
         self.lib = _lib.require_gpu()
         self.h = C.c_void_p()
-        st = self.lib.fastembedr_tsne_batch_create(len(knns), self.sizes.ctypes.data, idx.ctypes.data,
-                                                   dist.ctypes.data, None if init is None else init.ctypes.data,
-                                                   self.k, float(perplexity), off, int(grid_size), int(interpolation),
-                                                   int(seed) & 0xFFFFFFFF, C.byref(self.h))
+        st = self.lib.fastembedr_tsne_batch_create_rows(len(knns), self.sizes.ctypes.data, ptrs(idx), ptrs(dist),
+                                                        None if ys is None else ptrs(ys), self.k, float(perplexity),
+                                                        -1, int(grid_size), int(interpolation),
+                                                        int(seed) & 0xFFFFFFFF, C.byref(self.h))
         _lib.check(st, "t-SNE batch create")
 
     @property

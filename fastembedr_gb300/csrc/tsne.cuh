@@ -2,6 +2,8 @@
 // repulsion, fused update, C ABI). Device pointers only; the stream is explicit.
 #pragma once
 
+#include <vector>
+
 #include "common.cuh"
 
 namespace fe {
@@ -31,6 +33,12 @@ void row_probabilities(const int* d_idx, const float* d_dist, int n, int k, floa
 // column, sum duplicates in double and fill the CSR (allocated inside `out`).
 void symmetrise(const int* d_idx, const float* d_p, int n, int k, int offset, DeviceCsr& out,
                 cudaStream_t s);
+// The same for a batch: instance b owns rows [first[b], first[b + 1]) (first = {0, ..., n}); columns
+// of d_idx (minus offset) are global rows and stay inside their instance. Each instance's values
+// are normalised by its own total, summed in the order symmetrise uses for one instance, so an
+// instance's P equals the P it gets alone. totals (may be null) receives the instance totals.
+void symmetrise_batch(const int* d_idx, const float* d_p, int n, int k, int offset, const std::vector<int>& first,
+                      DeviceCsr& out, std::vector<double>* totals, cudaStream_t s);
 
 // Device-wide exclusive scan of n int32 counts into n + 1 int64 offsets (out[n] = total);
 // tmp holds ceil(n / 1024) int64 values.

@@ -18,6 +18,7 @@
 #include <climits>
 #include <cmath>
 #include <cstdlib>
+#include <vector>
 
 #include "sort.cuh"
 #include "tsne.cuh"
@@ -389,11 +390,14 @@ sort_unique_big_rows_kernel(unsigned long long* __restrict__ bucket, const long 
   }
 }
 
-// Deterministic total: one block, fixed assignment and fixed tree.
-__global__ void total_mass_kernel(const double* __restrict__ row_mass, int n, double* out_total, float* out_norm) {
+// Deterministic totals: block b sums the rows [first[b], first[b + 1]) of instance b with a
+// fixed assignment and a fixed tree (a single instance is first = {0, n}).
+__global__ void total_mass_kernel(const double* __restrict__ row_mass, const int* __restrict__ first,
+                                  double* __restrict__ out_total, float* __restrict__ out_norm) {
   __shared__ double part[1024];
+  const int r0 = first[blockIdx.x], r1 = first[blockIdx.x + 1];
   double s = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) s += row_mass[i];
+  for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) s += row_mass[i];
   part[threadIdx.x] = s;
   __syncthreads();
   for (int w = blockDim.x / 2; w > 0; w >>= 1) {
@@ -402,20 +406,27 @@ __global__ void total_mass_kernel(const double* __restrict__ row_mass, int n, do
   }
   if (threadIdx.x == 0) {
     const double total = 0.5 * part[0];  // every pair sum appears in both of its rows
-    *out_total = total;
-    *out_norm = (float)(0.5 / total);
+    out_total[blockIdx.x] = total;
+    out_norm[blockIdx.x] = (float)(0.5 / total);
   }
 }
 
 __global__ void fill_csr_kernel(const unsigned long long* __restrict__ bucket, const long long* __restrict__ offs,
-                                const long long* __restrict__ row_ptr64, int n, const float* __restrict__ norm,
-                                int* __restrict__ row_ptr, int* __restrict__ col, float* __restrict__ val) {
+                                const long long* __restrict__ row_ptr64, int n, const int* __restrict__ first,
+                                int ninst, const float* __restrict__ norm, int* __restrict__ row_ptr,
+                                int* __restrict__ col, float* __restrict__ val) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp > n) return;
   if (lane == 0) row_ptr[warp] = (int)row_ptr64[warp];
   if (warp == n) return;
-  const float nm = *norm;
+  int lo = 0, hi = ninst - 1;  // the instance holding this row
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (first[mid] <= warp) lo = mid;
+    else hi = mid - 1;
+  }
+  const float nm = norm[lo];
   const long long src = offs[warp];
   const long long dst = row_ptr64[warp];
   const int cnt = (int)(row_ptr64[warp + 1] - dst);
@@ -427,6 +438,13 @@ __global__ void fill_csr_kernel(const unsigned long long* __restrict__ bucket, c
 }
 
 void symmetrise(const int* d_idx, const float* d_p, int n, int k, int offset, DeviceCsr& out, cudaStream_t s) {
+  symmetrise_batch(d_idx, d_p, n, k, offset, std::vector<int>{0, n}, out, nullptr, s);
+}
+
+void symmetrise_batch(const int* d_idx, const float* d_p, int n, int k, int offset, const std::vector<int>& first,
+                      DeviceCsr& out, std::vector<double>* totals, cudaStream_t s) {
+  const int ninst = (int)first.size() - 1;
+  if (ninst < 1 || first.front() != 0 || first.back() != n) throw Error("invalid t-SNE instance boundaries");
   const long long directed = (long long)n * k;
   const int nscan = std::max(1, ceil_div(n, kScanBlock));
   int* counts = nullptr;
@@ -441,6 +459,7 @@ void symmetrise(const int* d_idx, const float* d_p, int n, int k, int offset, De
   long long* row_ptr64 = nullptr;
   double* d_total = nullptr;
   float* d_norm = nullptr;
+  int* d_first = nullptr;
   Arena work;
   work.reserve(&counts, n);
   work.reserve(&offs, n + 1);
@@ -452,9 +471,11 @@ void symmetrise(const int* d_idx, const float* d_p, int n, int k, int offset, De
   work.reserve(&big_rows, n);
   work.reserve(&big_count, 1);
   work.reserve(&row_ptr64, n + 1);
-  work.reserve(&d_total, 1);
-  work.reserve(&d_norm, 1);
+  work.reserve(&d_total, ninst);
+  work.reserve(&d_norm, ninst);
+  work.reserve(&d_first, ninst + 1);
   work.commit("t-SNE symmetrisation workspace");
+  FE_CUDA(cudaMemcpyAsync(d_first, first.data(), sizeof(int) * (ninst + 1), cudaMemcpyHostToDevice, s));
 
   const int grid = std::max(1, std::min(ceil_div(directed, 256), sm_count() * 16));
   FE_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * n, s));
@@ -474,17 +495,24 @@ void symmetrise(const int* d_idx, const float* d_p, int n, int k, int offset, De
   sort_unique_big_rows_kernel<<<sm_count(), 1024, 0, s>>>(bucket, offs, big_rows, big_count, ucount, row_mass);
   FE_LAUNCH("sort_unique_big_rows_kernel");
   exclusive_scan(ucount, row_ptr64, n, scan_tmp, s);
-  total_mass_kernel<<<1, 1024, 0, s>>>(row_mass, n, d_total, d_norm);
+  total_mass_kernel<<<ninst, 1024, 0, s>>>(row_mass, d_first, d_total, d_norm);
   FE_LAUNCH("total_mass_kernel");
 
-  long long nnz = 0;
-  double total = 0.0;
-  FE_CUDA(cudaMemcpyAsync(&nnz, row_ptr64 + n, sizeof(long long), cudaMemcpyDeviceToHost, s));
-  FE_CUDA(cudaMemcpyAsync(&total, d_total, sizeof(double), cudaMemcpyDeviceToHost, s));
+  std::vector<double> tot(ninst);
+  std::vector<long long> bounds(ninst + 1);
+  for (int b = 0; b <= ninst; ++b)
+    FE_CUDA(cudaMemcpyAsync(&bounds[b], row_ptr64 + first[b], sizeof(long long), cudaMemcpyDeviceToHost, s));
+  FE_CUDA(cudaMemcpyAsync(tot.data(), d_total, sizeof(double) * ninst, cudaMemcpyDeviceToHost, s));
   FE_CUDA(cudaStreamSynchronize(s));
-  if (nnz <= 0) throw Error("KNN graph produced no non-self t-SNE edges.");
+  const long long nnz = bounds[ninst];
+  double total = 0.0;
+  for (int b = 0; b < ninst; ++b) {
+    if (bounds[b + 1] <= bounds[b]) throw Error("KNN graph produced no non-self t-SNE edges.");
+    if (!std::isfinite(tot[b]) || tot[b] <= 0.0) throw Error("t-SNE probability normalization failed.");
+    total += tot[b];
+  }
   if (nnz > INT_MAX) throw Error("symmetrised t-SNE graph exceeds 2^31 - 1 entries.");
-  if (!std::isfinite(total) || total <= 0.0) throw Error("t-SNE probability normalization failed.");
+  if (totals) *totals = tot;
 
   out.n = n;
   out.nnz = nnz;
@@ -494,8 +522,8 @@ void symmetrise(const int* d_idx, const float* d_p, int n, int k, int offset, De
   out.arena.reserve(&out.col, nnz);
   out.arena.reserve(&out.val, nnz);
   out.arena.commit("t-SNE CSR");
-  fill_csr_kernel<<<ceil_div((long long)(n + 1) * 32, 256), 256, 0, s>>>(bucket, offs, row_ptr64, n, d_norm,
-                                                                          out.row_ptr, out.col, out.val);
+  fill_csr_kernel<<<ceil_div((long long)(n + 1) * 32, 256), 256, 0, s>>>(bucket, offs, row_ptr64, n, d_first, ninst,
+                                                                          d_norm, out.row_ptr, out.col, out.val);
   FE_LAUNCH("fill_csr_kernel");
   FE_CUDA(cudaStreamSynchronize(s));
 }

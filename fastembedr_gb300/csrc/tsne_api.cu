@@ -50,15 +50,44 @@ bool graph_capture_enabled() {
            std::strcmp(env, "no") == 0 || std::strcmp(env, "NO") == 0);
 }
 
-// Append one instance's CSR to the batch CSR: rows shifted by the instance's nnz offset, columns
-// by its first slot; the last instance's end offset closes row_ptr.
-__global__ void append_csr_kernel(const int* __restrict__ rp, const int* __restrict__ col, int n, long long nnz,
-                                  int nnz_off, int first, int* __restrict__ rp_out, int* __restrict__ col_out) {
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t <= n; t += stride)
-    rp_out[t] = nnz_off + rp[t];
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nnz; t += stride)
-    col_out[t] = col[t] + first;
+// Smallest and largest label of a KNN block (knn_index_offset's test on the device).
+__global__ void label_range_kernel(const int* __restrict__ idx, long long total, int* __restrict__ range) {
+  int lo = INT_MAX, hi = INT_MIN;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    lo = min(lo, idx[t]);
+    hi = max(hi, idx[t]);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(range, lo);
+    atomicMax(range + 1, hi);
+  }
+}
+
+// One instance's nb x k KNN (column-major, or row-major) into the batch's column-major n x k matrix at rows
+// [first, first + nb), neighbour labels turned into global 0-based rows.
+__global__ void globalize_knn_kernel(const int* __restrict__ idx, const float* __restrict__ dist, int nb, int k,
+                                     int offset, int row_major, int first, int n, int* __restrict__ idx_out,
+                                     float* __restrict__ dist_out) {
+  const long long total = (long long)nb * k;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    long long i, j;
+    if (row_major) {
+      i = t / k;
+      j = t - i * k;
+    } else {
+      j = t / nb;
+      i = t - j * nb;
+    }
+    const long long o = j * n + first + i;
+    idx_out[o] = idx[t] - offset + first;
+    dist_out[o] = dist[t];
+  }
 }
 
 // out[r] = full[inv[rows[r]]] for the two float2 force fields of a diagnostic.
@@ -159,11 +188,29 @@ struct TsneJob {
 
   // Batch: instances in table order (equal grids consecutive); `user` maps table position to
   // the caller's instance index. KNN / init are the caller's host arrays, instance after
-  // instance. P of every instance is built on its own and appended to one CSR whose rows and
-  // columns are offset by the instance's first slot.
+  // instance. The instances' KNN are placed in one matrix with global labels and P is built for
+  // all of them at once; every instance keeps its own normalisation (symmetrise_batch), so its
+  // rows of P equal the P it gets alone.
   std::vector<int> user, user_off;
   void prepare_batch(int ninst, const int* sizes, const int* idx_h, const float* dist_h, const float* init_h, int k,
                      float perplexity, int offset, int grid_size, int mode, unsigned seed) {
+    std::vector<const int*> iu(ninst);
+    std::vector<const float*> du(ninst), yu(init_h ? ninst : 0);
+    std::size_t at = 0;
+    for (int u = 0; u < ninst; ++u) {
+      iu[u] = idx_h + at * k;
+      du[u] = dist_h + at * k;
+      if (init_h) yu[u] = init_h + 2 * at;
+      at += (std::size_t)std::max(sizes[u], 0);
+    }
+    prepare_batch(ninst, sizes, iu, du, yu, false, k, perplexity, offset, grid_size, mode, seed);
+  }
+  // The same from one host pointer per instance (KNN column-major, or row-major n_b x k when
+  // row_major; init row-major n_b x 2 or none); offset < 0 detects each instance's 0- or 1-based
+  // labels on the device as knn_index_offset does.
+  void prepare_batch(int ninst, const int* sizes, const std::vector<const int*>& idx_u,
+                     const std::vector<const float*>& dist_u, const std::vector<const float*>& init_u,
+                     bool row_major, int k, float perplexity, int offset, int grid_size, int mode, unsigned seed) {
     cudaStream_t s = stream.s;
     std::vector<int> grid_u(ninst);
     user_off.assign(ninst + 1, 0);
@@ -188,53 +235,51 @@ struct TsneJob {
     }
     tsne_batch_alloc(D, sz, gr, lr, mode);
     const int n = D.n;
-    std::vector<std::unique_ptr<DeviceCsr>> parts(ninst);
-    long long total_nnz = 0;
-    double total_mass = 0.0;
+    std::vector<int> first(ninst + 1, 0);
+    for (int t = 0; t < ninst; ++t) first[t + 1] = first[t] + sz[t];
     {
-      int* d_idx = nullptr;
-      float* d_dist = nullptr;
-      float* d_p = nullptr;
+      // every instance's KNN into one column-major n x k matrix in table order, columns turned
+      // into global 0-based slots; then one bisection and one symmetrisation for the whole batch
+      const std::size_t items = (std::size_t)n * k;
+      int *d_loc_idx = nullptr, *d_idx = nullptr;
+      float *d_loc_dist = nullptr, *d_dist = nullptr, *d_p = nullptr;
       Arena tmp;
-      tmp.reserve(&d_idx, (std::size_t)max_n * k);
-      tmp.reserve(&d_dist, (std::size_t)max_n * k);
-      tmp.reserve(&d_p, (std::size_t)max_n * k);
+      tmp.reserve(&d_loc_idx, items);
+      tmp.reserve(&d_loc_dist, items);
+      tmp.reserve(&d_idx, items);
+      tmp.reserve(&d_dist, items);
+      tmp.reserve(&d_p, items);
       tmp.commit("t-SNE batch affinities");
+      int* d_range = nullptr;
+      Arena rng;
+      rng.reserve(&d_range, 2);
+      rng.commit("t-SNE batch label range");
       for (int t = 0; t < ninst; ++t) {
         const int u = user[t], nb = sz[t];
-        const std::size_t items = (std::size_t)nb * k, at = (std::size_t)user_off[u] * k;
-        FE_CUDA(cudaMemcpyAsync(d_idx, idx_h + at, sizeof(int) * items, cudaMemcpyHostToDevice, s));
-        FE_CUDA(cudaMemcpyAsync(d_dist, dist_h + at, sizeof(float) * items, cudaMemcpyHostToDevice, s));
-        validate_knn(d_idx, d_dist, nb, k, offset, s);
-        row_probabilities(d_idx, d_dist, nb, k, perplexity, d_p, nullptr, s);
-        parts[t] = std::make_unique<DeviceCsr>();
-        symmetrise(d_idx, d_p, nb, k, offset, *parts[t], s);
-        total_nnz += parts[t]->nnz;
-        total_mass += parts[t]->total_mass;
+        const std::size_t cnt = (std::size_t)nb * k;
+        const std::size_t loc = (std::size_t)first[t] * k;
+        FE_CUDA(cudaMemcpyAsync(d_loc_idx + loc, idx_u[u], sizeof(int) * cnt, cudaMemcpyHostToDevice, s));
+        FE_CUDA(cudaMemcpyAsync(d_loc_dist + loc, dist_u[u], sizeof(float) * cnt, cudaMemcpyHostToDevice, s));
+        const int blocks = std::max(1, std::min(ceil_div((long long)cnt, 256), sm_count() * 8));
+        int off = offset;
+        if (off < 0) {
+          const int init_range[2] = {INT_MAX, INT_MIN};
+          FE_CUDA(cudaMemcpyAsync(d_range, init_range, sizeof(init_range), cudaMemcpyHostToDevice, s));
+          label_range_kernel<<<blocks, 256, 0, s>>>(d_loc_idx + loc, (long long)cnt, d_range);
+          FE_LAUNCH("label_range_kernel");
+          int h_range[2] = {0, 0};
+          FE_CUDA(cudaMemcpyAsync(h_range, d_range, sizeof(h_range), cudaMemcpyDeviceToHost, s));
+          FE_CUDA(cudaStreamSynchronize(s));
+          off = (h_range[0] >= 1 && h_range[1] <= nb) ? 1 : 0;
+        }
+        validate_knn(d_loc_idx + loc, d_loc_dist + loc, nb, k, off, s);
+        globalize_knn_kernel<<<blocks, 256, 0, s>>>(d_loc_idx + loc, d_loc_dist + loc, nb, k, off, row_major ? 1 : 0,
+                                                    first[t], n, d_idx, d_dist);
+        FE_LAUNCH("globalize_knn_kernel");
       }
+      row_probabilities(d_idx, d_dist, n, k, perplexity, d_p, nullptr, s);
+      symmetrise_batch(d_idx, d_p, n, k, 0, first, P, nullptr, s);
     }
-    if (total_nnz > INT_MAX) throw Error("t-SNE batch: more than 2^31 affinities; split the batch");
-    P.n = n;
-    P.nnz = total_nnz;
-    P.total_mass = total_mass;
-    P.arena.release();
-    P.arena.reserve(&P.row_ptr, (std::size_t)n + 1);
-    P.arena.reserve(&P.col, (std::size_t)std::max<long long>(total_nnz, 1));
-    P.arena.reserve(&P.val, (std::size_t)std::max<long long>(total_nnz, 1));
-    P.arena.commit("t-SNE batch P");
-    long long nnz_off = 0;
-    for (int t = 0; t < ninst; ++t) {
-      const DeviceCsr& q = *parts[t];
-      const int first = D.inst[t].pt_begin;
-      append_csr_kernel<<<std::max(1, std::min(ceil_div(std::max<long long>(q.nnz, q.n + 1), 256), sm_count() * 8)),
-                          256, 0, s>>>(q.row_ptr, q.col, q.n, q.nnz, (int)nnz_off, first, P.row_ptr + first,
-                                       P.col + nnz_off);
-      FE_LAUNCH("append_csr_kernel");
-      FE_CUDA(cudaMemcpyAsync(P.val + nnz_off, q.val, sizeof(float) * q.nnz, cudaMemcpyDeviceToDevice, s));
-      nnz_off += q.nnz;
-    }
-    FE_CUDA(cudaStreamSynchronize(s));
-    parts.clear();
     reorder = reorder_enabled();
     float2* d_init = nullptr;
     Arena tmp;
@@ -243,9 +288,8 @@ struct TsneJob {
     for (int t = 0; t < ninst; ++t) {
       const int u = user[t];
       float2* dst = d_init + D.inst[t].pt_begin;
-      if (init_h) {
-        FE_CUDA(cudaMemcpyAsync(dst, init_h + 2 * (std::size_t)user_off[u], sizeof(float2) * sz[t],
-                                cudaMemcpyHostToDevice, s));
+      if (!init_u.empty()) {
+        FE_CUDA(cudaMemcpyAsync(dst, init_u[u], sizeof(float2) * sz[t], cudaMemcpyHostToDevice, s));
       } else {
         random_init_kernel<<<std::max(1, std::min(ceil_div(sz[t], 256), sm_count() * 8)), 256, 0, s>>>(dst, sz[t],
                                                                                                       seed);
@@ -794,6 +838,32 @@ int fastembedr_tsne_batch_create(int n_instances, const int* sizes, const int* i
     b->job.configure_adaptive(grid_size == -2);
     b->job.prepare_batch(n_instances, sizes, indices, distances, init, k, perplexity, index_offset, grid_size, mode,
                          seed);
+    *batch = b.release();
+  });
+}
+
+int fastembedr_tsne_batch_create_rows(int n_instances, const int* sizes, const int* const* indices,
+                                      const float* const* distances, const float* const* inits, int k,
+                                      float perplexity, int index_offset, int grid_size, int interpolation,
+                                      unsigned int seed, fastembedr_tsne_batch** batch) {
+  return fe::guarded([&] {
+    if (!sizes || !indices || !distances || !batch) throw fe::Error("null CUDA t-SNE batch pointer");
+    if (n_instances < 1 || k < 1 || k > 1024 || !(perplexity > 0.0f))
+      throw fe::Error("invalid CUDA t-SNE batch parameters");
+    if (grid_size > 0 && (grid_size < 8 || grid_size > 2048 || (grid_size & (grid_size - 1)) != 0))
+      throw fe::Error("`grid_size` must be a power of two between 8 and 2048.");
+    if (grid_size < -2)
+      throw fe::Error("`grid_size`: 0 (CUDA size policy), -1 (CPU size policy), -2 (adaptive) or a size");
+    std::vector<const int*> iu(indices, indices + n_instances);
+    std::vector<const float*> du(distances, distances + n_instances);
+    std::vector<const float*> yu;
+    if (inits) yu.assign(inits, inits + n_instances);
+    for (int u = 0; u < n_instances; ++u)
+      if (!iu[u] || !du[u] || (inits && !yu[u])) throw fe::Error("null CUDA t-SNE batch pointer");
+    const int mode = interpolation == 0 ? fe::kInterpBilinear : fe::kInterpLagrange3;
+    auto b = std::make_unique<fastembedr_tsne_batch>();
+    b->job.configure_adaptive(grid_size == -2);
+    b->job.prepare_batch(n_instances, sizes, iu, du, yu, true, k, perplexity, index_offset, grid_size, mode, seed);
     *batch = b.release();
   });
 }

@@ -373,6 +373,14 @@ typedef struct fastembedr_tsne_batch fastembedr_tsne_batch;
 int fastembedr_tsne_batch_create(int n_instances, const int* sizes, const int* indices, const float* distances,
                                  const float* init, int k, float perplexity, int index_offset, int grid_size,
                                  int interpolation, unsigned int seed, fastembedr_tsne_batch** batch);
+/* The same batch from one host pointer per instance, without a concatenated copy: indices[b] /
+ * distances[b] are ROW-major n_b x k (C order), inits[b] row-major n_b x 2 (inits may be NULL);
+ * index_offset < 0 detects each instance's 0- or 1-based labels on the device (min >= 1 and
+ * max <= n_b: 1-based, as knn_index_offset). */
+int fastembedr_tsne_batch_create_rows(int n_instances, const int* sizes, const int* const* indices,
+                                      const float* const* distances, const float* const* inits, int k,
+                                      float perplexity, int index_offset, int grid_size, int interpolation,
+                                      unsigned int seed, fastembedr_tsne_batch** batch);
 /* The two-phase schedule on every instance, returning when done. Instance b uses the learning
  * rate learning_rate x n_b in both phases; learning_rate <= 0 selects the package's opt-SNE
  * rate n_b / early_exaggeration (R/tsne_control.R:191-231). */

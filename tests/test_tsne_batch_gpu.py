@@ -46,6 +46,38 @@ def test_each_instance_matches_itself_alone():
     assert np.all(np.abs(kt - ka) <= 0.05 * ka) and abs(kt.mean() - ka.mean()) <= 0.02 * ka.mean(), (kt, ka)
 
 
+def test_mixed_label_bases_and_both_entry_points_agree():
+    """Instances may carry 0- or 1-based labels independently (each is detected on the device);
+    the concatenated column-major entry point and the per-instance row-major one give the same
+    first iteration."""
+    import ctypes as C
+
+    knns = _instances([400, 1500, 3000], seed=3)
+    mixed = [knns[0], (knns[1][0] + 1, knns[1][1]), knns[2]]
+    with api.TsneBatch(knns, perplexity=10.0, seed=7) as a:
+        a.iterate(1, 12.0, 1.0 / 12.0)
+        base = a.layouts()
+    with api.TsneBatch(mixed, perplexity=10.0, seed=7) as b:
+        b.iterate(1, 12.0, 1.0 / 12.0)
+        got = b.layouts()
+    lib = _lib.require_gpu()
+    sizes = np.array([i.shape[0] for i, _ in knns], np.int32)
+    idx = np.concatenate([np.asfortranarray(i.astype(np.int32)).ravel(order="F") for i, _ in knns])
+    dist = np.concatenate([np.asfortranarray(d.astype(np.float32)).ravel(order="F") for _, d in knns])
+    h = C.c_void_p()
+    _lib.check(lib.fastembedr_tsne_batch_create(3, sizes.ctypes.data, idx.ctypes.data, dist.ctypes.data, None, 30,
+                                                10.0, 0, 0, 0, 7, C.byref(h)), "column-major batch")
+    _lib.check(lib.fastembedr_tsne_batch_iterate(h, 1, 12.0, 1.0 / 12.0, 0.8, 0.01, 5.0), "iterate")
+    out = np.zeros((int(sizes.sum()), 2), np.float32)
+    _lib.check(lib.fastembedr_tsne_batch_layout(h, out.ctypes.data), "layout")
+    lib.fastembedr_tsne_batch_destroy(h)
+    cm = np.split(out, np.cumsum(sizes)[:-1])
+    for j in range(3):
+        scale = np.abs(base[j]).max()
+        assert np.abs(got[j] - base[j]).max() <= 1e-5 * scale
+        assert np.abs(cm[j] - base[j]).max() <= 1e-5 * scale
+
+
 def test_batch_matches_single_instance_path():
     """Against tsne_knn (one instance per call): KL averaged over the instances within 1% (a single
     run's KL moves by a few % with the float-atomic order alone, less in the mean), each instance
