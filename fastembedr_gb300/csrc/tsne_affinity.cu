@@ -56,116 +56,135 @@ void validate_knn(const int* d_idx, const float* d_dist, int n, int k, int offse
 }
 
 // ---------------------------------------------------------------- bisection
-// One warp per row. The CTA first stages a tile of `rows` rows x k columns of the
-// column-major distances in shared memory (each column read is `rows` consecutive floats),
-// then every warp bisects its rows out of shared memory.
-constexpr int kBisectWarps = 8;
+// One thread per row. The CTA stages its rows' distances (column-major in global memory, so
+// each column read is coalesced) in shared memory with a stride of k + 1 floats (consecutive rows
+// on distinct banks), next to each row's shifted squared distances s_j = d_j^2 - min d^2 (FP64,
+// rounded to float once). Every thread bisects its own row: per entry FP32 exp of -beta s_j and
+// compensated (Kahan) FP32 sums, whose error (~1e-7 relative) stays far inside the 1e-6 band
+// around the stop tolerance in which an iteration is re-evaluated from the distances with FP64
+// exp and FP64 sums; entropy, the update of beta and the stop test are FP64. The FP64 pipe of
+// this part is narrow, so the per-entry work stays on the FP32 pipe. The probabilities overwrite
+// the row's distances and the CTA stores them row-major with coalesced writes.
+constexpr int kBisectRows = 128;
 
-__global__ void __launch_bounds__(kBisectWarps * 32)
-row_probabilities_kernel(const float* __restrict__ dist, int n, int k, int rows,
-                         double log_perplexity, float* __restrict__ p_out,
-                         double* __restrict__ entropy_out) {
-  extern __shared__ float tile[];  // rows x k, row-major
+__global__ void __launch_bounds__(kBisectRows)
+row_probabilities_kernel(const float* __restrict__ dist, int n, int k, double log_perplexity,
+                         float* __restrict__ p_out, double* __restrict__ entropy_out) {
+  extern __shared__ float tile[];  // blockDim.x rows x (k + 1) distances, then as many s_j
+  const int rows = blockDim.x, stride = k + 1;
+  float* stile = tile + (long long)rows * stride;
   const int r0 = blockIdx.x * rows;
   const int nrows = min(rows, n - r0);
-  for (int t = threadIdx.x; t < rows * k; t += blockDim.x) {
-    const int rr = t % rows, j = t / rows;
-    if (rr < nrows) tile[rr * k + j] = dist[(long long)j * n + r0 + rr];
+  for (int t = threadIdx.x; t < nrows * k; t += rows) {
+    const int j = t / nrows, rr = t - j * nrows;
+    tile[rr * stride + j] = dist[(long long)j * n + r0 + rr];
   }
   __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int rr = warp; rr < nrows; rr += kBisectWarps) {
-    const float* d = tile + rr * k;
+  const int rr = threadIdx.x;
+  if (rr < nrows) {
+    float* d = tile + rr * stride;
     // zero-spread test in float arithmetic, as compute_row_probabilities_float does it
     float min_f = FLT_MAX, max_f = 0.0f;
     double min_d2 = DBL_MAX;
-    for (int j = lane; j < k; j += 32) {
+    for (int j = 0; j < k; ++j) {
       const float df = d[j] * d[j];
       min_f = fminf(min_f, df);
       max_f = fmaxf(max_f, df);
       const double dj = d[j];
       min_d2 = fmin(min_d2, dj * dj);  // exact: a float squared fits in a double
     }
-    min_f = warp_min(min_f);
-    max_f = warp_max(max_f);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) min_d2 = fmin(min_d2, __shfl_xor_sync(0xffffffffu, min_d2, o));
-    float* prow = p_out + (long long)(r0 + rr) * k;
+    double entropy_eval;
     if (max_f - min_f <= FLT_EPSILON * fmaxf(1.0f, max_f)) {
       const float u = 1.0f / (float)k;
-      for (int j = lane; j < k; j += 32) prow[j] = u;
-      if (entropy_out && lane == 0) entropy_out[r0 + rr] = log((double)k);
-      continue;
-    }
-    double beta = 1.0, beta_min = -DBL_MAX, beta_max = DBL_MAX;
-    double beta_eval = beta, sum_eval = 1.0, entropy_eval = 0.0;
-    bool exact_eval = false;
-    for (int it = 0; it < 200; ++it) {
-      double sp = 0.0, sw = 0.0;
-      for (int j = lane; j < k; j += 32) {
+      for (int j = 0; j < k; ++j) d[j] = u;
+      entropy_eval = log((double)k);
+    } else {
+      float* sf = stile + rr * stride;
+      for (int j = 0; j < k; ++j) {
         const double dj = d[j];
-        const double s = dj * dj - min_d2;
-        const double p = (double)expf((float)(-beta * s));
-        sp += p;
-        sw += s * p;
+        sf[j] = (float)(dj * dj - min_d2);
       }
-      sp = warp_sum(sp);
-      sw = warp_sum(sw);
-      double entropy = beta * sw / sp + log(sp);
-      double diff = entropy - log_perplexity;
-      exact_eval = false;
-      // The stop test is the only decision FP32 exp can flip: re-evaluate near its boundary
-      // with FP64 exp so the bisection follows the FP64 path.
-      if (fabs(fabs(diff) - 1e-5) < 1e-6) {
-        sp = 0.0;
-        sw = 0.0;
-        for (int j = lane; j < k; j += 32) {
-          const double dj = d[j];
-          const double s = dj * dj - min_d2;
-          const double p = exp(-beta * s);
-          sp += p;
-          sw += s * p;
+      double beta = 1.0, beta_min = -DBL_MAX, beta_max = DBL_MAX;
+      double beta_eval = beta, sum_eval = 1.0;
+      bool exact_eval = false;
+      entropy_eval = 0.0;
+      for (int it = 0; it < 200; ++it) {
+        const float nb = (float)(-beta);
+        float ps = 0.0f, pc = 0.0f, ws = 0.0f, wc = 0.0f;
+        for (int j = 0; j < k; ++j) {
+          const float sj = sf[j];
+          const float p = expf(nb * sj);
+          const float yp = p - pc;
+          const float tp = ps + yp;
+          pc = (tp - ps) - yp;
+          ps = tp;
+          const float yw = sj * p - wc;
+          const float tw = ws + yw;
+          wc = (tw - ws) - yw;
+          ws = tw;
         }
-        sp = warp_sum(sp);
-        sw = warp_sum(sw);
-        entropy = beta * sw / sp + log(sp);
-        diff = entropy - log_perplexity;
-        exact_eval = true;
+        double sp = (double)ps - (double)pc;
+        double sw = (double)ws - (double)wc;
+        double entropy = beta * sw / sp + log(sp);
+        double diff = entropy - log_perplexity;
+        exact_eval = false;
+        // The stop test is the only decision FP32 exp can flip: re-evaluate near its boundary
+        // with FP64 exp so the bisection follows the FP64 path.
+        if (fabs(fabs(diff) - 1e-5) < 1e-6) {
+          sp = 0.0;
+          sw = 0.0;
+          for (int j = 0; j < k; ++j) {
+            const double dj = d[j];
+            const double s = dj * dj - min_d2;
+            const double p = exp(-beta * s);
+            sp += p;
+            sw += s * p;
+          }
+          entropy = beta * sw / sp + log(sp);
+          diff = entropy - log_perplexity;
+          exact_eval = true;
+        }
+        beta_eval = beta;
+        sum_eval = sp;
+        entropy_eval = entropy;
+        if (fabs(diff) < 1e-5) break;
+        if (diff > 0.0) {
+          beta_min = beta;
+          beta = (beta_max == DBL_MAX) ? beta * 2.0 : 0.5 * (beta + beta_max);
+        } else {
+          beta_max = beta;
+          beta = (beta_min == -DBL_MAX) ? beta * 0.5 : 0.5 * (beta + beta_min);
+        }
+        if (!isfinite(beta)) break;
       }
-      beta_eval = beta;
-      sum_eval = sp;
-      entropy_eval = entropy;
-      if (fabs(diff) < 1e-5) break;
-      if (diff > 0.0) {
-        beta_min = beta;
-        beta = (beta_max == DBL_MAX) ? beta * 2.0 : 0.5 * (beta + beta_max);
-      } else {
-        beta_max = beta;
-        beta = (beta_min == -DBL_MAX) ? beta * 0.5 : 0.5 * (beta + beta_min);
+      const double inv = 1.0 / sum_eval;
+      const float nb = (float)(-beta_eval);
+      for (int j = 0; j < k; ++j) {
+        const double dj = d[j];
+        const double p = exact_eval ? exp(-beta_eval * (dj * dj - min_d2)) : (double)expf(nb * sf[j]);
+        d[j] = (float)(p * inv);
       }
-      if (!isfinite(beta)) break;
     }
-    const double inv = 1.0 / sum_eval;
-    for (int j = lane; j < k; j += 32) {
-      const double dj = d[j];
-      const double s = dj * dj - min_d2;
-      const double p = exact_eval ? exp(-beta_eval * s) : (double)expf((float)(-beta_eval * s));
-      prow[j] = (float)(p * inv);
-    }
-    if (entropy_out && lane == 0) entropy_out[r0 + rr] = entropy_eval;
+    if (entropy_out) entropy_out[r0 + rr] = entropy_eval;
+  }
+  __syncthreads();
+  float* out = p_out + (long long)r0 * k;
+  for (int t = threadIdx.x; t < nrows * k; t += rows) {
+    const int q = t / k, j = t - q * k;
+    out[t] = tile[q * stride + j];
   }
 }
 
 void row_probabilities(const int* /*d_idx*/, const float* d_dist, int n, int k, float perplexity,
                        float* d_p, double* d_entropy, cudaStream_t s) {
-  int rows = 32;
-  while (rows > 1 && (std::size_t)rows * k * sizeof(float) > 96 * 1024) rows >>= 1;
-  const std::size_t smem = (std::size_t)rows * k * sizeof(float);
+  int rows = kBisectRows;
+  while (rows > 1 && (std::size_t)rows * (k + 1) * 2 * sizeof(float) > 112 * 1024) rows >>= 1;
+  const std::size_t smem = (std::size_t)rows * (k + 1) * 2 * sizeof(float);
   if (smem > 48 * 1024)
     FE_CUDA(cudaFuncSetAttribute(row_probabilities_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem));
-  row_probabilities_kernel<<<ceil_div(n, rows), kBisectWarps * 32, smem, s>>>(
-      d_dist, n, k, rows, std::log((double)perplexity), d_p, d_entropy);
+  row_probabilities_kernel<<<ceil_div(n, rows), rows, smem, s>>>(d_dist, n, k, std::log((double)perplexity), d_p,
+                                                                 d_entropy);
   FE_LAUNCH("row_probabilities_kernel");
 }
 
@@ -292,18 +311,98 @@ __global__ void fill_buckets_kernel(const int* __restrict__ idx, const float* __
 constexpr int kSortThreads = 256;
 constexpr int kSortCap = 8192;  // entries of a row sorted in shared memory
 
-// Sort each row bucket by (column, p bits); rows above kSortCap are queued for the
-// global-memory path. Then collapse runs of equal columns: the compacted (column, float(sum))
-// entries are written back to the start of the bucket, `ucount` gets the unique count and
-// `row_mass` the double sum of the row's pair sums.
+// Sort each row bucket by (column, p bits), then collapse runs of equal columns: the compacted
+// (column, float(sum)) entries are written back to the start of the bucket, `ucount` gets the
+// unique count and `row_mass` the double sum of the row's pair sums. Rows of up to 256 entries
+// (nearly all) take one warp each (sort_unique_small_rows_kernel); longer rows are listed for a
+// CTA each (this kernel), and rows above kSortCap for the global-memory path.
+constexpr int kWarpSortCap = 256;
+constexpr int kWarpSortWarps = 8;
+
+// One warp per row of at most kWarpSortCap entries: the same ascending bitonic network in the
+// warp's slice of shared memory, then the run sums and the row mass with exactly the arithmetic
+// of the CTA path for such a row (thread t of 256 owning position t: each run summed in order by
+// its first position, warp sums over positions 32w .. 32w + 31, added for w = 0 .. 7), so the
+// result does not depend on which kernel took the row.
+__global__ void __launch_bounds__(kWarpSortWarps * 32)
+sort_unique_small_rows_kernel(unsigned long long* __restrict__ bucket, const long long* __restrict__ offs, int n,
+                              int* __restrict__ ucount, double* __restrict__ row_mass, int* __restrict__ mid_rows,
+                              int* __restrict__ mid_count) {
+  __shared__ unsigned long long sm[kWarpSortWarps][kWarpSortCap];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  unsigned long long* a = sm[wib];
+  const int warps = gridDim.x * kWarpSortWarps;
+  for (int row = blockIdx.x * kWarpSortWarps + wib; row < n; row += warps) {
+    const long long b = offs[row];
+    const int len = (int)(offs[row + 1] - b);
+    if (len > kWarpSortCap) {
+      if (lane == 0) mid_rows[atomicAdd(mid_count, 1)] = row;
+      continue;
+    }
+    int pw = 1;
+    while (pw < len) pw <<= 1;
+    for (int t = lane; t < pw; t += 32) a[t] = t < len ? bucket[b + t] : ~0ull;
+    __syncwarp();
+    for (int size = 2; size <= pw && len > 1; size <<= 1) {
+      const int half = size >> 1;
+      for (int t = lane; t < pw / 2; t += 32) {
+        const int blk = t / half, off = t % half;
+        const int i = blk * size + off, j = blk * size + size - 1 - off;
+        const unsigned long long x = a[i], y = a[j];
+        if (y < x) {
+          a[i] = y;
+          a[j] = x;
+        }
+      }
+      __syncwarp();
+      for (int stride = half >> 1; stride > 0; stride >>= 1) {
+        for (int t = lane; t < pw / 2; t += 32) {
+          const int blk = t / stride, off = t % stride;
+          const int i = blk * 2 * stride + off, j = i + stride;
+          const unsigned long long x = a[i], y = a[j];
+          if (y < x) {
+            a[i] = y;
+            a[j] = x;
+          }
+        }
+        __syncwarp();
+      }
+    }
+    int cnt = 0;
+    double tot = 0.0;
+    for (int w = 0; w < kWarpSortCap / 32; ++w) {
+      const int t = w * 32 + lane;
+      bool start = false;
+      if (t < len) start = (t == 0) || ((a[t] >> 32) != (a[t - 1] >> 32));
+      const unsigned ballot = __ballot_sync(0xffffffffu, start);
+      double sum = 0.0;
+      if (start) {
+        const unsigned col = (unsigned)(a[t] >> 32);
+        for (int u = t; u < len && (unsigned)(a[u] >> 32) == col; ++u) sum += (double)__uint_as_float((unsigned)a[u]);
+        const int pos = cnt + __popc(ballot & ((1u << lane) - 1u));
+        bucket[b + pos] = ((unsigned long long)col << 32) | (unsigned long long)__float_as_uint((float)sum);
+      }
+      cnt += __popc(ballot);
+      tot += warp_sum(sum);
+    }
+    if (lane == 0) {
+      row_mass[row] = tot;
+      ucount[row] = cnt;
+    }
+    __syncwarp();
+  }
+}
+
 __global__ void __launch_bounds__(kSortThreads)
-sort_unique_rows_kernel(unsigned long long* __restrict__ bucket, const long long* __restrict__ offs, int n,
-                        int* __restrict__ ucount, double* __restrict__ row_mass, int* __restrict__ big_rows,
-                        int* __restrict__ big_count) {
+sort_unique_rows_kernel(unsigned long long* __restrict__ bucket, const long long* __restrict__ offs,
+                        const int* __restrict__ rows, const int* __restrict__ row_count, int* __restrict__ ucount,
+                        double* __restrict__ row_mass, int* __restrict__ big_rows, int* __restrict__ big_count) {
   extern __shared__ unsigned long long sm[];
   __shared__ int warp_cnt[kSortThreads / 32];
   __shared__ double warp_mass[kSortThreads / 32];
-  for (int row = blockIdx.x; row < n; row += gridDim.x) {
+  const int count = *row_count;
+  for (int q = blockIdx.x; q < count; q += gridDim.x) {
+    const int row = rows[q];
     const long long b = offs[row];
     const int len = (int)(offs[row + 1] - b);
     if (len > kSortCap) {
@@ -456,6 +555,8 @@ void symmetrise_batch(const int* d_idx, const float* d_p, int n, int k, int offs
   double* row_mass = nullptr;
   int* big_rows = nullptr;
   int* big_count = nullptr;
+  int* mid_rows = nullptr;
+  int* mid_count = nullptr;
   long long* row_ptr64 = nullptr;
   double* d_total = nullptr;
   float* d_norm = nullptr;
@@ -470,6 +571,8 @@ void symmetrise_batch(const int* d_idx, const float* d_p, int n, int k, int offs
   work.reserve(&row_mass, n);
   work.reserve(&big_rows, n);
   work.reserve(&big_count, 1);
+  work.reserve(&mid_rows, n);
+  work.reserve(&mid_count, 1);
   work.reserve(&row_ptr64, n + 1);
   work.reserve(&d_total, ninst);
   work.reserve(&d_norm, ninst);
@@ -487,10 +590,14 @@ void symmetrise_batch(const int* d_idx, const float* d_p, int n, int k, int offs
   fill_buckets_kernel<<<grid, 256, 0, s>>>(d_idx, d_p, n, k, offset, cursor, bucket);
   FE_LAUNCH("fill_buckets_kernel");
 
+  FE_CUDA(cudaMemsetAsync(mid_count, 0, sizeof(int), s));
+  sort_unique_small_rows_kernel<<<std::max(1, std::min(ceil_div(n, kWarpSortWarps), sm_count() * 8)),
+                                  kWarpSortWarps * 32, 0, s>>>(bucket, offs, n, ucount, row_mass, mid_rows, mid_count);
+  FE_LAUNCH("sort_unique_small_rows_kernel");
   const std::size_t smem = kSortCap * sizeof(unsigned long long);
   FE_CUDA(cudaFuncSetAttribute(sort_unique_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  sort_unique_rows_kernel<<<std::min(n, sm_count() * 8), kSortThreads, smem, s>>>(bucket, offs, n, ucount,
-                                                                                  row_mass, big_rows, big_count);
+  sort_unique_rows_kernel<<<sm_count() * 3, kSortThreads, smem, s>>>(bucket, offs, mid_rows, mid_count, ucount,
+                                                                     row_mass, big_rows, big_count);
   FE_LAUNCH("sort_unique_rows_kernel");
   sort_unique_big_rows_kernel<<<sm_count(), 1024, 0, s>>>(bucket, offs, big_rows, big_count, ucount, row_mass);
   FE_LAUNCH("sort_unique_big_rows_kernel");
