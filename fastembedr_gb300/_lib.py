@@ -64,6 +64,7 @@ SIGNATURES = {
     "fastembedr_cuda_umap_spectral_init_csr": (I, [vp, vp, vp, I, I, D, I, vp]),
     "fastembedr_cuda_umap_knn_spectral": (I, [vp, vp, I, I, I, I, I, F, F, F, I, D, U, vp]),
     "fastembedr_umap_find_ab_params": (None, [D, D, C.POINTER(D), C.POINTER(D)]),
+    "fastembedr_host_normal_stream_check": (I, []),
     "fastembedr_cuda_opentsne_fft_from_device_knn_float_pca_double": (I, [vp, vp, vp, I, I, I, I, F, I, I, F, F, F, I,
                                                                        F, F, F, F, U, I, vp]),
     "fastembedr_cuda_opentsne_fft_from_device_knn_float_pca_float": (I, [vp, vp, vp, I, I, I, I, F, I, I, F, F, F, I,

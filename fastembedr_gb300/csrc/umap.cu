@@ -19,6 +19,7 @@
 #include <cfloat>
 #include <climits>
 #include <cmath>
+#include <future>
 #include <map>
 #include <memory>
 #include <type_traits>
@@ -52,48 +53,31 @@ __global__ void umap_distance_sum_kernel(const float* __restrict__ dist, long lo
   }
 }
 
-// One warp per row; distances column-major n x k.
-__global__ void umap_smooth_knn_kernel(const float* __restrict__ dist, int n, int k, const double* __restrict__ acc,
-                                       float* __restrict__ sigmas, float* __restrict__ rhos) {
-  const int lane = threadIdx.x & 31;
-  const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (row >= n) return;
-  const unsigned long long cnt = reinterpret_cast<const unsigned long long*>(acc)[1];
-  const double global_mean = cnt > 0 ? acc[0] / (double)cnt : 1.0;
-  const double target = log2((double)k);
-  double rho = INFINITY, row_sum = 0.0;
-  int row_count = 0;
-  for (int j = lane; j < k; j += 32) {
-    const float d = dist[(long long)j * n + row];
-    if (!isfinite(d)) continue;
-    if (d >= 0.0f) {
-      row_sum += (double)d;
-      ++row_count;
-    }
-    if (d > 0.0f && (double)d < rho) rho = (double)d;
+constexpr int kSmoothRows = 128;
+
+// Membership sum of one row at sigma, in the reference's order and FP64 arithmetic
+// (smooth_knn_dist's membership_sum, src/fast_knn_umap.cpp:924-934).
+__device__ double smooth_psum_exact(const float* __restrict__ d, int k, double rho, double sigma) {
+  const double safe = fmax(sigma, 1.0e-12);
+  double psum = 0.0;
+  for (int j = 0; j < k; ++j) {
+    const float raw = d[j];
+    if (!isfinite(raw)) continue;
+    const double x = (double)raw - rho;
+    psum += x <= 0.0 ? 1.0 : exp(-x / safe);
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    rho = fmin(rho, __shfl_xor_sync(0xffffffffu, rho, o));
-    row_sum += __shfl_xor_sync(0xffffffffu, row_sum, o);
-    row_count += __shfl_xor_sync(0xffffffffu, row_count, o);
-  }
-  if (!isfinite(rho)) rho = 0.0;
-  double sigma = 1.0, sigma_best = 1.0, best_diff = DBL_MAX, lo = 0.0, hi = DBL_MAX;
+  return psum;
+}
+
+// The reference's sigma search for one row (:961-985) in FP64 throughout.
+__device__ double smooth_sigma_exact(const float* __restrict__ d, int k, double rho, double target) {
+  double sigma = 1.0, best = 1.0, best_diff = DBL_MAX, lo = 0.0, hi = DBL_MAX;
   for (int it = 0; it < 64; ++it) {
-    const double safe = fmax(sigma, 1.0e-12);
-    double psum = 0.0;
-    for (int j = lane; j < k; j += 32) {
-      const float raw = dist[(long long)j * n + row];
-      if (!isfinite(raw)) continue;
-      const double d = (double)raw - rho;
-      psum += d <= 0.0 ? 1.0 : exp(-d / safe);
-    }
-    psum = warp_sum(psum);
+    const double psum = smooth_psum_exact(d, k, rho, sigma);
     const double diff = fabs(psum - target);
     if (diff < best_diff) {
       best_diff = diff;
-      sigma_best = sigma;
+      best = sigma;
     }
     if (psum > target) {
       hi = sigma;
@@ -104,13 +88,110 @@ __global__ void umap_smooth_knn_kernel(const float* __restrict__ dist, int n, in
     }
     if (diff < 1.0e-5) break;
   }
-  if (lane == 0) {
-    const double row_mean = row_count > 0 ? row_sum / (double)row_count : global_mean;
-    const double floor_s = 1.0e-3 * (rho > 0.0 ? row_mean : global_mean);
-    sigma_best = fmax(sigma_best, floor_s);
-    rhos[row] = (float)rho;
-    sigmas[row] = (float)fmax(sigma_best, 1.0e-12);
+  return best;
+}
+
+// smooth_knn_dist (:876-996), one thread per row; distances column-major n x k, staged through
+// shared memory (blockDim.x rows x (k + 1) raw distances, then as many positive offsets d - rho).
+// The search runs its membership sums on the FP32 pipe: exp of float offsets times a float
+// 1/sigma, Kahan-summed. Each FP32 term is within 2e-7 of the FP64 term and the Kahan sum adds
+// at most 1.2e-7 per unit of the total, so |psum32 - psum64| < 4e-7 k. The decisions of the
+// search are the sign of psum - target and the stop test |psum - target| < 1e-5; an FP32 sum
+// farther than that margin from the stop boundary takes both as FP64 would (a sum inside the
+// stop band stops either way), and one inside the margin is re-evaluated in FP64. The FP64
+// search keeps the sigma of the smallest |psum - target|, which at a stop is the stopping sigma
+// (every earlier difference was >= 1e-5), so the result is the FP64 search's. A row that does not
+// stop within 64 steps is searched again in FP64 from the start.
+__global__ void __launch_bounds__(kSmoothRows)
+umap_smooth_knn_kernel(const float* __restrict__ dist, int n, int k, const double* __restrict__ acc,
+                       float* __restrict__ sigmas, float* __restrict__ rhos) {
+  extern __shared__ float s_tile[];
+  const int rows = blockDim.x, stride = k + 1;
+  float* s_off = s_tile + (long long)rows * stride;
+  const int r0 = blockIdx.x * rows;
+  const int nrows = min(rows, n - r0);
+  for (int t = threadIdx.x; t < nrows * k; t += rows) {
+    const int j = t / nrows, rr = t - j * nrows;
+    s_tile[rr * stride + j] = dist[(long long)j * n + r0 + rr];
   }
+  __syncthreads();
+  const int rr = threadIdx.x;
+  if (rr >= nrows) return;
+  const float* d = s_tile + rr * stride;
+  float* off = s_off + rr * stride;
+  const unsigned long long cnt = reinterpret_cast<const unsigned long long*>(acc)[1];
+  const double global_mean = cnt > 0 ? acc[0] / (double)cnt : 1.0;
+  const double target = log2((double)k);
+  double rho = INFINITY, row_sum = 0.0;
+  int row_count = 0;
+  for (int j = 0; j < k; ++j) {
+    const float v = d[j];
+    if (!isfinite(v)) continue;
+    if (v >= 0.0f) {
+      row_sum += (double)v;
+      ++row_count;
+    }
+    if (v > 0.0f && (double)v < rho) rho = (double)v;
+  }
+  if (!isfinite(rho)) rho = 0.0;
+  // finite entries at or below rho contribute exactly 1; the others their float offset, which
+  // is positive (the difference of two distinct floats does not round to zero in FP32)
+  int ones = 0, m = 0;
+  for (int j = 0; j < k; ++j) {
+    const float v = d[j];
+    if (!isfinite(v)) continue;
+    const double x = (double)v - rho;
+    if (x <= 0.0) ++ones;
+    else off[m++] = (float)x;
+  }
+  const double margin = 4.0e-7 * (double)k;
+  double sigma = 1.0, best = 1.0, lo = 0.0, hi = DBL_MAX;
+  bool stopped = false;
+  for (int it = 0; it < 64; ++it) {
+    const float inv = (float)(1.0 / fmax(sigma, 1.0e-12));
+    float ps = (float)ones, pc = 0.0f;
+    for (int j = 0; j < m; ++j) {
+      const float y = expf(-off[j] * inv) - pc;
+      const float t = ps + y;
+      pc = (t - ps) - y;
+      ps = t;
+    }
+    double psum = (double)ps - (double)pc;
+    double diff = fabs(psum - target);
+    if (fabs(diff - 1.0e-5) < margin) {
+      psum = smooth_psum_exact(d, k, rho, sigma);
+      diff = fabs(psum - target);
+    }
+    if (diff < 1.0e-5) {
+      best = sigma;
+      stopped = true;
+      break;
+    }
+    if (psum > target) {
+      hi = sigma;
+      sigma = 0.5 * (lo + hi);
+    } else {
+      lo = sigma;
+      sigma = hi == DBL_MAX ? sigma * 2.0 : 0.5 * (lo + hi);
+    }
+  }
+  if (!stopped) best = smooth_sigma_exact(d, k, rho, target);
+  const double row_mean = row_count > 0 ? row_sum / (double)row_count : global_mean;
+  const double floor_s = 1.0e-3 * (rho > 0.0 ? row_mean : global_mean);
+  best = fmax(best, floor_s);
+  rhos[r0 + rr] = (float)rho;
+  sigmas[r0 + rr] = (float)fmax(best, 1.0e-12);
+}
+
+void smooth_knn(const float* d_dist, int n, int k, const double* acc, float* sig, float* rho, cudaStream_t s) {
+  int rows = kSmoothRows;
+  while (rows > 1 && (std::size_t)rows * (k + 1) * 2 * sizeof(float) > 96 * 1024) rows >>= 1;
+  const std::size_t smem = (std::size_t)rows * (k + 1) * 2 * sizeof(float);
+  if (smem > 200 * 1024) throw Error("k is too large for the UMAP smooth-kNN search (at most 25,000 neighbours)");
+  if (smem > 48 * 1024)
+    FE_CUDA(cudaFuncSetAttribute(umap_smooth_knn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  umap_smooth_knn_kernel<<<ceil_div(n, rows), rows, smem, s>>>(d_dist, n, k, acc, sig, rho);
+  FE_LAUNCH("umap_smooth_knn_kernel");
 }
 
 // ---------------------------------------------------------------- fuzzy union graph
@@ -343,8 +424,7 @@ void umap_build_graph(const int* d_idx, const float* d_dist, int n, int k, int o
   FE_CUDA(cudaMemsetAsync(big_count, 0, sizeof(int), s));
   umap_distance_sum_kernel<<<grid, 256, 0, s>>>(d_dist, directed, acc);
   FE_LAUNCH("umap_distance_sum_kernel");
-  umap_smooth_knn_kernel<<<ceil_div((long long)n * 32, 256), 256, 0, s>>>(d_dist, n, k, acc, sig, rho);
-  FE_LAUNCH("umap_smooth_knn_kernel");
+  smooth_knn(d_dist, n, k, acc, sig, rho, s);
   umap_count_kernel<<<grid, 256, 0, s>>>(d_idx, d_dist, sig, rho, n, k, offset, counts);
   FE_LAUNCH("umap_count_kernel");
   exclusive_scan(counts, offs, n, scan_tmp, s);
@@ -836,7 +916,15 @@ __global__ void umap_start_to_layout_kernel(const double* __restrict__ emb, int 
 // null (n_epochs must be 0 when y_out is).
 void umap_knn_spectral_job(const int* d_idx, const float* d_dist, int n, int k, int offset, int n_epochs, int nsr,
                            float lr, float min_dist, float rep, int spectral_n_iter, double init_scale,
-                           unsigned seed, double* emb_out, float* y_out) {
+                           unsigned seed, double* emb_out, float* y_out,
+                           std::future<SpectralDraws>* early = nullptr) {
+  // the start's host draws (started by the caller before its input copies, or here) run while
+  // the GPU validates the KNN and builds the graph
+  std::future<SpectralDraws> own;
+  if (!early) {
+    own = std::async(std::launch::async, spectral_draws, n, (int)seed);
+    early = &own;
+  }
   UmapJob job;
   job.alloc(n);
   cudaStream_t s = job.stream.s;
@@ -844,11 +932,13 @@ void umap_knn_spectral_job(const int* d_idx, const float* d_dist, int n, int k, 
   validate_knn(d_idx, d_dist, n, k, offset, s);
   UmapGraph g;
   umap_build_graph(d_idx, d_dist, n, k, offset, g, s);
+  SpectralDraws pre = early->get();
   double* emb = nullptr;
   Arena a;
   a.reserve(&emb, 2 * (std::size_t)n);
   a.commit("UMAP spectral start output");
-  umap_spectral_start(g.offsets, g.neighbors, g.weights, n, g.nnz, spectral_n_iter, init_scale, (int)seed, emb, s);
+  umap_spectral_start(g.offsets, g.neighbors, g.weights, n, g.nnz, spectral_n_iter, init_scale, (int)seed, emb, s,
+                      &pre);
   if (emb_out) FE_CUDA(cudaMemcpyAsync(emb_out, emb, sizeof(double) * 2 * (std::size_t)n, cudaMemcpyDeviceToHost, s));
   if (y_out) {
     umap_start_to_layout_kernel<<<std::max(1, std::min(ceil_div(n, 256), sm_count() * 8)), 256, 0, s>>>(emb, n,
@@ -1129,6 +1219,7 @@ int fastembedr_cuda_umap_spectral_init_from_knn(const int* indices, const float*
   return fe::guarded([&] {
     if (!indices || !distances || !out) throw fe::Error("null host pointer");
     if (n < 2 || k < 1 || spectral_n_iter < 1) throw fe::Error("invalid spectral initialization parameters");
+    auto draws = std::async(std::launch::async, fe::spectral_draws, n, seed);
     fe::Stream st;
     const std::size_t items = (std::size_t)n * k;
     int* d_idx = nullptr;
@@ -1141,7 +1232,7 @@ int fastembedr_cuda_umap_spectral_init_from_knn(const int* indices, const float*
     FE_CUDA(cudaMemcpyAsync(d_dist, distances, sizeof(float) * items, cudaMemcpyHostToDevice, st.s));
     FE_CUDA(cudaStreamSynchronize(st.s));
     fe::umap_knn_spectral_job(d_idx, d_dist, n, k, index_offset, 0, 0, 1.0f, 0.01f, 1.0f, spectral_n_iter,
-                              init_scale, (unsigned)seed, out, nullptr);
+                              init_scale, (unsigned)seed, out, nullptr, &draws);
   });
 }
 
@@ -1214,6 +1305,7 @@ int fastembedr_cuda_umap_knn_spectral(const int* indices, const float* distances
     if (n < 2 || k < 1 || n_epochs < 1 || negative_sample_rate < 0 || !(learning_rate > 0.0f) || min_dist < 0.0f ||
         !(repulsion_strength > 0.0f) || spectral_n_iter < 1)
       throw fe::Error("invalid CUDA UMAP parameters");
+    auto draws = std::async(std::launch::async, fe::spectral_draws, n, (int)seed);
     fe::Stream st;
     const std::size_t items = (std::size_t)n * k;
     int* d_idx = nullptr;
@@ -1226,7 +1318,7 @@ int fastembedr_cuda_umap_knn_spectral(const int* indices, const float* distances
     FE_CUDA(cudaMemcpyAsync(d_dist, distances, sizeof(float) * items, cudaMemcpyHostToDevice, st.s));
     FE_CUDA(cudaStreamSynchronize(st.s));
     fe::umap_knn_spectral_job(d_idx, d_dist, n, k, index_offset, n_epochs, negative_sample_rate, learning_rate,
-                              min_dist, repulsion_strength, spectral_n_iter, init_scale, seed, nullptr, out);
+                              min_dist, repulsion_strength, spectral_n_iter, init_scale, seed, nullptr, out, &draws);
   });
 }
 

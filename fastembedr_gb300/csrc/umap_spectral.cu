@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <future>
 #include <random>
 #include <vector>
 
@@ -39,7 +40,16 @@ __device__ double sum_partials(const double* __restrict__ part, int count) {
   __shared__ double s_total;
   if (threadIdx.x < 32) {
     double s = 0.0;
-    for (int b = threadIdx.x; b < count; b += 32) s = __dadd_rn(s, part[b]);
+    int b = threadIdx.x;
+    // the lane's partials in order; eight loads are issued before their adds
+    for (; b + 7 * 32 < count; b += 8 * 32) {
+      double v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v[u] = part[b + u * 32];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) s = __dadd_rn(s, v[u]);
+    }
+    for (; b < count; b += 32) s = __dadd_rn(s, part[b]);
     s = warp_sum(s);
     if (threadIdx.x == 0) s_total = s;
   }
@@ -72,20 +82,28 @@ __global__ void sp_degree_kernel(const int* __restrict__ offsets, const float* _
   }
 }
 
-// nw[p] = float(w / sqrt(max(deg_r deg_j, 1e-24))); triv[r] = sqrt(max(deg_r, 0)); partials of
-// sum triv^2. One thread per row, grid-stride with a fixed row-to-block assignment.
+// nw[p] = float(w / sqrt(max(deg_r deg_j, 1e-24))): one warp per row, lanes over its entries.
 __global__ void __launch_bounds__(kSpThreads)
 sp_adjacency_kernel(const int* __restrict__ offsets, const int* __restrict__ nb, const float* __restrict__ w,
-                    const float* __restrict__ deg, int n, float* __restrict__ nw, double* __restrict__ triv,
-                    double* __restrict__ part) {
-  double acc = 0.0;
-  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+                    const float* __restrict__ deg, int n, float* __restrict__ nw) {
+  const int lane = threadIdx.x & 31;
+  const int warps = gridDim.x * (blockDim.x >> 5);
+  for (int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < n; r += warps) {
     const double dr = (double)deg[r];
-    for (int p = offsets[r]; p < offsets[r + 1]; ++p) {
+    for (int p = offsets[r] + lane; p < offsets[r + 1]; p += 32) {
       const double den = __dsqrt_rn(fmax(__dmul_rn(dr, (double)deg[nb[p]]), 1e-24));
       nw[p] = (float)__ddiv_rn((double)w[p], den);
     }
-    const double t = __dsqrt_rn(fmax(dr, 0.0));
+  }
+}
+
+// triv[r] = sqrt(max(deg_r, 0)); block partials of sum triv^2 (one thread per row, grid-stride
+// with a fixed row-to-block assignment).
+__global__ void __launch_bounds__(kSpThreads)
+sp_trivial_kernel(const float* __restrict__ deg, int n, double* __restrict__ triv, double* __restrict__ part) {
+  double acc = 0.0;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    const double t = __dsqrt_rn(fmax((double)deg[r], 0.0));
     triv[r] = t;
     acc = __dadd_rn(acc, __dmul_rn(t, t));
   }
@@ -101,21 +119,40 @@ __global__ void sp_normalise_trivial_kernel(double* __restrict__ triv, int n, co
 
 // Gram-Schmidt steps. A column whose norm vanished sets *flag to its index; the later steps of
 // the same pass see the flag and do nothing, and the host redraws that column and resumes.
+//
+// Block partials of m[:, c] . triv for columns from..B-1 (part + c * nparts): the first
+// projection of every column, which the earlier columns do not change.
 __global__ void __launch_bounds__(kSpThreads)
-gs_dot_kernel(const double* __restrict__ a, const double* __restrict__ b, int n, double* __restrict__ part,
-              const int* __restrict__ flag) {
+gs_trivial_dots_kernel(const double* __restrict__ m, const double* __restrict__ triv, int n, int from, int B,
+                       double* __restrict__ part, const int* __restrict__ flag) {
   if (*flag >= 0) return;
-  double acc = 0.0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    acc = __dadd_rn(acc, __dmul_rn(a[i], b[i]));
-  block_partial(acc, part);
+  for (int c = from; c < B; ++c) {
+    const double* qc = m + (long long)c * n;
+    double acc = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+      acc = __dadd_rn(acc, __dmul_rn(qc[i], triv[i]));
+    block_partial(acc, part + (long long)c * gridDim.x);
+    __syncthreads();
+  }
 }
 
-// qc -= (sum of part_in) * u; then partials of sum qc * v (v may be qc)
+// Optionally first finish column `prev` (prev >= 0): divide it by the root of the sum of
+// prev_part, or flag it as vanished. Then qc -= (sum of part_in) * u and partials of sum qc * v
+// (v may be qc).
 __global__ void __launch_bounds__(kSpThreads)
 gs_sub_dot_kernel(double* qc, const double* __restrict__ u, const double* __restrict__ part_in, int nparts,
-                  const double* v, int n, double* __restrict__ part_out, const int* __restrict__ flag) {
+                  const double* v, int n, double* __restrict__ part_out, double* prev_col,
+                  const double* __restrict__ prev_part, int prev, int* __restrict__ flag) {
   if (*flag >= 0) return;
+  if (prev >= 0) {
+    const double nrm = __dsqrt_rn(sum_partials(prev_part, nparts));
+    if (nrm < 1e-10) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) *flag = prev;
+      return;
+    }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+      prev_col[i] = __ddiv_rn(prev_col[i], nrm);
+  }
   const double d = sum_partials(part_in, nparts);
   double acc = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -138,24 +175,51 @@ __global__ void gs_scale_kernel(double* __restrict__ qc, const double* __restric
     qc[i] = __ddiv_rn(qc[i], nrm);
 }
 
-// y[:, c] = A x[:, c] for the B columns; one thread per row, neighbours in CSR order.
-__global__ void sp_multiply_kernel(const int* __restrict__ offsets, const int* __restrict__ nb,
-                                   const float* __restrict__ nw, int n, int B, const double* __restrict__ x,
-                                   double* __restrict__ y) {
-  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
-    double s[kSpBlock];
-#pragma unroll
-    for (int c = 0; c < kSpBlock; ++c) s[c] = 0.0;
-    for (int p = offsets[r]; p < offsets[r + 1]; ++p) {
-      const double w = (double)nw[p];
-      const long long j = nb[p];
-#pragma unroll
-      for (int c = 0; c < kSpBlock; ++c)
-        if (c < B) s[c] = __dadd_rn(s[c], __dmul_rn(w, x[(long long)c * n + j]));
+// y[:, c] = A x[:, c] for the B columns. A warp works on four rows at once, eight lanes per row
+// (lane = 8 * slot + column): per group of 8 entries of its row the slot's lanes load the
+// entries' neighbours and weights (one each, the next group's loads issued ahead), pass them
+// round by shuffles, and every lane gathers its column's 8 values and adds the products in CSR
+// order. Each (row, column) sum is the sequential FP64 sum of the row, and all 32 lanes of a
+// warp instruction on the FP64 pipe carry work.
+__global__ void __launch_bounds__(kSpThreads)
+sp_multiply_kernel(const int* __restrict__ offsets, const int* __restrict__ nb, const float* __restrict__ nw,
+                   int n, int B, const double* __restrict__ x, double* __restrict__ y) {
+  const int lane = threadIdx.x & 31, slot = lane >> 3, c = lane & 7;
+  const unsigned gmask = 0xffu << (slot * 8);
+  const int slots = gridDim.x * (blockDim.x >> 5) * 4;
+  const double* xc = x + (long long)(c < B ? c : 0) * n;
+  for (int r = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 4 + slot; r < n; r += slots) {
+    const int p0 = offsets[r], p1 = offsets[r + 1];
+    double acc = 0.0;
+    int j = 0;
+    double w = 0.0;
+    if (p0 + c < p1) {
+      j = nb[p0 + c];
+      w = (double)nw[p0 + c];
     }
+    for (int base = p0; base < p1; base += 8) {
+      const int cnt = min(8, p1 - base);
+      int jn = 0;
+      double wn = 0.0;
+      if (base + 8 + c < p1) {
+        jn = nb[base + 8 + c];
+        wn = (double)nw[base + 8 + c];
+      }
+      double v[8];
 #pragma unroll
-    for (int c = 0; c < kSpBlock; ++c)
-      if (c < B) y[(long long)c * n + r] = s[c];
+      for (int t = 0; t < 8; ++t) {
+        const int jt = __shfl_sync(gmask, j, t, 8);
+        v[t] = t < cnt ? xc[jt] : 0.0;
+      }
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const double wt = __shfl_sync(gmask, w, t, 8);
+        if (t < cnt) acc = __dadd_rn(acc, __dmul_rn(wt, v[t]));
+      }
+      j = jn;
+      w = wn;
+    }
+    if (c < B) y[(long long)c * n + r] = acc;
   }
 }
 
@@ -194,15 +258,31 @@ sp_project_kernel(const double* __restrict__ q, const double* __restrict__ z, in
 // 80, each on the largest off-diagonal entry), Ritz values sorted descending; coef[c * 8 + b]
 // = component c's coefficients on the basis.
 __global__ void sp_ritz_kernel(const double* __restrict__ part, int nparts, int B, double* __restrict__ coef) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  __shared__ double s_pair[kSpPairs];
+  if (blockIdx.x != 0) return;
+  if ((int)threadIdx.x < kSpPairs) {
+    // entry t of the upper triangle: its block partials in block order, loads issued ahead
+    const int t = threadIdx.x;
+    double s = 0.0;
+    int k = 0;
+    for (; k + 7 < nparts; k += 8) {
+      double v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v[u] = part[(long long)(k + u) * kSpPairs + t];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) s = __dadd_rn(s, v[u]);
+    }
+    for (; k < nparts; ++k) s = __dadd_rn(s, part[(long long)k * kSpPairs + t]);
+    s_pair[t] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
   double P[kSpBlock][kSpBlock], V[kSpBlock][kSpBlock];
   int t = 0;
   for (int a = 0; a < kSpBlock; ++a)
     for (int b = a; b < kSpBlock; ++b, ++t) {
-      double s = 0.0;
-      for (int k = 0; k < nparts; ++k) s = __dadd_rn(s, part[(long long)k * kSpPairs + t]);
-      P[a][b] = s;
-      P[b][a] = s;
+      P[a][b] = s_pair[t];
+      P[b][a] = s_pair[t];
     }
   for (int i = 0; i < kSpBlock; ++i)
     for (int j = 0; j < kSpBlock; ++j) V[i][j] = i == j ? 1.0 : 0.0;
@@ -352,15 +432,33 @@ __global__ void sp_rescale_kernel(double* __restrict__ col, int n, const double*
 
 }  // namespace
 
+SpectralDraws spectral_draws(int n, int seed) {
+  SpectralDraws d;
+  d.rng.seed((std::uint32_t)seed);
+  const int B = std::min(n - 1, kSpBlock);
+  if (B < 2) return d;
+  d.block.resize((std::size_t)n * B);
+  d.normal.fill(d.rng, d.block.data(), d.block.size(), 10000.0);
+  d.jitter = std::async(std::launch::async, [ahead = d.rng, n]() mutable {
+               NormalStream jitter(0.0, 1e-4);
+               std::vector<double> v(2 * (std::size_t)n);
+               jitter.fill(ahead, v.data(), v.size(), 1.0);
+               return v;
+             }).share();
+  return d;
+}
+
 void umap_spectral_start(const int* offsets, const int* neighbors, const float* weights, int n, long long nnz,
-                         int spectral_n_iter, double init_scale, int seed, double* out, cudaStream_t s) {
+                         int spectral_n_iter, double init_scale, int seed, double* out, cudaStream_t s,
+                         SpectralDraws* pre) {
   if (n < 1 || spectral_n_iter < 1) throw Error("invalid spectral initialization parameters");
   std::mt19937 rng((std::uint32_t)seed);
-  std::normal_distribution<double> normal(0.0, 0.0001);
   std::uniform_real_distribution<double> uniform(-10.0, 10.0);
   const int B = std::min(n - 1, kSpBlock);
   const int nb = sp_blocks(n);
   const int gb = std::max(1, std::min(ceil_div(n, kSpThreads), sm_count() * 8));
+  const int gw = std::max(1, std::min(ceil_div(n, kSpThreads / 32), sm_count() * 8));  // warp per row
+  const int gm = std::max(1, std::min(ceil_div(n, kSpThreads / 8), sm_count() * 8));   // 8 lanes per row
   std::vector<double> host;
   if (nnz < 1 || B < 2) {
     // the reference's fallback: uniform(-10, 10) coordinates, column after column
@@ -387,38 +485,55 @@ void umap_spectral_start(const int* offsets, const int* neighbors, const float* 
     w.commit("UMAP spectral start");
     sp_degree_kernel<<<gb, kSpThreads, 0, s>>>(offsets, weights, n, deg);
     FE_LAUNCH("sp_degree_kernel");
-    sp_adjacency_kernel<<<nb, kSpThreads, 0, s>>>(offsets, neighbors, weights, deg, n, nw, triv, pa);
+    sp_adjacency_kernel<<<gw, kSpThreads, 0, s>>>(offsets, neighbors, weights, deg, n, nw);
     FE_LAUNCH("sp_adjacency_kernel");
+    sp_trivial_kernel<<<nb, kSpThreads, 0, s>>>(deg, n, triv, pa);
+    FE_LAUNCH("sp_trivial_kernel");
     sp_normalise_trivial_kernel<<<gb, kSpThreads, 0, s>>>(triv, n, pa, nb);
     FE_LAUNCH("sp_normalise_trivial_kernel");
     FE_CUDA(cudaMemsetAsync(flag, 0xff, sizeof(int), s));  // -1: no vanished column
+    SpectralDraws local;
+    SpectralDraws* dr = pre;
+    if (!dr || dr->block.size() != (std::size_t)n * B) {
+      local = spectral_draws(n, seed);
+      dr = &local;
+    }
+    bool redrawn = false;
 
     // column c of the block in `m`, orthonormalised from column `from` on; the host redraws a
     // vanished column from the stream and resumes there
     auto orthonormalise = [&](double* m, int from) {
       for (;;) {
+        // every column's projection on the trivial vector first (pa), then per column the
+        // projections on the earlier columns; a column is divided by its norm inside the next
+        // column's first step
+        gs_trivial_dots_kernel<<<nb, kSpThreads, 0, s>>>(m, triv, n, from, B, pa, flag);
+        FE_LAUNCH("gs_trivial_dots_kernel");
+        double* in = pb;
+        double* outp = pc;
         for (int c = from; c < B; ++c) {
           double* qc = m + (std::size_t)c * n;
-          double* in = pb;
-          double* outp = pc;
-          gs_dot_kernel<<<nb, kSpThreads, 0, s>>>(qc, triv, n, in, flag);
-          FE_LAUNCH("gs_dot_kernel");
           for (int j = 0; j <= c; ++j) {
             const double* u = j == 0 ? triv : m + (std::size_t)(j - 1) * n;
             const double* v = j < c ? m + (std::size_t)j * n : qc;
-            gs_sub_dot_kernel<<<nb, kSpThreads, 0, s>>>(qc, u, in, nb, v, n, outp, flag);
+            const double* pin = j == 0 ? pa + (std::size_t)c * nb : in;
+            const int prev = j == 0 && c > from ? c - 1 : -1;
+            gs_sub_dot_kernel<<<nb, kSpThreads, 0, s>>>(qc, u, pin, nb, v, n, outp,
+                                                        prev >= 0 ? m + (std::size_t)prev * n : nullptr, in, prev,
+                                                        flag);
             FE_LAUNCH("gs_sub_dot_kernel");
             std::swap(in, outp);
           }
-          gs_scale_kernel<<<nb, kSpThreads, 0, s>>>(qc, in, nb, n, c, flag);
-          FE_LAUNCH("gs_scale_kernel");
         }
+        gs_scale_kernel<<<nb, kSpThreads, 0, s>>>(m + (std::size_t)(B - 1) * n, in, nb, n, B - 1, flag);
+        FE_LAUNCH("gs_scale_kernel");
         int f = -1;
         FE_CUDA(cudaMemcpyAsync(&f, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
         FE_CUDA(cudaStreamSynchronize(s));
         if (f < 0) return;
+        redrawn = true;
         host.resize(n);
-        for (double& v : host) v = normal(rng) * 10000.0;
+        dr->normal.fill(dr->rng, host.data(), host.size(), 10000.0);
         FE_CUDA(cudaMemcpyAsync(m + (std::size_t)f * n, host.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
         FE_CUDA(cudaMemsetAsync(flag, 0xff, sizeof(int), s));
         FE_CUDA(cudaStreamSynchronize(s));
@@ -426,31 +541,34 @@ void umap_spectral_start(const int* offsets, const int* neighbors, const float* 
       }
     };
 
-    host.resize((std::size_t)n * B);
-    for (double& v : host) v = normal(rng) * 10000.0;
-    FE_CUDA(cudaMemcpyAsync(q, host.data(), sizeof(double) * host.size(), cudaMemcpyHostToDevice, s));
+    FE_CUDA(cudaMemcpyAsync(q, dr->block.data(), sizeof(double) * dr->block.size(), cudaMemcpyHostToDevice, s));
     orthonormalise(q, 0);
     for (int it = 0; it < spectral_n_iter; ++it) {
-      sp_multiply_kernel<<<gb, kSpThreads, 0, s>>>(offsets, neighbors, nw, n, B, q, z);
+      sp_multiply_kernel<<<gm, kSpThreads, 0, s>>>(offsets, neighbors, nw, n, B, q, z);
       FE_LAUNCH("sp_multiply_kernel");
       orthonormalise(z, 0);
       std::swap(q, z);
     }
-    sp_multiply_kernel<<<gb, kSpThreads, 0, s>>>(offsets, neighbors, nw, n, B, q, z);
+    sp_multiply_kernel<<<gm, kSpThreads, 0, s>>>(offsets, neighbors, nw, n, B, q, z);
     FE_LAUNCH("sp_multiply_kernel");
     sp_project_kernel<<<nb, kSpThreads, 0, s>>>(q, z, n, B, pa);
     FE_LAUNCH("sp_project_kernel");
-    sp_ritz_kernel<<<1, 32, 0, s>>>(pa, nb, B, coef);
+    sp_ritz_kernel<<<1, 64, 0, s>>>(pa, nb, B, coef);
     FE_LAUNCH("sp_ritz_kernel");
     sp_embed_kernel<<<nb, kSpThreads, 0, s>>>(q, coef, n, B, out, pb);
     FE_LAUNCH("sp_embed_kernel");
     sp_centre_kernel<<<nb, kSpThreads, 0, s>>>(out, n, pb, nb, pc);
     FE_LAUNCH("sp_centre_kernel");
-    // jitter: a fresh normal(0, 1e-4) distribution on the same stream, column after column
-    std::normal_distribution<double> jitter(0.0, 1e-4);
-    host.resize(2 * (std::size_t)n);
-    for (double& v : host) v = jitter(rng);
-    FE_CUDA(cudaMemcpyAsync(jit, host.data(), sizeof(double) * host.size(), cudaMemcpyHostToDevice, s));
+    // jitter: a fresh normal(0, 1e-4) distribution on the same stream, column after column (drawn
+    // ahead unless a redraw moved the stream on)
+    std::vector<double> fresh;
+    if (redrawn) {
+      NormalStream jitter(0.0, 1e-4);
+      fresh.resize(2 * (std::size_t)n);
+      jitter.fill(dr->rng, fresh.data(), fresh.size(), 1.0);
+    }
+    const std::vector<double>& jv = redrawn ? fresh : dr->jitter.get();
+    FE_CUDA(cudaMemcpyAsync(jit, jv.data(), sizeof(double) * jv.size(), cudaMemcpyHostToDevice, s));
     sp_expand_kernel<<<gb, kSpThreads, 0, s>>>(out, n, pc, nb, jit);
     FE_LAUNCH("sp_expand_kernel");
     FE_CUDA(cudaStreamSynchronize(s));

@@ -146,6 +146,12 @@ int fastembedr_cuda_umap_knn_spectral(const int* indices, const float* distances
  * compute on the host before calling the fused UMAP entry points below (host code, no GPU). */
 void fastembedr_umap_find_ab_params(double spread, double min_dist, double* a, double* b);
 
+/* No reference counterpart (diagnostic, host code, no GPU): 1 when the multi-threaded normal draws
+ * of the spectral start reproduce std::normal_distribution<double> on std::mt19937 bit for bit on
+ * this platform (checked once at first use), 0 when the start falls back to drawing through
+ * std::normal_distribution itself. Either way the draws equal the reference's. */
+int fastembedr_host_normal_stream_check(void);
+
 /* replaces fastembedr_cuda_spectral_init_from_knn, src/embedding_cuda_kernels.cpp:4801-4960
  * (bound by spectral_knn_init_cuda_impl, src/embedding_cuda_impl.cpp:1589-1628): the diffusion
  * start of initialize_layout_csr_cuda_diffusion (src/fast_knn_umap.cpp:2597-2652) over the fuzzy

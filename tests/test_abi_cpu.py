@@ -75,6 +75,12 @@ def test_umap_curve_parameters_match_the_oracle(min_dist):
     assert a == pytest.approx(ra, rel=1e-12) and b == pytest.approx(rb, rel=1e-12)
 
 
+def test_multithreaded_normal_draws_reproduce_the_standard_library():
+    """The spectral start's host draws take the multi-threaded polar path, which checks itself
+    bit for bit against std::normal_distribution on std::mt19937 at first use."""
+    assert _lib.load().fastembedr_host_normal_stream_check() == 1
+
+
 def test_spectral_start_csr_checks_its_graph_before_any_device_work():
     """Host-side checks of fastembedr_cuda_umap_spectral_init_csr (validate_csr_inputs plus the
     symmetry the GPU start needs) report errors without a GPU."""

@@ -92,22 +92,26 @@ def test_umap_invalid_parameters():
 
 
 def test_batched_umap_matches_each_instance_alone():
-    """Instances in one batched job reach the local structure they reach alone (15-NN
-    preservation within 0.01; float atomics make runs differ in rounding only)."""
-    knns, inits, xs = [], [], []
+    """Instances in one batched job reach the local structure they reach alone: mean 15-NN
+    preservation of three batched runs within 0.01 of three runs alone. Float atomics (Hogwild)
+    make every run differ; single runs of the 3,000-point instance spread over about 0.008, so
+    single pairs can differ by twice that while the means of three stay well inside 0.01."""
+    knns, inits = [], []
     for j, n in enumerate([3000, 12000, 5000]):
         x, _ = synthetic.mixture(n, 20, 6, 300 + j, centre_sd=3.0)
         knns.append(synthetic.exact_knn_numpy(x, 15))
         inits.append(_pca_init(x, 400 + j))
-    lays = api.umap_knn_batch(knns, inits, n_epochs=200)
-    for (idx, dist), y0, lay in zip(knns, inits, lays):
-        alone = api.umap_knn(idx, dist, y0, n_epochs=200).layout
-        n = idx.shape[0]
-        keep = np.arange(0, n, 2, dtype=np.int32)
-        pa = O.knn_preservation(alone, idx, keep=keep, preserve_k=15)
-        pb = O.knn_preservation(lay, idx, keep=keep, preserve_k=15)
-        assert np.all(np.isfinite(lay)) and np.abs(lay).max() <= 16.0
-        assert abs(pa - pb) < 0.01, (n, pa, pb)
+    keeps = [np.arange(0, idx.shape[0], 2, dtype=np.int32) for idx, _ in knns]
+    pb = np.zeros(len(knns))
+    for _ in range(3):
+        lays = api.umap_knn_batch(knns, inits, n_epochs=200)
+        for j, ((idx, dist), lay) in enumerate(zip(knns, lays)):
+            assert np.all(np.isfinite(lay)) and np.abs(lay).max() <= 16.0
+            pb[j] += O.knn_preservation(lay, idx, keep=keeps[j], preserve_k=15) / 3
+    for j, ((idx, dist), y0) in enumerate(zip(knns, inits)):
+        pa = np.mean([O.knn_preservation(api.umap_knn(idx, dist, y0, n_epochs=200).layout, idx, keep=keeps[j],
+                                         preserve_k=15) for _ in range(3)])
+        assert abs(pa - pb[j]) < 0.01, (idx.shape[0], pa, pb[j])
 
 
 @pytest.mark.parametrize("tag", ["3k", "200"])
