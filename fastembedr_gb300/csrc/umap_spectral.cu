@@ -35,7 +35,8 @@ constexpr int kSpPairs = kSpBlock * (kSpBlock + 1) / 2;  // upper triangle of th
 
 int sp_blocks(int n) { return std::max(1, std::min(ceil_div(n, kSpThreads), kSpMaxBlocks)); }
 
-// Fixed-order sum of `count` partials, valid in every thread of the block (all threads call).
+// Fixed-order sum of `count` partials, valid in every thread of the block (all threads call). The
+// loads go to L2: the partials may come from other blocks of the same launch.
 __device__ double sum_partials(const double* __restrict__ part, int count) {
   __shared__ double s_total;
   if (threadIdx.x < 32) {
@@ -45,11 +46,11 @@ __device__ double sum_partials(const double* __restrict__ part, int count) {
     for (; b + 7 * 32 < count; b += 8 * 32) {
       double v[8];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) v[u] = part[b + u * 32];
+      for (int u = 0; u < 8; ++u) v[u] = __ldcg(part + b + u * 32);
 #pragma unroll
       for (int u = 0; u < 8; ++u) s = __dadd_rn(s, v[u]);
     }
-    for (; b < count; b += 32) s = __dadd_rn(s, part[b]);
+    for (; b < count; b += 32) s = __dadd_rn(s, __ldcg(part + b));
     s = warp_sum(s);
     if (threadIdx.x == 0) s_total = s;
   }
@@ -59,8 +60,24 @@ __device__ double sum_partials(const double* __restrict__ part, int count) {
   return r;
 }
 
-// Block sum of v into part[blockIdx.x] (fixed order: warp trees, then warps in order).
-__device__ void block_partial(double v, double* __restrict__ part) {
+// The total of sum_partials computed by one full warp (every lane gets it).
+__device__ double warp_total(const double* __restrict__ part, int count) {
+  const int lane = threadIdx.x & 31;
+  double s = 0.0;
+  int b = lane;
+  for (; b + 7 * 32 < count; b += 8 * 32) {
+    double v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = __ldcg(part + b + u * 32);
+#pragma unroll
+    for (int u = 0; u < 8; ++u) s = __dadd_rn(s, v[u]);
+  }
+  for (; b < count; b += 32) s = __dadd_rn(s, __ldcg(part + b));
+  return warp_sum(s);
+}
+
+// Block sum of v into *dst (fixed order: warp trees, then warps in order).
+__device__ void block_partial_at(double v, double* __restrict__ dst) {
   __shared__ double s_w[kSpThreads / 32];
   v = warp_sum(v);
   if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = v;
@@ -68,9 +85,11 @@ __device__ void block_partial(double v, double* __restrict__ part) {
   if (threadIdx.x == 0) {
     double t = 0.0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t = __dadd_rn(t, s_w[w]);
-    part[blockIdx.x] = t;
+    *dst = t;
   }
 }
+
+__device__ void block_partial(double v, double* __restrict__ part) { block_partial_at(v, part + blockIdx.x); }
 
 // deg[r] = float(sum of row r's weights in double)
 __global__ void sp_degree_kernel(const int* __restrict__ offsets, const float* __restrict__ w, int n,
@@ -117,62 +136,70 @@ __global__ void sp_normalise_trivial_kernel(double* __restrict__ triv, int n, co
     triv[r] = __ddiv_rn(triv[r], nrm);
 }
 
-// Gram-Schmidt steps. A column whose norm vanished sets *flag to its index; the later steps of
-// the same pass see the flag and do nothing, and the host redraws that column and resumes.
+// ---------------------------------------------------------------- subspace iteration
 //
-// Block partials of m[:, c] . triv for columns from..B-1 (part + c * nparts): the first
-// projection of every column, which the earlier columns do not change.
-__global__ void __launch_bounds__(kSpThreads)
-gs_trivial_dots_kernel(const double* __restrict__ m, const double* __restrict__ triv, int n, int from, int B,
-                       double* __restrict__ part, const int* __restrict__ flag) {
-  if (*flag >= 0) return;
-  for (int c = from; c < B; ++c) {
-    const double* qc = m + (long long)c * n;
-    double acc = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-      acc = __dadd_rn(acc, __dmul_rn(qc[i], triv[i]));
-    block_partial(acc, part + (long long)c * gridDim.x);
-    __syncthreads();
-  }
-}
+// The block subspace iteration runs as one cooperative launch: all rounds of multiply and modified
+// Gram-Schmidt, with a grid barrier between dependent steps. Every sum over points keeps the
+// partial structure of a grid of `nparts` = sp_blocks(n) blocks of kSpThreads threads ("virtual
+// blocks": thread t of virtual block vb covers points vb * kSpThreads + t + k * nparts *
+// kSpThreads), whatever the number of resident blocks that run them, so its value does not depend
+// on the launch. Vectors written during the launch are read through L2 (__ldcg): another block
+// may have written them, and L1 is not coherent.
 
-// Optionally first finish column `prev` (prev >= 0): divide it by the root of the sum of
-// prev_part, or flag it as vanished. Then qc -= (sum of part_in) * u and partials of sum qc * v
-// (v may be qc).
-__global__ void __launch_bounds__(kSpThreads)
-gs_sub_dot_kernel(double* qc, const double* __restrict__ u, const double* __restrict__ part_in, int nparts,
-                  const double* v, int n, double* __restrict__ part_out, double* prev_col,
-                  const double* __restrict__ prev_part, int prev, int* __restrict__ flag) {
-  if (*flag >= 0) return;
-  if (prev >= 0) {
-    const double nrm = __dsqrt_rn(sum_partials(prev_part, nparts));
-    if (nrm < 1e-10) {
-      if (blockIdx.x == 0 && threadIdx.x == 0) *flag = prev;
-      return;
+constexpr long long kSpBarrierCycles = 4000000000LL;  // about 2 s at the SM clock
+
+struct SpGrid {
+  unsigned count, gen;  // barrier arrivals, barrier generation
+  int error;            // 1: a barrier wait gave up
+  int status;           // -1, or 16 * (round + 1) + column of a vanished Gram-Schmidt column
+};
+
+// Grid barrier number `bar` (0, 1, ... within a launch) of a cooperative launch (all blocks
+// resident). Arrivals count up without reset, so barrier `bar` is complete at count G * (bar + 1).
+// The last block to arrive first sums the partial arrays of the columns in `mask` (part + c *
+// nparts) into totals[c], the sums the next step needs, then releases the others by writing the
+// generation bar + 1. A wait is bounded: after kSpBarrierCycles the block records the error and
+// returns false, and later barriers return false at once, so every block leaves the kernel.
+__device__ bool sp_grid_sync(SpGrid* g, unsigned bar, unsigned mask, const double* part, int nparts,
+                             double* totals) {
+  __shared__ int s_ok, s_last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    s_ok = *(volatile int*)&g->error == 0;
+    s_last = 0;
+    if (s_ok) {
+      __threadfence();
+      s_last = atomicAdd(&g->count, 1u) == gridDim.x * (bar + 1) - 1;
     }
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-      prev_col[i] = __ddiv_rn(prev_col[i], nrm);
   }
-  const double d = sum_partials(part_in, nparts);
-  double acc = 0.0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const double x = __dsub_rn(qc[i], __dmul_rn(d, u[i]));
-    qc[i] = x;
-    acc = __dadd_rn(acc, __dmul_rn(x, v == qc ? x : v[i]));
+  __syncthreads();
+  if (!s_ok) return false;
+  if (s_last) {
+    __threadfence();
+    const int w = threadIdx.x >> 5;
+    if (w < kSpBlock && ((mask >> w) & 1u)) {
+      const double t = warp_total(part + (long long)w * nparts, nparts);
+      if ((threadIdx.x & 31) == 0) totals[w] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      *(volatile unsigned*)&g->gen = bar + 1;
+    }
+  } else if (threadIdx.x == 0) {
+    const long long t0 = clock64();
+    while (*(volatile unsigned*)&g->gen < bar + 1) {
+      if (clock64() - t0 > kSpBarrierCycles) {
+        atomicExch(&g->error, 1);
+        s_ok = 0;
+        break;
+      }
+      __nanosleep(32);
+    }
+    __threadfence();
   }
-  block_partial(acc, part_out);
-}
-
-__global__ void gs_scale_kernel(double* __restrict__ qc, const double* __restrict__ part_in, int nparts, int n,
-                                int col, int* __restrict__ flag) {
-  if (*flag >= 0) return;
-  const double nrm = __dsqrt_rn(sum_partials(part_in, nparts));
-  if (nrm < 1e-10) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) *flag = col;
-    return;
-  }
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    qc[i] = __ddiv_rn(qc[i], nrm);
+  __syncthreads();
+  return s_ok != 0;
 }
 
 // y[:, c] = A x[:, c] for the B columns. A warp works on four rows at once, eight lanes per row
@@ -181,9 +208,8 @@ __global__ void gs_scale_kernel(double* __restrict__ qc, const double* __restric
 // round by shuffles, and every lane gathers its column's 8 values and adds the products in CSR
 // order. Each (row, column) sum is the sequential FP64 sum of the row, and all 32 lanes of a
 // warp instruction on the FP64 pipe carry work.
-__global__ void __launch_bounds__(kSpThreads)
-sp_multiply_kernel(const int* __restrict__ offsets, const int* __restrict__ nb, const float* __restrict__ nw,
-                   int n, int B, const double* __restrict__ x, double* __restrict__ y) {
+__device__ void sp_multiply_rows(const int* __restrict__ offsets, const int* __restrict__ nb,
+                                 const float* __restrict__ nw, int n, int B, const double* x, double* y) {
   const int lane = threadIdx.x & 31, slot = lane >> 3, c = lane & 7;
   const unsigned gmask = 0xffu << (slot * 8);
   const int slots = gridDim.x * (blockDim.x >> 5) * 4;
@@ -209,7 +235,7 @@ sp_multiply_kernel(const int* __restrict__ offsets, const int* __restrict__ nb, 
 #pragma unroll
       for (int t = 0; t < 8; ++t) {
         const int jt = __shfl_sync(gmask, j, t, 8);
-        v[t] = t < cnt ? xc[jt] : 0.0;
+        v[t] = t < cnt ? __ldcg(xc + jt) : 0.0;
       }
 #pragma unroll
       for (int t = 0; t < 8; ++t) {
@@ -220,6 +246,155 @@ sp_multiply_kernel(const int* __restrict__ offsets, const int* __restrict__ nb, 
       w = wn;
     }
     if (c < B) y[(long long)c * n + r] = acc;
+  }
+}
+
+__global__ void __launch_bounds__(kSpThreads)
+sp_multiply_kernel(const int* __restrict__ offsets, const int* __restrict__ nb, const float* __restrict__ nw,
+                   int n, int B, const double* __restrict__ x, double* __restrict__ y) {
+  sp_multiply_rows(offsets, nb, nw, n, B, x, y);
+}
+
+// Block partials of acc[c] for the columns in `mask` into part[c * nparts + vb]: per column the
+// order of block_partial_at (warp trees, then warps in order).
+__device__ void sp_block_partials(const double (&acc)[kSpBlock], unsigned mask, double* part, int nparts, int vb) {
+  __shared__ double s_red[kSpBlock][kSpThreads / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int c = 0; c < kSpBlock; ++c)
+    if ((mask >> c) & 1u) {
+      const double v = warp_sum(acc[c]);
+      if (lane == 0) s_red[c][w] = v;
+    }
+  __syncthreads();
+  if (threadIdx.x < kSpBlock && ((mask >> threadIdx.x) & 1u)) {
+    double t = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t = __dadd_rn(t, s_red[threadIdx.x][k]);
+    part[(long long)threadIdx.x * nparts + vb] = t;
+  }
+  __syncthreads();
+}
+
+// Modified Gram-Schmidt of the columns from..B-1 of m against the trivial vector and the columns
+// before them (columns below `from` are final), as a wavefront. Column c's step j (j = 0..c)
+// subtracts its last dot times u_j (u_0 = triv, u_j = q_{j-1}) and forms the partials of its dot
+// with v_j = q_j, or of its squared norm when j = c; a column is divided by its norm at the start
+// of the step after its norm step. Step j needs q_j final, so every column whose next step has
+// its v final advances in the same grid step: the pass takes 2 (B - from) + 1 grid steps instead
+// of one per projection, and each column sees exactly the operations of the column-by-column
+// order. The columns' post-multiply values are copied to `backup` first (restored by the host
+// before a redraw resumes the pass). Returns 0 when done, 1 + c when column c vanished, -1 when a
+// barrier gave up.
+__device__ int sp_orthonormalise(double* m, double* backup, const double* __restrict__ triv, int n, int B, int from,
+                                 int nparts, double* part, double* totals, SpGrid* grid, unsigned& bar) {
+  // the first projection of every column, which the earlier columns do not change
+  const unsigned all = ((1u << B) - 1u) & ~((1u << from) - 1u);
+  for (int vb = blockIdx.x; vb < nparts; vb += gridDim.x) {
+    double acc[kSpBlock];
+#pragma unroll
+    for (int c = 0; c < kSpBlock; ++c) acc[c] = 0.0;
+    for (int i = vb * blockDim.x + threadIdx.x; i < n; i += nparts * blockDim.x) {
+      const double t = triv[i];
+#pragma unroll
+      for (int c = 0; c < kSpBlock; ++c)
+        if ((all >> c) & 1u) {
+          const double x = __ldcg(m + (long long)c * n + i);
+          backup[(long long)c * n + i] = x;
+          acc[c] = __dadd_rn(acc[c], __dmul_rn(x, t));
+        }
+    }
+    sp_block_partials(acc, all, part, nparts, vb);
+  }
+  if (!sp_grid_sync(grid, bar++, all, part, nparts, totals)) return -1;
+  int jn[kSpBlock];  // next step of each column (block-uniform)
+#pragma unroll
+  for (int c = 0; c < kSpBlock; ++c) jn[c] = 0;
+  int nfinal = from, pending = -1;
+  while (nfinal < B) {
+    double nrm = 0.0;
+    const int fin = pending;
+    if (fin >= 0) {
+      nrm = __dsqrt_rn(__ldcg(totals + fin));
+      if (nrm < 1e-10) return 1 + fin;
+      nfinal = fin + 1;
+    }
+    // ready columns: not final, next step's v final (or the norm step); all share one step j
+    int j = kSpBlock;
+#pragma unroll
+    for (int c = 0; c < kSpBlock; ++c)
+      if (c >= nfinal && c < B && (jn[c] == c || jn[c] < nfinal)) j = min(j, jn[c]);
+    unsigned ready = 0u;
+#pragma unroll
+    for (int c = 0; c < kSpBlock; ++c)
+      if (c >= nfinal && c < B && jn[c] == j && (j == c || j < nfinal)) ready |= 1u << c;
+    double d[kSpBlock];
+#pragma unroll
+    for (int c = 0; c < kSpBlock; ++c) d[c] = ((ready >> c) & 1u) ? __ldcg(totals + c) : 0.0;
+    const double* u = j == 0 ? triv : m + (long long)(j - 1) * n;
+    double* qf = fin >= 0 ? m + (long long)fin * n : nullptr;
+    const double* qv = m + (long long)(j < kSpBlock ? j : 0) * n;
+    for (int vb = blockIdx.x; vb < nparts; vb += gridDim.x) {
+      double acc[kSpBlock];
+#pragma unroll
+      for (int c = 0; c < kSpBlock; ++c) acc[c] = 0.0;
+      for (int i = vb * blockDim.x + threadIdx.x; i < n; i += nparts * blockDim.x) {
+        double xf = 0.0;
+        if (qf) {
+          xf = __ddiv_rn(__ldcg(qf + i), nrm);
+          qf[i] = xf;
+        }
+        if (ready) {
+          const double ui = __ldcg(u + i);
+          const double vi = j == fin ? xf : __ldcg(qv + i);
+#pragma unroll
+          for (int c = 0; c < kSpBlock; ++c)
+            if ((ready >> c) & 1u) {
+              double* qc = m + (long long)c * n;
+              const double x = __dsub_rn(__ldcg(qc + i), __dmul_rn(d[c], ui));
+              qc[i] = x;
+              acc[c] = __dadd_rn(acc[c], __dmul_rn(x, j < c ? vi : x));
+            }
+        }
+      }
+      if (ready) sp_block_partials(acc, ready, part, nparts, vb);
+    }
+    pending = -1;
+#pragma unroll
+    for (int c = 0; c < kSpBlock; ++c)
+      if ((ready >> c) & 1u) {
+        if (jn[c] == c) pending = c;
+        jn[c] += 1;
+      }
+    if (!sp_grid_sync(grid, bar++, ready, part, nparts, totals)) return -1;
+  }
+  return 0;
+}
+
+// Rounds round_begin..round_end-1 of the subspace iteration over the two blocks buf0 / buf1 (n x B
+// column-major): round r multiplies buf[r % 2] into buf[(r + 1) % 2] and orthonormalises the
+// result (round -1: orthonormalise buf0 only); buf[r % 2] then holds the post-multiply copy. The
+// first round starts at column first_from and multiplies only when first_multiply is set. A
+// column whose norm vanishes stops every block at the same step (they all read the same norm);
+// block 0 records round and column in grid->status for the host's redraw.
+__global__ void __launch_bounds__(kSpThreads, 3)
+sp_rounds_kernel(const int* __restrict__ offsets, const int* __restrict__ nbr, const float* __restrict__ nw,
+                 const double* __restrict__ triv, int n, int B, int nparts, double* buf0, double* buf1, double* part,
+                 double* totals, int round_begin, int round_end, int first_from, int first_multiply, SpGrid* grid) {
+  unsigned bar = 0;
+  for (int r = round_begin; r < round_end; ++r) {
+    double* m = ((r + 1) & 1) ? buf1 : buf0;
+    double* other = (r & 1) ? buf1 : buf0;
+    const bool first = r == round_begin;
+    if (!first || first_multiply) {
+      sp_multiply_rows(offsets, nbr, nw, n, B, other, m);
+      if (!sp_grid_sync(grid, bar++, 0u, part, nparts, totals)) return;
+    }
+    const int st = sp_orthonormalise(m, other, triv, n, B, first ? first_from : 0, nparts, part, totals, grid, bar);
+    if (st > 0) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) grid->status = 16 * (r + 1) + (st - 1);
+      return;
+    }
+    if (st < 0) return;
   }
 }
 
@@ -469,7 +644,8 @@ void umap_spectral_start(const int* offsets, const int* neighbors, const float* 
     float *deg = nullptr, *nw = nullptr;
     double *triv = nullptr, *q = nullptr, *z = nullptr, *pa = nullptr, *pb = nullptr, *pc = nullptr;
     double *coef = nullptr, *jit = nullptr;
-    int* flag = nullptr;
+    SpGrid* grid = nullptr;
+    double* totals = nullptr;
     Arena w;
     w.reserve(&deg, n);
     w.reserve(&nw, (std::size_t)nnz);
@@ -481,7 +657,8 @@ void umap_spectral_start(const int* offsets, const int* neighbors, const float* 
     w.reserve(&pc, kSpMaxBlocks * 2);
     w.reserve(&coef, 2 * kSpBlock);
     w.reserve(&jit, 2 * (std::size_t)n);
-    w.reserve(&flag, 1);
+    w.reserve(&grid, 1);
+    w.reserve(&totals, kSpBlock);
     w.commit("UMAP spectral start");
     sp_degree_kernel<<<gb, kSpThreads, 0, s>>>(offsets, weights, n, deg);
     FE_LAUNCH("sp_degree_kernel");
@@ -491,7 +668,8 @@ void umap_spectral_start(const int* offsets, const int* neighbors, const float* 
     FE_LAUNCH("sp_trivial_kernel");
     sp_normalise_trivial_kernel<<<gb, kSpThreads, 0, s>>>(triv, n, pa, nb);
     FE_LAUNCH("sp_normalise_trivial_kernel");
-    FE_CUDA(cudaMemsetAsync(flag, 0xff, sizeof(int), s));  // -1: no vanished column
+    SpGrid g0{0u, 0u, 0, -1};
+    FE_CUDA(cudaMemcpyAsync(grid, &g0, sizeof(SpGrid), cudaMemcpyHostToDevice, s));
     SpectralDraws local;
     SpectralDraws* dr = pre;
     if (!dr || dr->block.size() != (std::size_t)n * B) {
@@ -500,55 +678,52 @@ void umap_spectral_start(const int* offsets, const int* neighbors, const float* 
     }
     bool redrawn = false;
 
-    // column c of the block in `m`, orthonormalised from column `from` on; the host redraws a
-    // vanished column from the stream and resumes there
-    auto orthonormalise = [&](double* m, int from) {
-      for (;;) {
-        // every column's projection on the trivial vector first (pa), then per column the
-        // projections on the earlier columns; a column is divided by its norm inside the next
-        // column's first step
-        gs_trivial_dots_kernel<<<nb, kSpThreads, 0, s>>>(m, triv, n, from, B, pa, flag);
-        FE_LAUNCH("gs_trivial_dots_kernel");
-        double* in = pb;
-        double* outp = pc;
-        for (int c = from; c < B; ++c) {
-          double* qc = m + (std::size_t)c * n;
-          for (int j = 0; j <= c; ++j) {
-            const double* u = j == 0 ? triv : m + (std::size_t)(j - 1) * n;
-            const double* v = j < c ? m + (std::size_t)j * n : qc;
-            const double* pin = j == 0 ? pa + (std::size_t)c * nb : in;
-            const int prev = j == 0 && c > from ? c - 1 : -1;
-            gs_sub_dot_kernel<<<nb, kSpThreads, 0, s>>>(qc, u, pin, nb, v, n, outp,
-                                                        prev >= 0 ? m + (std::size_t)prev * n : nullptr, in, prev,
-                                                        flag);
-            FE_LAUNCH("gs_sub_dot_kernel");
-            std::swap(in, outp);
-          }
-        }
-        gs_scale_kernel<<<nb, kSpThreads, 0, s>>>(m + (std::size_t)(B - 1) * n, in, nb, n, B - 1, flag);
-        FE_LAUNCH("gs_scale_kernel");
-        int f = -1;
-        FE_CUDA(cudaMemcpyAsync(&f, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
-        FE_CUDA(cudaStreamSynchronize(s));
-        if (f < 0) return;
-        redrawn = true;
-        host.resize(n);
-        dr->normal.fill(dr->rng, host.data(), host.size(), 10000.0);
-        FE_CUDA(cudaMemcpyAsync(m + (std::size_t)f * n, host.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
-        FE_CUDA(cudaMemsetAsync(flag, 0xff, sizeof(int), s));
-        FE_CUDA(cudaStreamSynchronize(s));
-        from = f;
-      }
-    };
-
+    // The subspace iteration as cooperative launches of every resident block (at most one per
+    // partial slot): the initial orthonormalisation (round -1) and spectral_n_iter rounds. A
+    // launch that stops at a vanished column is resumed from it after the host redraws the
+    // column from the stream, as the reference redraws and repeats it.
+    int per_sm = 0;
+    FE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sp_rounds_kernel, kSpThreads, 0));
+    const int G = std::min(nb, per_sm * sm_count());
+    if (G < 1) throw Error("the spectral start's subspace iteration cannot be made resident");
+    int dev = 0, coop = 0;
+    FE_CUDA(cudaGetDevice(&dev));
+    FE_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    if (!coop) throw Error("the device does not support cooperative launches");
     FE_CUDA(cudaMemcpyAsync(q, dr->block.data(), sizeof(double) * dr->block.size(), cudaMemcpyHostToDevice, s));
-    orthonormalise(q, 0);
-    for (int it = 0; it < spectral_n_iter; ++it) {
-      sp_multiply_kernel<<<gm, kSpThreads, 0, s>>>(offsets, neighbors, nw, n, B, q, z);
-      FE_LAUNCH("sp_multiply_kernel");
-      orthonormalise(z, 0);
-      std::swap(q, z);
+    int r0 = -1, from = 0, mult = 0;
+    for (;;) {
+      int nparts = nb, r_end = spectral_n_iter;
+      void* args[] = {(void*)&offsets, (void*)&neighbors, (void*)&nw, (void*)&triv, (void*)&n, (void*)&B,
+                      (void*)&nparts, (void*)&q, (void*)&z, (void*)&pa, (void*)&totals, (void*)&r0, (void*)&r_end,
+                      (void*)&from, (void*)&mult, (void*)&grid};
+      FE_CUDA(cudaLaunchCooperativeKernel((const void*)sp_rounds_kernel, dim3(G), dim3(kSpThreads), args, 0, s));
+      FE_LAUNCH("sp_rounds_kernel");
+      SpGrid g1;
+      FE_CUDA(cudaMemcpyAsync(&g1, grid, sizeof(SpGrid), cudaMemcpyDeviceToHost, s));
+      FE_CUDA(cudaStreamSynchronize(s));
+      if (g1.error) throw Error("spectral start: a grid barrier of the subspace iteration timed out");
+      if (g1.status < 0) break;
+      const int rr = g1.status / 16 - 1, f = g1.status % 16;
+      if (rr < -1 || rr >= spectral_n_iter || f < 0 || f >= B) throw Error("spectral start: invalid redraw status");
+      redrawn = true;
+      host.resize(n);
+      dr->normal.fill(dr->rng, host.data(), host.size(), 10000.0);
+      // the later columns back to their post-multiply values (the pass had started on them), then
+      // the redrawn column
+      double* m = ((rr + 1) & 1) ? z : q;
+      const double* bk = (rr & 1) ? z : q;
+      if (f + 1 < B)
+        FE_CUDA(cudaMemcpyAsync(m + (std::size_t)(f + 1) * n, bk + (std::size_t)(f + 1) * n,
+                                sizeof(double) * (std::size_t)(B - f - 1) * n, cudaMemcpyDeviceToDevice, s));
+      FE_CUDA(cudaMemcpyAsync(m + (std::size_t)f * n, host.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+      FE_CUDA(cudaMemcpyAsync(grid, &g0, sizeof(SpGrid), cudaMemcpyHostToDevice, s));
+      r0 = rr;
+      from = f;
+      mult = 0;
     }
+    // after round r the block is in buf[(r + 1) % 2]: the last round leaves it in buf[n_iter % 2]
+    if (spectral_n_iter & 1) std::swap(q, z);
     sp_multiply_kernel<<<gm, kSpThreads, 0, s>>>(offsets, neighbors, nw, n, B, q, z);
     FE_LAUNCH("sp_multiply_kernel");
     sp_project_kernel<<<nb, kSpThreads, 0, s>>>(q, z, n, B, pa);

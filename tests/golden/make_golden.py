@@ -154,6 +154,28 @@ def umap_spectral_case():
     st = R.ref_umap_spectral_init(off, nb[:m].copy(), w[:m].copy(), n, m, 5, 2.0, 9, y)
     assert st == 0, R.ref_last_error()
     out["start_40_scaled"] = y.reshape(n, 2)
+    # a graph whose operator has rank 6 (a 6-ring with weights exact in float32, 34 isolated
+    # points): after each multiply the block's later columns vanish in Gram-Schmidt and are
+    # redrawn from the stream
+    n = 40
+    ring = 6
+    rows = [[] for _ in range(n)]
+    for i in range(ring):
+        for j, wv in (((i + 1) % ring, 0.5 + 0.125 * i), ((i + 2) % ring, 0.25 + 0.0625 * i)):
+            rows[i].append((j, wv))
+            rows[j].append((i, wv))
+    off = np.zeros(n + 1, np.int32)
+    nbl, wl = [], []
+    for i in range(n):
+        for j, wv in sorted(rows[i]):
+            nbl.append(j)
+            wl.append(wv)
+        off[i + 1] = len(nbl)
+    nb, w = np.array(nbl, np.int32), np.array(wl, np.float64)
+    y = np.zeros(2 * n)
+    st = R.ref_umap_spectral_init(off, nb, w, n, len(nb), 4, float("nan"), 11, y)
+    assert st == 0, R.ref_last_error()
+    out.update({"iso_offsets": off, "iso_neighbors": nb, "iso_weights": w, "start_iso": y.reshape(n, 2)})
     np.savez_compressed(os.path.join(OUT, "umap_spectral.npz"), **out)
 
 

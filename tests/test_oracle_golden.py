@@ -73,6 +73,13 @@ def test_umap_spectral_start_matches_reference(golden, tag):
         np.testing.assert_array_equal(ys, g["start_40_scaled"])
 
 
+def test_umap_spectral_start_redraws_like_the_reference(golden):
+    """Gram-Schmidt redraws of vanished columns (a rank-6 graph with 34 isolated points)."""
+    g = golden("umap_spectral")
+    y = O.umap_spectral_init(g["iso_offsets"], g["iso_neighbors"], g["iso_weights"].astype(np.float32), 4, 11)
+    np.testing.assert_array_equal(y, g["start_iso"])
+
+
 @pytest.mark.parametrize("tag,nneg,thr", [("exact", 256, 4096), ("sampled", 64, 10)])
 def test_transform_matches_reference(golden, tag, nneg, thr):
     g = golden("transform_2k")

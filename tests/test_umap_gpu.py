@@ -221,6 +221,15 @@ def test_spectral_start_matches_reference_golden(golden, tag):
         assert np.std(scaled, axis=0, ddof=1) == pytest.approx([2.0, 2.0], rel=1e-9)
 
 
+def test_spectral_start_redraws_vanished_columns_like_the_reference(golden):
+    """A graph whose operator has rank 6 (a weighted 6-ring and 34 isolated points): after every
+    multiply the block's later columns vanish in Gram-Schmidt and are redrawn from the random
+    stream, so the start depends on each redraw landing where the reference's does."""
+    g = golden("umap_spectral")
+    got = api.umap_spectral_start_csr(g["iso_offsets"], g["iso_neighbors"], g["iso_weights"], 4, 11)
+    assert np.abs(got - g["start_iso"]).max() <= 1e-6, np.abs(got - g["start_iso"]).max()
+
+
 def test_spectral_start_matches_oracle_20k():
     x, _ = synthetic.mixture(20000, 30, 12, 46, centre_sd=3.0, lognormal_sizes=True, anisotropic=True)
     idx, dist = synthetic.exact_knn_numpy(x, 15)
