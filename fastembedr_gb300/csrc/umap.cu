@@ -25,6 +25,9 @@
 #include <type_traits>
 #include <vector>
 
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_segmented_radix_sort.cuh>
+
 #include "../../include/fastembedr_cuda.h"
 #include "philox.cuh"
 #include "sort.cuh"
@@ -655,6 +658,28 @@ void umap_ab_params(double spread, double min_dist, double* a, double* b) {
 }
 
 // Optimizer state of one UMAP instance.
+// Sort keys of the period-ordered edge list: the bits of epochs_per_sample (non-negative floats,
+// so their bit patterns order as the values; inf and NaN, never sampled, sort last).
+__global__ void umap_period_keys_kernel(const float* __restrict__ eps, int m, unsigned* __restrict__ keys,
+                                        int* __restrict__ idx) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < m; e += gridDim.x * blockDim.x) {
+    const float v = eps[e];
+    keys[e] = v > 0.0f || isnan(v) ? __float_as_uint(v) : 0u;
+    idx[e] = e;
+  }
+}
+
+__global__ void umap_gather_edges_kernel(const int* __restrict__ perm, const int* __restrict__ heads,
+                                         const int* __restrict__ tails, const float* __restrict__ eps, int m,
+                                         int* __restrict__ oh, int* __restrict__ ot, float* __restrict__ oe) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < m; e += gridDim.x * blockDim.x) {
+    const int q = perm[e];
+    oh[e] = heads[q];
+    ot[e] = tails[q];
+    oe[e] = eps[q];
+  }
+}
+
 struct UmapJob {
   Stream stream;
   Arena arena;
@@ -676,8 +701,61 @@ struct UmapJob {
   const long long* edge_begin = nullptr;
   const int* vert_begin = nullptr;
   int ninst = 1;
+  // Edges ordered by sampling period (stable, within each instance of a batch): the edges of a
+  // warp then fire in the same epochs and draw similar numbers of negative samples, where the
+  // head-ordered list left most lanes of a warp idle in any one epoch. Only the order of the
+  // asynchronous (Hogwild) updates changes.
+  Arena ordered;
+  void order_by_period(const int*& heads, const int*& tails, const float*& eps, long long n_edges) {
+    if (n_edges < 2 || n_edges > INT_MAX) return;
+    cudaStream_t s = stream.s;
+    const int m = (int)n_edges;
+    unsigned *keys = nullptr, *keys_out = nullptr;
+    int *idx = nullptr, *perm = nullptr, *oh = nullptr, *ot = nullptr;
+    float* oe = nullptr;
+    std::size_t temp_bytes = 0;
+    if (ninst > 1)
+      FE_CUDA(cub::DeviceSegmentedRadixSort::SortPairs(nullptr, temp_bytes, keys, keys_out, idx, perm, m, ninst,
+                                                       edge_begin, edge_begin + 1, 0, 32, s));
+    else
+      FE_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, temp_bytes, keys, keys_out, idx, perm, m, 0, 32, s));
+    unsigned char* temp = nullptr;
+    Arena work;
+    work.reserve(&keys, m);
+    work.reserve(&keys_out, m);
+    work.reserve(&idx, m);
+    work.reserve(&perm, m);
+    work.reserve(&temp, std::max<std::size_t>(temp_bytes, 16));
+    work.commit("UMAP edge order workspace");
+    ordered.release();
+    ordered.reserve(&oh, m);
+    ordered.reserve(&ot, m);
+    ordered.reserve(&oe, m);
+    ordered.commit("UMAP edges in period order");
+    const int blocks = std::max(1, std::min(ceil_div(m, 256), sm_count() * 8));
+    umap_period_keys_kernel<<<blocks, 256, 0, s>>>(eps, m, keys, idx);
+    FE_LAUNCH("umap_period_keys_kernel");
+    if (ninst > 1)
+      FE_CUDA(cub::DeviceSegmentedRadixSort::SortPairs(temp, temp_bytes, keys, keys_out, idx, perm, m, ninst,
+                                                       edge_begin, edge_begin + 1, 0, 32, s));
+    else
+      FE_CUDA(cub::DeviceRadixSort::SortPairs(temp, temp_bytes, keys, keys_out, idx, perm, m, 0, 32, s));
+    umap_gather_edges_kernel<<<blocks, 256, 0, s>>>(perm, heads, tails, eps, m, oh, ot, oe);
+    FE_LAUNCH("umap_gather_edges_kernel");
+    FE_CUDA(cudaStreamSynchronize(s));  // the workspace is released on return
+    heads = oh;
+    tails = ot;
+    eps = oe;
+  }
   void run(const int* heads, const int* tails, const float* eps, long long n_edges, const UmapParams& p) {
     cudaStream_t s = stream.s;
+    order_by_period(heads, tails, eps, n_edges);
+    // captured graphs hold the edge arrays of the run that captured them
+    for (auto& kv : graphs) {
+      if (kv.second.second) cudaGraphExecDestroy(kv.second.second);
+      if (kv.second.first) cudaGraphDestroy(kv.second.first);
+    }
+    graphs.clear();
     FE_CUDA(cudaMemsetAsync(epoch, 0, sizeof(unsigned), s));
     const int eblocks = std::max(1, std::min(ceil_div(n_edges, 256), sm_count() * 8));
     const int pblocks = std::max(1, std::min(ceil_div(p.n, 256), sm_count() * 4));
