@@ -567,24 +567,32 @@ umap_epoch_kernel(float2* __restrict__ y, const int* __restrict__ heads, const i
       atomicAdd(y + t, make_float2(-gx, -gy));
     }
     const int ns = umap_negative_samples(period, p.negative_sample_rate, epoch);
-    uint4 r = make_uint4(0u, 0u, 0u, 0u);
-    for (int s = 0; s < ns; ++s) {
-      if ((s & 3) == 0)
-        r = philox4x32_10(make_uint4((unsigned)e_local, (unsigned)(e_local >> 32), epoch, (unsigned)(s >> 2)),
-                          make_uint2(p.seed, 0x5eed0f0cu));
-      const unsigned draw = (s & 3) == 0 ? r.x : ((s & 3) == 1 ? r.y : ((s & 3) == 2 ? r.z : r.w));
-      const int neg = v0 + (int)bounded(draw, (unsigned)nv);
-      if (neg == h || neg == t) continue;
-      const float2 yn = y[neg];
-      const float dx = yh.x - yn.x, dy = yh.y - yn.y;
-      const float d2 = fmaxf(fe, dx * dx + dy * dy);
-      const float d2b = schraudolph_pow(d2, p.b);
-      const float rc = p.repulsion_strength * 2.0f * p.b / ((0.001f + d2) * (p.a * d2b + 1.0f));
-      const float gx = clip4(rc * dx) * alpha, gy = clip4(rc * dy) * alpha;
-      yh.x += gx;
-      yh.y += gy;
-      mx += gx;
-      my += gy;
+    // negatives four at a time (one Philox block): the four positions are loaded together, then
+    // the samples are applied in order
+    for (int s0 = 0; s0 < ns; s0 += 4) {
+      const uint4 r = philox4x32_10(make_uint4((unsigned)e_local, (unsigned)(e_local >> 32), epoch, (unsigned)(s0 >> 2)),
+                                    make_uint2(p.seed, 0x5eed0f0cu));
+      const unsigned draws[4] = {r.x, r.y, r.z, r.w};
+      int neg[4];
+      float2 yn[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        neg[q] = v0 + (int)bounded(draws[q], (unsigned)nv);
+        yn[q] = s0 + q < ns ? y[neg[q]] : make_float2(0.0f, 0.0f);
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (s0 + q >= ns || neg[q] == h || neg[q] == t) continue;
+        const float dx = yh.x - yn[q].x, dy = yh.y - yn[q].y;
+        const float d2 = fmaxf(fe, dx * dx + dy * dy);
+        const float d2b = schraudolph_pow(d2, p.b);
+        const float rc = p.repulsion_strength * 2.0f * p.b / ((0.001f + d2) * (p.a * d2b + 1.0f));
+        const float gx = clip4(rc * dx) * alpha, gy = clip4(rc * dy) * alpha;
+        yh.x += gx;
+        yh.y += gy;
+        mx += gx;
+        my += gy;
+      }
     }
     atomicAdd(y + h, make_float2(mx, my));
   }
