@@ -80,6 +80,7 @@ def orc() -> C.CDLL:
             "orc_umap_powf_fast": (F, [F, F]),
             "orc_umap_pow": (D, [D, D]),
             "orc_umap_sgd_serial": (V, [I, i32p, i32p, f32p, f64p, I, D, D, I, D, D, I]),
+            "orc_umap_sgd_threaded": (V, [I, i32p, i32p, f32p, f64p, I, D, D, I, D, D, I, I]),
             "orc_umap_diffusion_init": (V, [i32p, i32p, f32p, I, I, I, I, f32p]),
             "orc_umap_spectral_init": (V, [i32p, i32p, f32p, I, I, D, I, f64p]),
             "orc_umap_sgd_coo_schedule": (V, [I, I, i32p, i32p, f32p, f32p, I, F, F, I, F, F, C.c_uint]),

@@ -80,6 +80,10 @@ void orc_umap_sgd_serial(int n, const int* offsets, const int* neighbors, const 
                          double* emb_colmajor, int n_epochs, double a, double b,
                          int negative_sample_rate, double learning_rate,
                          double repulsion_strength, int seed);
+void orc_umap_sgd_threaded(int n, const int* offsets, const int* neighbors, const float* weights,
+                           double* emb_colmajor, int n_epochs, double a, double b,
+                           int negative_sample_rate, double learning_rate,
+                           double repulsion_strength, int seed, int threads);
 void orc_umap_diffusion_init(const int* offsets, const int* neighbors, const float* weights, int n,
                              int index_offset, int n_iter, int seed, float* out);
 void orc_umap_spectral_init(const int* offsets, const int* neighbors, const float* weights, int n,

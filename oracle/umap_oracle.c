@@ -11,6 +11,9 @@
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 /* smooth_knn_dist, src/fast_knn_umap.cpp:876-1003 (distances column-major) */
 void orc_umap_smooth_knn(const float* dist, int n, int k, float* sigmas, float* rhos) {
@@ -390,6 +393,180 @@ void orc_umap_sgd_serial(int n, const int* offsets, const int* neighbors, const 
     }
   }
   free(arow); free(atail); free(eps); free(next); free(epsn); free(nextn);
+}
+
+static float clip4f(float x);
+
+/* TauPrng and make_tau_prng, src/fast_knn_umap.cpp:659-701: a per-(worker, epoch) xorshift32
+ * stream whose seed mixes the seed, the epoch, the worker and the end of its edge range. */
+static uint32_t tau_seed(uint32_t s0, uint32_t s1, uint32_t s2) {
+  const uint32_t st = mix_seed(s0 ^ (s1 << 7) ^ (s2 << 17));
+  return st == 0u ? 0x9e3779b9u : st;
+}
+
+static uint32_t tau_make(int seed, int epoch, size_t window_end, int worker) {
+  const uint32_t base = mix_seed((uint32_t)seed ^ (uint32_t)((uint32_t)(epoch + 1) * 0x9e3779b9u) ^
+                                 (uint32_t)((uint32_t)(worker + 1) * 0x85ebca6bu) ^
+                                 (uint32_t)((window_end + 1u) * 0xc2b2ae35u));
+  return tau_seed(mix_seed(base ^ 0xa341316cu), mix_seed(base ^ 0xc8013ea4u), mix_seed(base ^ 0xad90777du));
+}
+
+static int tau_vertex(uint32_t* st, int n) {
+  uint32_t x = *st;
+  x ^= x << 13;
+  x ^= x >> 17;
+  x ^= x << 5;
+  *st = x == 0u ? 0x9e3779b9u : x;
+  return (int)(*st % (uint32_t)n);
+}
+
+/* The multi-threaded branch of optimize_layout_csr (n_components = 2, more than one worker,
+ * n >= 10000), src/fast_knn_umap.cpp:3224-3350, which the package's default thread policy
+ * (umap_default_threads, R/fast_knn_umap.R:966-981: up to 4 workers at n >= 500, k >= 15) selects
+ * at these sizes. The edges are selected and scheduled as in the serial branch (:3116-3190);
+ * each worker runs every epoch over its own range of them (ranges end at row boundaries), moves
+ * float positions with atomic adds while the others do the same, draws negatives from its own
+ * stream, and the workers meet every 50 epochs and at the last. Asynchronous by construction,
+ * so results vary from run to run: a timing baseline for the reference's CPU path, not a parity
+ * pin (the serial branch above is). */
+void orc_umap_sgd_threaded(int n, const int* offsets, const int* neighbors, const float* weights,
+                           double* emb, int n_epochs, double a, double b, int nsr, double learning_rate,
+                           double gamma, int seed, int threads) {
+  double max_weight = 0.0;
+  for (int row = 0; row < n; ++row)
+    for (int pos = offsets[row]; pos < offsets[row + 1]; ++pos) {
+      const int nb = neighbors[pos];
+      if (nb >= 0 && nb < n && nb != row && (double)weights[pos] > max_weight) max_weight = weights[pos];
+    }
+  if (max_weight <= 0.0 || n_epochs < 1) return;
+  const double min_sample_weight = max_weight / (double)n_epochs;
+  const int64_t nnz = offsets[n];
+  const size_t cap = (size_t)(nnz > 0 ? nnz : 1);
+  int* arow = (int*)malloc(sizeof(int) * cap);
+  int* atail = (int*)malloc(sizeof(int) * cap);
+  float* eps = (float*)malloc(sizeof(float) * cap);
+  float* next = (float*)malloc(sizeof(float) * cap);
+  float* epsn = (float*)malloc(sizeof(float) * cap);
+  float* nextn = (float*)malloc(sizeof(float) * cap);
+  float* x = (float*)malloc(sizeof(float) * (size_t)n);
+  float* y = (float*)malloc(sizeof(float) * (size_t)n);
+  size_t na = 0;
+  for (int row = 0; row < n; ++row)
+    for (int pos = offsets[row]; pos < offsets[row + 1]; ++pos) {
+      const int nb = neighbors[pos];
+      if (nb >= 0 && nb < n && nb != row && (double)weights[pos] >= min_sample_weight) {
+        arow[na] = row;
+        atail[na] = nb;
+        const double wd = (double)weights[pos] > 1e-6 ? (double)weights[pos] : 1e-6;
+        eps[na] = (float)(max_weight / wd);
+        next[na] = eps[na];
+        if (nsr > 0) {
+          epsn[na] = eps[na] / (float)nsr;
+          nextn[na] = epsn[na];
+        } else {
+          epsn[na] = INFINITY;
+          nextn[na] = INFINITY;
+        }
+        ++na;
+      }
+    }
+  for (int i = 0; i < n; ++i) {
+    x[i] = (float)emb[i];
+    y[i] = (float)emb[(int64_t)n + i];
+  }
+  const float af = (float)a, bf = (float)b;
+  const float attraction = (float)(-2.0 * a * b), repulsion = (float)(2.0 * gamma * b);
+  const float alpha0 = (float)learning_rate, alpha_step = alpha0 / (float)n_epochs;
+  const float fe = FLT_EPSILON;
+  if (threads < 1) threads = 1;
+  size_t* begin = (size_t*)malloc(sizeof(size_t) * (size_t)(threads + 1));
+#pragma omp parallel num_threads(threads)
+  {
+#ifdef _OPENMP
+    const int t = omp_get_thread_num(), nt = omp_get_num_threads();
+#else
+    const int t = 0, nt = 1;
+#endif
+#pragma omp single
+    {
+      begin[0] = 0;
+      begin[nt] = na;
+      for (int w = 1; w < nt; ++w) {
+        size_t bd = na * (size_t)w / (size_t)nt;
+        while (bd < na && bd > 0 && arow[bd] == arow[bd - 1]) ++bd;
+        begin[w] = bd;
+      }
+    }
+    const size_t lo = begin[t], hi = begin[t + 1];
+    float alpha = alpha0;
+    for (int epoch = 0; epoch < n_epochs; ++epoch) {
+      uint32_t st = tau_make(seed, epoch, hi, t);
+      for (size_t i = lo; i < hi; ++i) {
+        if (next[i] > (float)epoch) continue;
+        const int j = arow[i], k = atail[i];
+        float hx, hy, tx, ty;
+#pragma omp atomic read
+        hx = x[j];
+#pragma omp atomic read
+        hy = y[j];
+#pragma omp atomic read
+        tx = x[k];
+#pragma omp atomic read
+        ty = y[k];
+        const float dx = hx - tx, dy = hy - ty;
+        const float d2 = fmaxf(fe, dx * dx + dy * dy);
+        const float dp = orc_umap_powf_fast(d2, bf);
+        const float gc = attraction * dp / (d2 * (af * dp + 1.0f));
+        const float gx = clip4f(gc * dx) * alpha, gy = clip4f(gc * dy) * alpha;
+#pragma omp atomic
+        x[j] += gx;
+#pragma omp atomic
+        y[j] += gy;
+#pragma omp atomic
+        x[k] += -gx;
+#pragma omp atomic
+        y[k] += -gy;
+        next[i] += eps[i];
+        int nneg = 0;
+        if (nsr > 0 && (float)epoch >= nextn[i]) {
+          nneg = (int)floorf(((float)epoch - nextn[i]) / epsn[i]);
+          if (nneg < 0) nneg = 0;
+        }
+        for (int p = 0; p < nneg; ++p) {
+          const int neg = tau_vertex(&st, n);
+          if (neg == j) continue;
+          float cx, cy, nx, ny;
+#pragma omp atomic read
+          cx = x[j];
+#pragma omp atomic read
+          cy = y[j];
+#pragma omp atomic read
+          nx = x[neg];
+#pragma omp atomic read
+          ny = y[neg];
+          const float ndx = cx - nx, ndy = cy - ny;
+          const float nd2 = fmaxf(fe, ndx * ndx + ndy * ndy);
+          const float np = orc_umap_powf_fast(nd2, bf);
+          const float rep = repulsion / ((0.001f + nd2) * (af * np + 1.0f));
+          const float rx = clip4f(rep * ndx) * alpha, ry = clip4f(rep * ndy) * alpha;
+#pragma omp atomic
+          x[j] += rx;
+#pragma omp atomic
+          y[j] += ry;
+        }
+        if (nneg > 0) nextn[i] += (float)nneg * epsn[i];
+      }
+      if ((epoch + 1) % 50 == 0 || epoch == n_epochs - 1) {
+#pragma omp barrier
+      }
+      alpha -= alpha_step;
+    }
+  }
+  for (int i = 0; i < n; ++i) {
+    emb[i] = (double)x[i];
+    emb[(int64_t)n + i] = (double)y[i];
+  }
+  free(begin); free(arow); free(atail); free(eps); free(next); free(epsn); free(nextn); free(x); free(y);
 }
 
 /* ---- COO epoch schedule of the reference CUDA optimizer, src/embedding_cuda_kernels.cpp ---- */
