@@ -2,8 +2,9 @@
  * CPU oracle, UMAP part. TEST INFRASTRUCTURE ONLY (see oracle.h).
  *
  * Restates the reference CPU UMAP pieces in fastEmbedR src/fast_knn_umap.cpp
- * (smooth-KNN, fuzzy-union CSR, a/b fit, serial SGD) and the COO epoch schedule
- * of src/embedding_cuda_kernels.cpp, each cited per function.
+ * (smooth-KNN, fuzzy-union CSR, a/b fit, serial SGD, and the asynchronous
+ * multi-threaded SGD branch, which only serves as a timing baseline) and the COO
+ * epoch schedule of src/embedding_cuda_kernels.cpp, each cited per function.
  */
 #include "oracle.h"
 
