@@ -303,7 +303,7 @@ class TsneBatch:
     own grid, bounding box, Z and learning rate (opt-SNE: n_b / early exaggeration). ``grid_size``:
     "cuda" (the CUDA size policy, 256 / 512 / 1024 nodes by n), "cpu" (the reference CPU policy,
     128 / 256), "adaptive" (per instance and per 25-iteration chunk, the smallest grid of at least
-    128 nodes with node spacing <= 0.7 over the current layout) or a power of two for every
+    256 nodes with node spacing <= 0.7 over the current layout) or a power of two for every
     instance."""
 
     def __init__(self, knns, perplexity=30.0, inits=None, grid_size="cuda", interpolation=0, seed=4):

@@ -11,6 +11,15 @@
 // The array is shared by every call: a call overwrites the whole region it uses before reading
 // it, so nothing needs clearing between calls, but calls that overlap on the GPU (concurrent
 // streams or threads) race on it and must be serialised by the caller.
+//
+// The first call on a device does the set-up for that device: with CUDA's lazy module loading
+// (the default since CUDA 12.2) it is the call that loads this file's device code, and with it
+// the 1.5 MB array, onto the GPU, and it looks up the array's device address
+// (cudaGetSymbolAddress, with that device current), which later calls on the device reuse.
+// Make that first call before a memory pool reserves the device's free memory, and before any
+// stream capture. The address stays valid for the life of the device's primary context; after
+// cudaDeviceReset the library must not be called again in that process.
+#include <cstdint>
 #include <mutex>
 
 #include "../../include/fastembedr_cuda.h"
@@ -64,6 +73,9 @@ extern "C" int fastembedr_cuda_tsne_exact_repulsion_noalloc(const float* layout,
                                                             double* sum_q, void* stream) {
   return fe::guarded([&] {
     if (!layout || !repulsive) throw fe::Error("null device pointer passed to the no-allocation t-SNE repulsion");
+    // the layout is read as float2 pairs
+    if ((reinterpret_cast<std::uintptr_t>(layout) & 7u) != 0u)
+      throw fe::Error("the no-allocation t-SNE repulsion needs an 8-byte aligned layout pointer");
     if (n < 2) throw fe::Error("the no-allocation t-SNE repulsion needs at least two points");
     if (n > fe::kNoAllocMaxPoints)
       throw fe::Error("n = " + std::to_string(n) + " exceeds the no-allocation scratch capacity of " +

@@ -510,10 +510,12 @@ __global__ void total_mass_kernel(const double* __restrict__ row_mass, const int
   }
 }
 
+// Entries of a row past its `real` count are padding (the row itself, value 0): they contribute
+// exactly nothing to forces and KL.
 __global__ void fill_csr_kernel(const unsigned long long* __restrict__ bucket, const long long* __restrict__ offs,
-                                const long long* __restrict__ row_ptr64, int n, const int* __restrict__ first,
-                                int ninst, const float* __restrict__ norm, int* __restrict__ row_ptr,
-                                int* __restrict__ col, float* __restrict__ val) {
+                                const long long* __restrict__ row_ptr64, const int* __restrict__ real, int n,
+                                const int* __restrict__ first, int ninst, const float* __restrict__ norm,
+                                int* __restrict__ row_ptr, int* __restrict__ col, float* __restrict__ val) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp > n) return;
@@ -529,11 +531,22 @@ __global__ void fill_csr_kernel(const unsigned long long* __restrict__ bucket, c
   const long long src = offs[warp];
   const long long dst = row_ptr64[warp];
   const int cnt = (int)(row_ptr64[warp + 1] - dst);
+  const int have = real[warp];
   for (int t = lane; t < cnt; t += 32) {
-    const unsigned long long e = bucket[src + t];
-    col[dst + t] = (int)(e >> 32);
-    val[dst + t] = __uint_as_float((unsigned)e) * nm;
+    if (t < have) {
+      const unsigned long long e = bucket[src + t];
+      col[dst + t] = (int)(e >> 32);
+      val[dst + t] = __uint_as_float((unsigned)e) * nm;
+    } else {
+      col[dst + t] = warp;
+      val[dst + t] = 0.0f;
+    }
   }
+}
+
+__global__ void pad_rows_kernel(int* __restrict__ count, const int2* __restrict__ pads, int m) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < m) count[pads[t].x] += pads[t].y;
 }
 
 void symmetrise(const int* d_idx, const float* d_p, int n, int k, int offset, DeviceCsr& out, cudaStream_t s) {
@@ -561,6 +574,8 @@ void symmetrise_batch(const int* d_idx, const float* d_p, int n, int k, int offs
   double* d_total = nullptr;
   float* d_norm = nullptr;
   int* d_first = nullptr;
+  int* pcount = nullptr;
+  int2* d_pads = nullptr;
   Arena work;
   work.reserve(&counts, n);
   work.reserve(&offs, n + 1);
@@ -577,6 +592,10 @@ void symmetrise_batch(const int* d_idx, const float* d_p, int n, int k, int offs
   work.reserve(&d_total, ninst);
   work.reserve(&d_norm, ninst);
   work.reserve(&d_first, ninst + 1);
+  if (ninst > 1) {
+    work.reserve(&pcount, n);
+    work.reserve(&d_pads, ninst);
+  }
   work.commit("t-SNE symmetrisation workspace");
   FE_CUDA(cudaMemcpyAsync(d_first, first.data(), sizeof(int) * (ninst + 1), cudaMemcpyHostToDevice, s));
 
@@ -611,12 +630,33 @@ void symmetrise_batch(const int* d_idx, const float* d_p, int n, int k, int offs
     FE_CUDA(cudaMemcpyAsync(&bounds[b], row_ptr64 + first[b], sizeof(long long), cudaMemcpyDeviceToHost, s));
   FE_CUDA(cudaMemcpyAsync(tot.data(), d_total, sizeof(double) * ninst, cudaMemcpyDeviceToHost, s));
   FE_CUDA(cudaStreamSynchronize(s));
-  const long long nnz = bounds[ninst];
+  long long nnz = bounds[ninst];
   double total = 0.0;
   for (int b = 0; b < ninst; ++b) {
     if (bounds[b + 1] <= bounds[b]) throw Error("KNN graph produced no non-self t-SNE edges.");
     if (!std::isfinite(tot[b]) || tot[b] <= 0.0) throw Error("t-SNE probability normalization failed.");
     total += tot[b];
+  }
+  const int* real = ucount;
+  if (ninst > 1) {
+    // every instance's entries start at a multiple of 4 (the attractive pass reads rows with
+    // 128-bit loads aligned to the array, so an instance then reads its rows exactly as it does
+    // alone): the last row of each instance is padded with zero entries
+    std::vector<int2> pads;
+    for (int b = 0; b + 1 < ninst; ++b) {
+      const long long cnt = bounds[b + 1] - bounds[b];
+      const int pad = (int)((4 - cnt % 4) % 4);
+      if (pad) pads.push_back(make_int2(first[b + 1] - 1, pad));
+    }
+    if (!pads.empty()) {
+      FE_CUDA(cudaMemcpyAsync(pcount, ucount, sizeof(int) * n, cudaMemcpyDeviceToDevice, s));
+      FE_CUDA(cudaMemcpyAsync(d_pads, pads.data(), sizeof(int2) * pads.size(), cudaMemcpyHostToDevice, s));
+      pad_rows_kernel<<<ceil_div((long long)pads.size(), 256), 256, 0, s>>>(pcount, d_pads, (int)pads.size());
+      FE_LAUNCH("pad_rows_kernel");
+      exclusive_scan(pcount, row_ptr64, n, scan_tmp, s);
+      for (const int2& p : pads) nnz += p.y;
+      FE_CUDA(cudaStreamSynchronize(s));
+    }
   }
   if (nnz > INT_MAX) throw Error("symmetrised t-SNE graph exceeds 2^31 - 1 entries.");
   if (totals) *totals = tot;
@@ -629,8 +669,8 @@ void symmetrise_batch(const int* d_idx, const float* d_p, int n, int k, int offs
   out.arena.reserve(&out.col, nnz);
   out.arena.reserve(&out.val, nnz);
   out.arena.commit("t-SNE CSR");
-  fill_csr_kernel<<<ceil_div((long long)(n + 1) * 32, 256), 256, 0, s>>>(bucket, offs, row_ptr64, n, d_first, ninst,
-                                                                          d_norm, out.row_ptr, out.col, out.val);
+  fill_csr_kernel<<<ceil_div((long long)(n + 1) * 32, 256), 256, 0, s>>>(bucket, offs, row_ptr64, real, n, d_first,
+                                                                          ninst, d_norm, out.row_ptr, out.col, out.val);
   FE_LAUNCH("fill_csr_kernel");
   FE_CUDA(cudaStreamSynchronize(s));
 }

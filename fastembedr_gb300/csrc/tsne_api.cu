@@ -113,9 +113,12 @@ struct TsneJob {
   // grid whose node spacing over its current bounding square is at most `spacing` (clamped to
   // [grid_min, grid_max]); grids grow at once and shrink only when four times too fine.
   bool reorder = true;  // periodic spatial reorder (FASTEMBEDR_TSNE_REORDER=0 turns it off), fixed at prepare
+  // The 256-node floor keeps small instances on the CUDA size policy's grid (below 20,000 points
+  // both give 256 nodes for final spans up to ~180), so adaptivity only coarsens the large
+  // instances whose policy grid is finer than their layout needs.
   bool adaptive = false;
   float spacing = 0.7f;
-  int grid_min = 128, grid_max = 1024;
+  int grid_min = 256, grid_max = 1024;
   int regrids = 0;
   ~TsneJob() { clear_graphs(); }
   void clear_graphs() {
@@ -183,6 +186,7 @@ struct TsneJob {
       FE_LAUNCH("random_init_kernel");
     }
     tsne_device_init(D, reinterpret_cast<const float*>(d_init), s);
+    tsne_bind_rows(D, P, s);
     FE_CUDA(cudaStreamSynchronize(s));
   }
 
@@ -297,6 +301,7 @@ struct TsneJob {
       }
     }
     tsne_device_init(D, reinterpret_cast<const float*>(d_init), s);
+    tsne_bind_rows(D, P, s);
     FE_CUDA(cudaStreamSynchronize(s));
   }
 
@@ -347,6 +352,15 @@ struct TsneJob {
     const float lr_normal = lr_auto ? (float)((double)n / std::max((double)exag, 1e-300)) : lr;
     run(early_iter, early_exag, lr_early, m0, min_gain, max_step, true);
     run(n_iter, exag, lr_normal, m1, min_gain, max_step, true);
+  }
+
+  // Per-instance learning-rate multipliers (table order), uploaded on the job's stream so that
+  // work already queued keeps the values it was queued with.
+  void set_lr_mult(const std::vector<float>& mult) {
+    for (std::size_t t = 0; t < D.inst.size(); ++t) D.inst[t].lr_mult = mult[t];
+    FE_CUDA(cudaMemcpyAsync(D.d_inst, D.inst.data(), sizeof(TsneInstance) * D.inst.size(), cudaMemcpyHostToDevice,
+                            stream.s));
+    FE_CUDA(cudaStreamSynchronize(stream.s));
   }
 
   void layout(float* out_host) {
@@ -883,11 +897,25 @@ int fastembedr_tsne_batch_run(fastembedr_tsne_batch* batch, int early_exaggerati
     if (!batch || early_exaggeration_iter < 0 || n_iter < 0 || !(early_exaggeration > 0.0f) ||
         !(exaggeration > 0.0f) || !(min_gain > 0.0f))
       throw fe::Error("invalid CUDA t-SNE batch schedule");
-    // opt-SNE rate of the package's auto configuration: n_b / early_exaggeration in both phases
-    const float lr = learning_rate > 0.0f ? learning_rate : 1.0f / early_exaggeration;
     fe::TsneJob& J = batch->job;
-    J.run(early_exaggeration_iter, early_exaggeration, lr, initial_momentum, min_gain, max_step_norm, true);
-    J.run(n_iter, exaggeration, lr, final_momentum, min_gain, max_step_norm, true);
+    if (learning_rate > 0.0f) {
+      J.run(early_exaggeration_iter, early_exaggeration, learning_rate, initial_momentum, min_gain, max_step_norm,
+            true);
+      J.run(n_iter, exaggeration, learning_rate, final_momentum, min_gain, max_step_norm, true);
+    } else {
+      // opt-SNE rate of the package's auto configuration, n_b / early_exaggeration in both phases,
+      // rounded once to float exactly as the one-instance path rounds it (so an instance of the
+      // batch takes the same steps as tsne_knn on its own)
+      std::vector<float> per(J.D.inst.size()), plain(J.D.inst.size());
+      for (std::size_t t = 0; t < per.size(); ++t) {
+        plain[t] = (float)J.D.inst[t].n;
+        per[t] = (float)((double)J.D.inst[t].n / (double)early_exaggeration);
+      }
+      J.set_lr_mult(per);
+      J.run(early_exaggeration_iter, early_exaggeration, 1.0f, initial_momentum, min_gain, max_step_norm, true);
+      J.run(n_iter, exaggeration, 1.0f, final_momentum, min_gain, max_step_norm, true);
+      J.set_lr_mult(plain);
+    }
     FE_CUDA(cudaStreamSynchronize(J.stream.s));
   });
 }

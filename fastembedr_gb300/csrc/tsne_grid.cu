@@ -130,6 +130,15 @@ __device__ void finish_layout_stats(const StepPartial* __restrict__ part, int nb
     g.mean_y = s_sy[0] / (double)n;
     g.z = 0.0;
     g.inv_z = 0.0f;
+    // |mass| and |mass * d| summed over any subset of points stay below 1.5625 n max(half, 1)
+    // (stencil weights sum to 1 in absolute value for bilinear, 1.5625 for Lagrange; |d| <= half):
+    // scale so that bound stays below 2^62.
+    float bound = 2.0f * (float)n * fmaxf(half, 1.0f);
+    if (!(bound < 1.0e30f)) bound = 1.0e30f;
+    int e = 0;
+    frexpf(bound, &e);  // bound < 2^e
+    g.qscale = ldexpf(1.0f, 62 - e);
+    g.inv_qscale = ldexpf(1.0f, e - 62);
     *next = g;
   }
 }
@@ -206,27 +215,36 @@ layout_stats_kernel(const float2* __restrict__ ynew, const TsneInstance* __restr
 // Points are stored in spatial (Morton) order and every block takes 256 consecutive points of one
 // instance, so a block covers a compact patch of the grid even when clusters collapse onto a few
 // cells:
-//   1. runs of equal stencil anchors inside a warp are summed by a segmented shuffle reduction;
-//   2. run heads accumulate into a kTile x kTile node tile in shared memory anchored at the
-//      block's lowest anchor (heads outside the tile go straight to global memory);
-//   3. the tile is flushed with one float4 vector atomic per touched node.
+//   1. runs of equal stencil anchors inside a warp are summed by a segmented shuffle reduction
+//      (a fixed tree: the same inputs give the same float sums);
+//   2. the run sums are turned into 64-bit fixed point (rounded to a multiple of 1 / qscale, about
+//      2^-62 of the largest possible node sum) and run heads accumulate into a kTile x kTile node
+//      tile in shared memory anchored at the block's lowest anchor (heads outside the tile go
+//      straight to global memory);
+//   3. the tile is flushed with integer atomics on the touched nodes.
+// Integer sums do not depend on the order in which atomics arrive, so the charges (and the
+// whole iteration) are deterministic.
 constexpr int kScatterTile = 32;
+
+__device__ __forceinline__ void red_add_i64(long long* p, long long v) {
+  atomicAdd(reinterpret_cast<unsigned long long*>(p), static_cast<unsigned long long>(v));
+}
 
 template <int TAPS>
 __global__ void __launch_bounds__(256)
 scatter_kernel(const float2* __restrict__ y, const TsneInstance* __restrict__ inst, const int2* __restrict__ blocks,
                GridState* __restrict__ cur, const GridState* __restrict__ next) {
   constexpr int NV = TAPS * TAPS * 3;
-  __shared__ float tile[kScatterTile * kScatterTile * 3];
+  __shared__ unsigned long long tile[kScatterTile * kScatterTile * 3];
   __shared__ int s_box[4];
   const int2 bl = blocks[blockIdx.x];
   const TsneInstance I = inst[bl.x];
   const int grid = I.grid;
-  float4* __restrict__ charges = I.charges;
+  long long* __restrict__ charges = I.charges;
   const GridState g = next[bl.x];
   if (bl.y == I.pt_begin && threadIdx.x == 0) cur[bl.x] = g;
   const int lane = threadIdx.x & 31;
-  for (int t = threadIdx.x; t < kScatterTile * kScatterTile * 3; t += blockDim.x) tile[t] = 0.0f;
+  for (int t = threadIdx.x; t < kScatterTile * kScatterTile * 3; t += blockDim.x) tile[t] = 0ull;
   if (threadIdx.x == 0) {
     s_box[0] = INT_MAX;
     s_box[1] = INT_MAX;
@@ -267,6 +285,9 @@ scatter_kernel(const float2* __restrict__ y, const TsneInstance* __restrict__ in
     }
   }
   const bool head = valid && ((heads >> lane) & 1u);
+  long long q[NV];
+#pragma unroll
+  for (int c = 0; c < NV; ++c) q[c] = __float2ll_rn(v[c] * g.qscale);
   __syncthreads();
   if (head) {
     atomicMin(&s_box[0], sx.base);
@@ -283,20 +304,22 @@ scatter_kernel(const float2* __restrict__ y, const TsneInstance* __restrict__ in
       for (int a = 0; a < TAPS; ++a)
 #pragma unroll
         for (int b = 0; b < TAPS; ++b) {
-          float* t = tile + ((ty + a) * kScatterTile + tx + b) * 3;
+          unsigned long long* t = tile + ((ty + a) * kScatterTile + tx + b) * 3;
           const int c = (a * TAPS + b) * 3;
-          atomicAdd(t, v[c]);
-          atomicAdd(t + 1, v[c + 1]);
-          atomicAdd(t + 2, v[c + 2]);
+          atomicAdd(t, (unsigned long long)q[c]);
+          atomicAdd(t + 1, (unsigned long long)q[c + 1]);
+          atomicAdd(t + 2, (unsigned long long)q[c + 2]);
         }
     } else {
 #pragma unroll
       for (int a = 0; a < TAPS; ++a) {
-        float4* row = charges + (long long)(sy.base + a) * grid + sx.base;
+        long long* row = charges + ((long long)(sy.base + a) * grid + sx.base) * kChargeStride;
 #pragma unroll
         for (int b = 0; b < TAPS; ++b) {
           const int c = (a * TAPS + b) * 3;
-          atomicAdd(row + b, make_float4(v[c], v[c + 1], v[c + 2], 0.0f));
+          red_add_i64(row + b * kChargeStride, q[c]);
+          red_add_i64(row + b * kChargeStride + 1, q[c + 1]);
+          red_add_i64(row + b * kChargeStride + 2, q[c + 2]);
         }
       }
     }
@@ -307,10 +330,14 @@ scatter_kernel(const float2* __restrict__ y, const TsneInstance* __restrict__ in
   const int hu = min(kScatterTile, s_box[3] - oy + TAPS);
   for (int t = threadIdx.x; t < wu * hu; t += blockDim.x) {
     const int r = t / wu, c = t - r * wu;
-    const float* src = tile + (r * kScatterTile + c) * 3;
-    const float a0 = src[0], a1 = src[1], a2 = src[2];
-    if (a0 != 0.0f || a1 != 0.0f || a2 != 0.0f)
-      atomicAdd(charges + (long long)(oy + r) * grid + ox + c, make_float4(a0, a1, a2, 0.0f));
+    const unsigned long long* src = tile + (r * kScatterTile + c) * 3;
+    const long long a0 = (long long)src[0], a1 = (long long)src[1], a2 = (long long)src[2];
+    if (a0 != 0 || a1 != 0 || a2 != 0) {
+      long long* dst = charges + ((long long)(oy + r) * grid + ox + c) * kChargeStride;
+      red_add_i64(dst, a0);
+      red_add_i64(dst + 1, a1);
+      red_add_i64(dst + 2, a2);
+    }
   }
 }
 
@@ -447,19 +474,21 @@ rows_forward_kernel(const TsneInstance* __restrict__ inst, const int* __restrict
   const int m = 1 << logm;
   const int r = blockIdx.x;
   const int b = members[blockIdx.y];
-  float4* __restrict__ charges = inst[b].charges;
+  long long* __restrict__ charges = inst[b].charges;
   cur += b;
   rows += (long long)blockIdx.y * 2 * nodes * m;
   krows += (long long)blockIdx.y * nodes * m;
   if (r < nodes) {
-    float4* crow = charges + (long long)r * grid;
+    longlong2* crow = reinterpret_cast<longlong2*>(charges + (long long)r * grid * kChargeStride);
+    const float inv_q = cur->inv_qscale;
     for (int c = threadIdx.x; c < m; c += blockDim.x) {
       float2 a = make_float2(0.0f, 0.0f), b = make_float2(0.0f, 0.0f);
       if (c < nodes) {
-        const float4 q = crow[c];
-        crow[c] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        a = make_float2(q.y, q.z);
-        b = make_float2(q.x, 0.0f);
+        const longlong2 q0 = crow[2 * c], q1 = crow[2 * c + 1];
+        crow[2 * c] = make_longlong2(0, 0);
+        crow[2 * c + 1] = make_longlong2(0, 0);
+        a = make_float2((float)q0.y * inv_q, (float)q1.x * inv_q);
+        b = make_float2((float)q0.x * inv_q, 0.0f);
       }
       sbuf[sidx(c)] = a;
       sbuf[sidx(m + c)] = b;
@@ -606,14 +635,23 @@ rows_inverse_kernel(const float2* __restrict__ rows, const TsneInstance* __restr
 // ---------------------------------------------------------------- attractive pass
 // a_i = exag * sum_j p_ij q_ij (y_i - y_j), q = 1 / (1 + d^2)
 // (add_sparse_attractive_gradient_f, src/tsne_neighbors.cpp:1061-1088).
-// Each warp owns a contiguous range of CSR rows (original point order), so the whole grid
-// streams P front to back. A row of up to 256 entries is covered by one round of 8 independent
-// coalesced loads per lane; lane 0 keeps a bulk L2 prefetch (cp.async.bulk.prefetch) running
-// kAttrAhead rows ahead, so the column/value loads of later rows hit L2 without holding
-// registers. Columns are storage slots (spatially sorted), so the y gathers of one row fall
-// into few sectors. Rows longer than 256 entries accumulate with per-lane Kahan sums.
+// Rows are taken in storage (spatial) order: slot_rows[s] = (begin, end) of the CSR row of the
+// point in slot s (rebuilt at every reorder), so a row is one contiguous segment of P and
+// consecutive rows of a warp belong to neighbouring points, whose neighbour sets overlap: their
+// y gathers hit L1. Warps take chunks of kAttrChunk consecutive slots from a counter (the last
+// warp to finish resets it for the next launch), which keeps every SM busy to the end whatever
+// the row lengths of a region. A row is read with 128-bit loads: lane l takes entries
+// c0 + 4 l .. + 3 of each 128-entry round (c0 = the row's first entry rounded down to a multiple
+// of 4; entries outside the row are masked), kAttrRounds rounds loaded before their gathers.
+// Lane 0 keeps a bulk L2 prefetch (cp.async.bulk.prefetch) of the row kAttrAhead rows ahead.
+// Each lane sums its entries in a fixed order, groups of rounds past the first 256 entries are
+// added with Kahan compensation, and the warp sum is a fixed butterfly: the force depends only
+// on the row and its entries' positions modulo 4, not on the schedule.
 constexpr int kAttrThreads = 256;
-constexpr int kAttrAhead = 3;
+constexpr int kAttrWarps = kAttrThreads / 32;
+constexpr int kAttrAhead = 2;
+constexpr int kAttrChunk = 32;  // slots per work item
+constexpr int kAttrRounds = 2;  // 128-entry rounds loaded together
 
 __device__ __forceinline__ void prefetch_l2_range(const void* base, long long first, long long last, int elem) {
   // [first, last) elements of a 4-byte array, widened to 16-byte boundaries (the arena pads
@@ -625,68 +663,132 @@ __device__ __forceinline__ void prefetch_l2_range(const void* base, long long fi
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a16), "r"((unsigned)(e16 - a16)) : "memory");
 }
 
+__device__ __forceinline__ int int4_at(const int4& v, int c) { return c == 0 ? v.x : c == 1 ? v.y : c == 2 ? v.z : v.w; }
+__device__ __forceinline__ float float4_at(const float4& v, int c) {
+  return c == 0 ? v.x : c == 1 ? v.y : c == 2 ? v.z : v.w;
+}
+
+// Butterfly of lane partials (x, y): the warp's x sum ends in lanes 0-15, its y sum in lanes
+// 16-31 (fixed order).
+__device__ __forceinline__ float butterfly_xy(float x, float y, int lane) {
+  const bool upper = lane >= 16;
+  float keep = upper ? y : x;
+  const float send = upper ? x : y;
+  keep += __shfl_xor_sync(0xffffffffu, send, 16);
+  keep += __shfl_xor_sync(0xffffffffu, keep, 8);
+  keep += __shfl_xor_sync(0xffffffffu, keep, 4);
+  keep += __shfl_xor_sync(0xffffffffu, keep, 2);
+  keep += __shfl_xor_sync(0xffffffffu, keep, 1);
+  return keep;
+}
+
+__device__ __forceinline__ void prefetch_row(const int2* __restrict__ slot_rows, const int* col, const float* val,
+                                             int s) {
+  const int2 se = __ldg(slot_rows + s);
+  prefetch_l2_range(col, se.x, se.y, 4);
+  prefetch_l2_range(val, se.x, se.y, 4);
+}
+
 __global__ void __launch_bounds__(kAttrThreads)
-attractive_kernel(const int* __restrict__ row_ptr, const int* __restrict__ col, const float* __restrict__ val,
-                  const float2* __restrict__ y, const int* __restrict__ inv, int n, float exag,
-                  float2* __restrict__ attr) {
+attractive_kernel(const int2* __restrict__ slot_rows, const int* __restrict__ col, const float* __restrict__ val,
+                  const float2* __restrict__ y, int n, float exag, float2* __restrict__ attr,
+                  unsigned* __restrict__ ctr) {
   const int lane = threadIdx.x & 31;
-  const long long warps_total = (long long)gridDim.x * (blockDim.x >> 5);
-  const long long w = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int r0 = (int)(w * n / warps_total), r1 = (int)((w + 1) * n / warps_total);
-  if (lane == 0 && r0 < r1) {
-    const int pe = min(r1, r0 + kAttrAhead);
-    prefetch_l2_range(col, row_ptr[r0], row_ptr[pe], 4);
-    prefetch_l2_range(val, row_ptr[r0], row_ptr[pe], 4);
+  const unsigned nchunks = (unsigned)((n + kAttrChunk - 1) / kAttrChunk);
+  unsigned c = 0, next = 0;
+  if (lane == 0) {
+    c = atomicAdd(ctr, 1u);
+    next = atomicAdd(ctr, 1u);
   }
-  for (int i = r0; i < r1; ++i) {
-    if (lane == 0 && i + kAttrAhead < r1) {
-      const int j = i + kAttrAhead;
-      const int pb = __ldg(row_ptr + j), pe = __ldg(row_ptr + j + 1);
-      prefetch_l2_range(col, pb, pe, 4);
-      prefetch_l2_range(val, pb, pe, 4);
+  c = __shfl_sync(0xffffffffu, c, 0);
+  next = __shfl_sync(0xffffffffu, next, 0);
+  // slot at position t of chunk c (positions past the chunk run into chunk `next`), or -1
+  auto slot_at = [&](int t) -> int {
+    const unsigned ch = t < kAttrChunk ? c : next;
+    if (ch >= nchunks) return -1;
+    const int sl = (int)ch * kAttrChunk + (t < kAttrChunk ? t : t - kAttrChunk);
+    return sl < n ? sl : -1;
+  };
+  if (lane == 0)
+    for (int a = 0; a < kAttrAhead; ++a) {
+      const int t = slot_at(a);
+      if (t >= 0) prefetch_row(slot_rows, col, val, t);
     }
-    const int b = __ldg(row_ptr + i), e = __ldg(row_ptr + i + 1);
-    const int si = inv ? __ldg(inv + i) : i;
-    const float2 yi = __ldg(y + si);
-    float ax = 0.0f, ay = 0.0f;
-    if (e - b <= 256) {
-      int ci[8];
-      float v[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int q = b + lane + 32 * u;
-        ci[u] = q < e ? __ldcs(col + q) : si;
-        v[u] = q < e ? __ldcs(val + q) : 0.0f;
+  while (c < nchunks) {
+    for (int t = 0; t < kAttrChunk; ++t) {
+      const int s = slot_at(t);
+      if (s < 0) break;
+      if (lane == 0) {
+        const int pf = slot_at(t + kAttrAhead);
+        if (pf >= 0) prefetch_row(slot_rows, col, val, pf);
       }
+      const int2 se = __ldg(slot_rows + s);
+      const float2 yi = __ldg(y + s);
+      const int b = se.x, e = se.y;
+      float ax = 0.0f, ay = 0.0f, kx = 0.0f, ky = 0.0f;
+      for (int c0 = b & ~3; c0 < e; c0 += 128 * kAttrRounds) {
+        int4 ci[kAttrRounds];
+        float4 vv[kAttrRounds];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const float2 yj = __ldg(y + ci[u]);
-        const float dx = yi.x - yj.x, dy = yi.y - yj.y;
-        const float q = 1.0f / (1.0f + (dx * dx + dy * dy));
-        const float c = exag * v[u] * q;
-        ax += c * dx;
-        ay += c * dy;
-      }
-    } else {
-      float kx = 0.0f, ky = 0.0f;
-      for (int p = b + lane; p < e; p += 32) {
-        const int j = __ldcs(col + p);
-        const float pv = __ldcs(val + p);
-        const float2 yj = __ldg(y + j);
-        const float dx = yi.x - yj.x, dy = yi.y - yj.y;
-        const float q = 1.0f / (1.0f + (dx * dx + dy * dy));
-        const float c = exag * pv * q;
-        const float tx = c * dx - kx, ty = c * dy - ky;
+        for (int u = 0; u < kAttrRounds; ++u) {
+          const int p = c0 + 128 * u + 4 * lane;
+          if (p < e) {
+            ci[u] = __ldcs(reinterpret_cast<const int4*>(col + p));
+            vv[u] = __ldcs(reinterpret_cast<const float4*>(val + p));
+          } else {
+            ci[u] = make_int4(s, s, s, s);
+            vv[u] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+          }
+        }
+        float rx = 0.0f, ry = 0.0f;
+#pragma unroll
+        for (int u = 0; u < kAttrRounds; ++u) {
+#pragma unroll
+          for (int cc = 0; cc < 4; ++cc) {
+            const int p = c0 + 128 * u + 4 * lane + cc;
+            const bool ok = p >= b && p < e;
+            const float w = ok ? float4_at(vv[u], cc) : 0.0f;
+            const float2 yj = ok ? __ldg(y + int4_at(ci[u], cc)) : yi;
+            const float dx = yi.x - yj.x, dy = yi.y - yj.y;
+            const float q = 1.0f / (1.0f + (dx * dx + dy * dy));
+            const float cq = w * q;
+            rx += cq * dx;
+            ry += cq * dy;
+          }
+        }
+        const float tx = rx - kx, ty = ry - ky;
         const float nx = ax + tx, ny = ay + ty;
         kx = (nx - ax) - tx;
         ky = (ny - ay) - ty;
         ax = nx;
         ay = ny;
       }
+      const float keep = butterfly_xy(ax, ay, lane);
+      const float sy = __shfl_sync(0xffffffffu, keep, 16);
+      if (lane == 0) attr[s] = make_float2(exag * keep, exag * sy);
     }
-    ax = warp_sum(ax);
-    ay = warp_sum(ay);
-    if (lane == 0) attr[si] = make_float2(ax, ay);
+    c = next;
+    if (c < nchunks) {
+      if (lane == 0) next = atomicAdd(ctr, 1u);
+      next = __shfl_sync(0xffffffffu, next, 0);
+    }
+  }
+  if (lane == 0) {
+    __threadfence();
+    const unsigned done = atomicAdd(ctr + 1, 1u);
+    if (done == gridDim.x * kAttrWarps - 1u) {
+      atomicExch(ctr, 0u);
+      atomicExch(ctr + 1, 0u);
+    }
+  }
+}
+
+// slot_rows[t] = CSR segment of the point stored in slot t.
+__global__ void bind_rows_kernel(const int* __restrict__ perm, const int* __restrict__ row_ptr, int n,
+                                 int2* __restrict__ slot_rows) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int o = perm[t];
+    slot_rows[t] = make_int2(row_ptr[o], row_ptr[o + 1]);
   }
 }
 
@@ -844,8 +946,9 @@ __global__ void gather_points_kernel(const int* __restrict__ order, int n, const
 }
 
 __global__ void scatter_points_kernel(const float2* __restrict__ scratch, const int* __restrict__ perm_tmp, int n,
-                                      float2* __restrict__ y, float2* __restrict__ gains,
-                                      float2* __restrict__ update, int* __restrict__ perm, int* __restrict__ inv) {
+                                      const int* __restrict__ row_ptr, float2* __restrict__ y,
+                                      float2* __restrict__ gains, float2* __restrict__ update, int* __restrict__ perm,
+                                      int* __restrict__ inv, int2* __restrict__ slot_rows) {
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
     y[r] = scratch[r];
     gains[r] = scratch[n + r];
@@ -853,6 +956,7 @@ __global__ void scatter_points_kernel(const float2* __restrict__ scratch, const 
     const int o = perm_tmp[r];
     perm[r] = o;
     inv[o] = r;
+    slot_rows[r] = make_int2(row_ptr[o], row_ptr[o + 1]);
   }
 }
 
@@ -929,7 +1033,7 @@ void build_grid_classes(TsneDevice& d, const std::vector<int>& grids) {
     k.cols_per_block = k.fft >= 512 ? 2 : 1;
     k.col_blocks = k.fft / k.cols_per_block;
     const std::size_t m = k.fft;
-    d.grid_arena.reserve(&k.charges, (std::size_t)k.count * k.grid * k.grid);
+    d.grid_arena.reserve(&k.charges, (std::size_t)k.count * k.grid * k.grid * kChargeStride);
     d.grid_arena.reserve(&k.potential, (std::size_t)k.count * k.grid * k.grid);
     d.grid_arena.reserve(&k.rows, (std::size_t)k.count * 2 * k.nodes * m);
     d.grid_arena.reserve(&k.krows, (std::size_t)k.count * k.nodes * m);
@@ -951,7 +1055,7 @@ void build_grid_classes(TsneDevice& d, const std::vector<int>& grids) {
       TsneInstance& I = d.inst[b];
       I.grid = k.grid;
       I.nodes = k.nodes;
-      I.charges = k.charges + (std::size_t)j * k.grid * k.grid;
+      I.charges = k.charges + (std::size_t)j * k.grid * k.grid * kChargeStride;
       I.potential = k.potential + (std::size_t)j * k.grid * k.grid;
     }
     std::vector<float2> tw(m / 2);
@@ -960,7 +1064,7 @@ void build_grid_classes(TsneDevice& d, const std::vector<int>& grids) {
       tw[t] = make_float2((float)std::cos(ang), (float)std::sin(ang));
     }
     FE_CUDA(cudaMemcpy(k.twiddle, tw.data(), sizeof(float2) * tw.size(), cudaMemcpyHostToDevice));
-    FE_CUDA(cudaMemset(k.charges, 0, sizeof(float4) * (std::size_t)k.count * k.grid * k.grid));
+    FE_CUDA(cudaMemset(k.charges, 0, sizeof(long long) * kChargeStride * (std::size_t)k.count * k.grid * k.grid));
     FE_CUDA(cudaMemset(k.potential, 0, sizeof(float4) * (std::size_t)k.count * k.grid * k.grid));
   }
   FE_CUDA(cudaMemcpy(d_members, flat.data(), sizeof(int) * ninst, cudaMemcpyHostToDevice));
@@ -1016,6 +1120,8 @@ void tsne_batch_alloc(TsneDevice& d, const std::vector<int>& sizes, const std::v
   const int nb = radix_sort_blocks(n);
   d.arena.reserve(&d.perm, n);
   d.arena.reserve(&d.inv, n);
+  d.arena.reserve(&d.slot_rows, n);
+  d.arena.reserve(&d.attr_ctr, 2);
   d.arena.reserve(&d.keys, n);
   d.arena.reserve(&d.keys_tmp, n);
   d.arena.reserve(&d.order, n);
@@ -1036,6 +1142,7 @@ void tsne_batch_alloc(TsneDevice& d, const std::vector<int>& sizes, const std::v
   FE_CUDA(cudaMemcpy(d.d_inst, d.inst.data(), sizeof(TsneInstance) * ninst, cudaMemcpyHostToDevice));
   FE_CUDA(cudaMemcpy(d.blocks, blk.data(), sizeof(int2) * nblocks, cudaMemcpyHostToDevice));
   FE_CUDA(cudaMemset(d.counter, 0, sizeof(unsigned) * ninst));
+  FE_CUDA(cudaMemset(d.attr_ctr, 0, sizeof(unsigned) * 2));
   FE_CUDA(cudaMemset(d.cur, 0, sizeof(GridState) * ninst));
   if (!d.side) FE_CUDA(cudaStreamCreateWithFlags(&d.side, cudaStreamNonBlocking));
   if (!d.fork) FE_CUDA(cudaEventCreateWithFlags(&d.fork, cudaEventDisableTiming));
@@ -1097,9 +1204,15 @@ void tsne_grid_stage(TsneDevice& d, cudaStream_t s) {
   }
 }
 
+void tsne_bind_rows(TsneDevice& d, const DeviceCsr& P, cudaStream_t s) {
+  if (P.n != d.n) throw Error("t-SNE: P and the optimizer state have different sizes");
+  bind_rows_kernel<<<point_blocks(d.n), 256, 0, s>>>(d.perm, P.row_ptr, d.n, d.slot_rows);
+  FE_LAUNCH("bind_rows_kernel");
+}
+
 void tsne_attractive_stage(TsneDevice& d, const DeviceCsr& P, float exag, cudaStream_t s) {
-  attractive_kernel<<<d.attr_blocks, kAttrThreads, 0, s>>>(P.row_ptr, P.col, P.val, d.y, d.inv, d.n, exag,
-                                                           d.attr);
+  attractive_kernel<<<d.attr_blocks, kAttrThreads, 0, s>>>(d.slot_rows, P.col, P.val, d.y, d.n, exag, d.attr,
+                                                           d.attr_ctr);
   FE_LAUNCH("attractive_kernel");
 }
 
@@ -1161,8 +1274,8 @@ void tsne_reorder(TsneDevice& d, DeviceCsr& P, cudaStream_t s) {
   gather_points_kernel<<<point_blocks(n), 256, 0, s>>>(d.order, n, d.y, d.gains, d.update, d.perm, d.scratch,
                                                        d.perm_tmp, d.delta);
   FE_LAUNCH("gather_points_kernel");
-  scatter_points_kernel<<<point_blocks(n), 256, 0, s>>>(d.scratch, d.perm_tmp, n, d.y, d.gains, d.update, d.perm,
-                                                        d.inv);
+  scatter_points_kernel<<<point_blocks(n), 256, 0, s>>>(d.scratch, d.perm_tmp, n, P.row_ptr, d.y, d.gains, d.update,
+                                                        d.perm, d.inv, d.slot_rows);
   FE_LAUNCH("scatter_points_kernel");
   relabel_cols_kernel<<<std::max(1, std::min(ceil_div(P.nnz, 256), sm_count() * 16)), 256, 0, s>>>(P.col, P.nnz,
                                                                                                    d.delta);

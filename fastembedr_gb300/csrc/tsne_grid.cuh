@@ -20,7 +20,16 @@ struct GridState {
   double z;            // sum_{i != j} q_ij from the grid
   float inv_z;
   int nodes;           // nodes used per side (G for bilinear, 3 * floor(G / 3) for Lagrange)
+  // Charges are summed as 64-bit fixed-point integers (value x qscale, qscale a power of two
+  // chosen from n and the grid's half-width so no partial sum can overflow): integer addition is
+  // associative, so the grid, and with it every later step, is the same whatever order the
+  // atomics land in.
+  float qscale, inv_qscale;
 };
+
+// Fixed-point charges of one grid node: mass, mass * dx, mass * dy and a pad slot, so a node is
+// one 32-byte sector.
+constexpr int kChargeStride = 4;
 
 struct StepPartial {
   float min_x, max_x, min_y, max_y;
@@ -34,7 +43,7 @@ struct TsneInstance {
   int grid, nodes;          // G and the nodes used per side
   int block_begin, blocks;  // point blocks of this instance (and its StepPartial slice)
   float lr_mult;            // learning rate of this instance = run learning rate x lr_mult
-  float4* charges;          // G x G (mass, mass*dx, mass*dy, 0)
+  long long* charges;       // G x G x kChargeStride fixed-point (mass, mass*dx, mass*dy, 0)
   float4* potential;        // G x G (phi_q2, phi_x, phi_y, 0)
 };
 
@@ -48,7 +57,7 @@ struct GridClass {
   float2* krows = nullptr;    // count x (nodes x (M/2 + 1)): row-transformed kernel (q, q^2)
   double* zpart = nullptr;    // count x col_blocks
   float2* twiddle = nullptr;  // M / 2 forward twiddles
-  float4* charges = nullptr;  // count x G x G
+  long long* charges = nullptr;  // count x G x G x kChargeStride
   float4* potential = nullptr;
 };
 
@@ -80,6 +89,8 @@ struct TsneDevice {
   // leave their instance's slot range.
   int* perm = nullptr;
   int* inv = nullptr;
+  int2* slot_rows = nullptr;     // CSR segment (begin, end) of the point in each storage slot
+  unsigned* attr_ctr = nullptr;  // work counters of the attractive pass (zero between launches)
   unsigned* keys = nullptr;
   unsigned* keys_tmp = nullptr;
   int* order = nullptr;
@@ -117,6 +128,8 @@ void tsne_regrid(TsneDevice& d, const std::vector<int>& grids, cudaStream_t s);
 std::vector<float> tsne_grid_extents(TsneDevice& d, cudaStream_t s);
 // Copy a row-major float2 init into the layout, reset gains/update and compute `next`.
 void tsne_device_init(TsneDevice& d, const float* d_init, cudaStream_t s);
+// Point every storage slot at its CSR row (after init; the reorder keeps it current).
+void tsne_bind_rows(TsneDevice& d, const DeviceCsr& P, cudaStream_t s);
 // One optimizer iteration: grid stage on `s` concurrently with the attractive pass on the side
 // stream, then the update (3 + 3 x grid classes launches).
 void tsne_iteration(TsneDevice& d, const DeviceCsr& P, float exaggeration, float learning_rate, float momentum,

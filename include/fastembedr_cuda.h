@@ -231,10 +231,12 @@ int fastembedr_cuda_tsne_force_diagnostic(const int* indices, const float* dista
  * For callers that cannot call cudaMalloc where they need the result (the GPU's memory is owned
  * by another framework's pool, or a serving loop forbids allocation on its request path).
  * layout (row-major n x 2 floats), repulsive (n x 2 floats) and sum_q (1 double, may be NULL) are
- * caller-owned DEVICE pointers; the working memory is a fixed array inside the library, so
- * n <= 65536 (larger n is rejected with an error). The first call on a device resolves that
- * array's address on the device (make it before any stream capture). Every call reuses the same
- * array, so calls that overlap on the GPU race and must be serialised by the caller. `stream` is a
+ * caller-owned DEVICE pointers (layout 8-byte aligned); the working memory is a fixed 1.5 MB array
+ * inside the library, so n <= 65536 (larger n is rejected with an error). The first call on a
+ * device loads that array onto the device (CUDA loads modules lazily) and resolves its address:
+ * make it before a memory pool reserves the device's free memory and before any stream capture.
+ * Every call reuses the same array, so calls that overlap on the GPU race and must be serialised
+ * by the caller. `stream` is a
  * cudaStream_t (NULL: the legacy default stream); the call returns after the stream has finished.
  * Output equals the repulsive_exact / z_exact of fastembedr_cuda_tsne_force_diagnostic. */
 int fastembedr_cuda_tsne_exact_repulsion_noalloc(const float* layout, int n, float* repulsive, double* sum_q,
