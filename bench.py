@@ -917,7 +917,8 @@ def batched_result(args, local):
     # plain form on a size-stratified subset: every `stride`-th instance by size, one call each
     order = np.argsort(sizes)
     subset = order[:: max(1, args.plain_stride)]
-    kl_rows = [j for j in subset if sizes[j] <= 60_000][: args.kl_instances]
+    # KL checks on instances spread over the whole size range (the subset is in size order)
+    kl_rows = [int(subset[i]) for i in np.unique(np.linspace(0, len(subset) - 1, args.kl_instances).astype(int))]
     plain_t, plain_work, plain_kl, plain_lay = 0.0, 0.0, {}, {}
     for j in subset:
         idx, dist = knns[j]
