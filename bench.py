@@ -974,6 +974,41 @@ def batched_result(args, local):
     return line
 
 
+def run_grid_calibration(args):
+    """Calibration of the adaptive box count: KL, final span and time per iteration of one t-SNE
+    instance per (size, grid) pair, each run as a batch of one with a fixed grid size (250 early-
+    exaggeration + 750 normal iterations, opt-SNE rate n / 12; 50-d mixture of 10 log-normal
+    clusters, exact k = 90 KNN, perplexity 30). One JSON line per (n, G)."""
+    import torch
+
+    from fastembedr_gb300 import api
+    from fastembedr_gb300 import synthetic as S
+
+    for n in (2000, 10000, 50000, 200000):
+        x, _ = S.mixture(n, 50, 10, 11, centre_sd=4.0, lognormal_sizes=True)
+        idx, dist = S.exact_knn_torch(x, K)
+        knn = (idx.cpu().numpy(), dist.cpu().numpy())
+        init = S.tsne_init(n, seed=5)
+        for g in (64, 128, 256, 512, 1024):
+            if n <= 10000 and g > 512:
+                continue
+            with api.TsneBatch([knn], perplexity=PERPLEXITY, inits=[init], grid_size=g) as b:
+                stream = torch.cuda.ExternalStream(b.stream)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                b.iterate(250, 12.0, 1.0 / 12.0)
+                b.synchronize()
+                e0.record(stream)
+                b.iterate(750, 1.0, 1.0 / 12.0)
+                e1.record(stream)
+                b.synchronize()
+                lay = b.layouts()[0]
+                kl = b.kl(0)
+            span = float(np.ptp(lay, 0).max())
+            print(json.dumps(dict(n=n, G=g, kl=kl, span=span, h=1.1 * span / (g - 1),
+                                  ms_iter=e0.elapsed_time(e1) / 750)), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -987,7 +1022,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adaptive", action="store_true", help="skip the adaptive-grid run of the 1M instance")
     ap.add_argument("--n", type=int, default=N_POINTS, help="points (profiling captures use a smaller case)")
-    ap.add_argument("--workload", default="tsne", choices=["tsne", "serving", "umap", "batched"],
+    ap.add_argument("--workload", default="tsne", choices=["tsne", "serving", "umap", "batched", "grid-calibration"],
                     help="tsne: the headline 1M-point optimizer; serving: transform_tsne served; umap: 100k UMAP; "
                          "batched: many t-SNE instances per launch")
     ap.add_argument("--instances", type=int, default=512, help="batched: half t-SNE (k = 90), half UMAP (k = 15)")
@@ -1002,6 +1037,8 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.workload == "grid-calibration":
+        return run_grid_calibration(args)
     if args.workload == "serving":
         return run_serving_reference(args) if args.impl == "reference" else run_serving(args)
     if args.workload == "umap":

@@ -30,11 +30,22 @@ f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 
 
+def reference_sources():
+    """Directory of the reference's C++ sources (its src/), from FASTEMBEDR_REFERENCE_SRC; None
+    when unset or missing. Only the build of the reference library reads it."""
+    path = os.environ.get("FASTEMBEDR_REFERENCE_SRC", "")
+    return path if path and os.path.isdir(path) else None
+
+
 def build(ref: bool = False) -> None:
-    """Compile liborc.so (and the reference library when ``ref``)."""
+    """Compile liborc.so (and the reference library when ``ref`` and the reference sources are
+    given by FASTEMBEDR_REFERENCE_SRC)."""
     subprocess.run(["make", "-s", "-C", HERE, "liborc.so"], check=True)
+    src = reference_sources()
     if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        if src is None:
+            raise FileNotFoundError("set FASTEMBEDR_REFERENCE_SRC to the reference's src/ directory")
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_SRC={src}"], check=True)
 
 
 def ref_available() -> bool:

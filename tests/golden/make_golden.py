@@ -3,8 +3,9 @@
 Runs fastEmbedR's src/tsne_neighbors.cpp and src/fast_knn_umap.cpp, compiled where
 they lie against the test-only Rcpp shim (``make -C oracle ref``), on small seeded
 inputs and stores inputs + outputs. The fixtures travel with the repository; the
-reference sources do not. Re-run with:  python tests/golden/make_golden.py
-(or ``python tests/golden/make_golden.py umap_diffusion`` for one case).
+reference sources do not. Re-run with
+    FASTEMBEDR_REFERENCE_SRC=<the reference's src/ directory> python tests/golden/make_golden.py
+(or ``... make_golden.py umap_diffusion`` for one case).
 """
 from __future__ import annotations
 
