@@ -139,6 +139,13 @@ __device__ void finish_layout_stats(const StepPartial* __restrict__ part, int nb
     frexpf(bound, &e);  // bound < 2^e
     g.qscale = ldexpf(1.0f, 62 - e);
     g.inv_qscale = ldexpf(1.0f, e - 62);
+    // the same bound over the points of one block (at most kPointBlock), below 2^30
+    float tbound = 2.0f * (float)min(n, kPointBlock) * fmaxf(half, 1.0f);
+    if (!(tbound < 1.0e30f)) tbound = 1.0e30f;
+    int et = 0;
+    frexpf(tbound, &et);
+    g.tile_shift = (62 - e) - (30 - et);  // >= 0: et <= e
+    g.tscale = ldexpf(1.0f, 30 - et);
     *next = g;
   }
 }
@@ -217,11 +224,12 @@ layout_stats_kernel(const float2* __restrict__ ynew, const TsneInstance* __restr
 // cells:
 //   1. runs of equal stencil anchors inside a warp are summed by a segmented shuffle reduction
 //      (a fixed tree: the same inputs give the same float sums);
-//   2. the run sums are turned into 64-bit fixed point (rounded to a multiple of 1 / qscale, about
-//      2^-62 of the largest possible node sum) and run heads accumulate into a kTile x kTile node
-//      tile in shared memory anchored at the block's lowest anchor (heads outside the tile go
-//      straight to global memory);
-//   3. the tile is flushed with integer atomics on the touched nodes.
+//   2. run heads accumulate into a kTile x kTile node tile in shared memory anchored at the block's
+//      lowest anchor, in 32-bit fixed point (the run sums rounded to a multiple of 1 / tscale,
+//      about 2^-30 of the largest sum a block can make; native 32-bit shared atomics); heads
+//      outside the tile add to the grid directly in 64-bit fixed point (x qscale);
+//   3. the tile is flushed with one 64-bit integer atomic per touched node and value, the tile sum
+//      shifted up to the grid's scale (exact: both scales are powers of two).
 // Integer sums do not depend on the order in which atomics arrive, so the charges (and the
 // whole iteration) are deterministic.
 constexpr int kScatterTile = 32;
@@ -235,7 +243,7 @@ __global__ void __launch_bounds__(256)
 scatter_kernel(const float2* __restrict__ y, const TsneInstance* __restrict__ inst, const int2* __restrict__ blocks,
                GridState* __restrict__ cur, const GridState* __restrict__ next) {
   constexpr int NV = TAPS * TAPS * 3;
-  __shared__ unsigned long long tile[kScatterTile * kScatterTile * 3];
+  __shared__ int tile[kScatterTile * kScatterTile * 3];
   __shared__ int s_box[4];
   const int2 bl = blocks[blockIdx.x];
   const TsneInstance I = inst[bl.x];
@@ -244,7 +252,7 @@ scatter_kernel(const float2* __restrict__ y, const TsneInstance* __restrict__ in
   const GridState g = next[bl.x];
   if (bl.y == I.pt_begin && threadIdx.x == 0) cur[bl.x] = g;
   const int lane = threadIdx.x & 31;
-  for (int t = threadIdx.x; t < kScatterTile * kScatterTile * 3; t += blockDim.x) tile[t] = 0ull;
+  for (int t = threadIdx.x; t < kScatterTile * kScatterTile * 3; t += blockDim.x) tile[t] = 0;
   if (threadIdx.x == 0) {
     s_box[0] = INT_MAX;
     s_box[1] = INT_MAX;
@@ -285,9 +293,6 @@ scatter_kernel(const float2* __restrict__ y, const TsneInstance* __restrict__ in
     }
   }
   const bool head = valid && ((heads >> lane) & 1u);
-  long long q[NV];
-#pragma unroll
-  for (int c = 0; c < NV; ++c) q[c] = __float2ll_rn(v[c] * g.qscale);
   __syncthreads();
   if (head) {
     atomicMin(&s_box[0], sx.base);
@@ -304,11 +309,11 @@ scatter_kernel(const float2* __restrict__ y, const TsneInstance* __restrict__ in
       for (int a = 0; a < TAPS; ++a)
 #pragma unroll
         for (int b = 0; b < TAPS; ++b) {
-          unsigned long long* t = tile + ((ty + a) * kScatterTile + tx + b) * 3;
+          int* t = tile + ((ty + a) * kScatterTile + tx + b) * 3;
           const int c = (a * TAPS + b) * 3;
-          atomicAdd(t, (unsigned long long)q[c]);
-          atomicAdd(t + 1, (unsigned long long)q[c + 1]);
-          atomicAdd(t + 2, (unsigned long long)q[c + 2]);
+          atomicAdd(t, __float2int_rn(v[c] * g.tscale));
+          atomicAdd(t + 1, __float2int_rn(v[c + 1] * g.tscale));
+          atomicAdd(t + 2, __float2int_rn(v[c + 2] * g.tscale));
         }
     } else {
 #pragma unroll
@@ -317,9 +322,9 @@ scatter_kernel(const float2* __restrict__ y, const TsneInstance* __restrict__ in
 #pragma unroll
         for (int b = 0; b < TAPS; ++b) {
           const int c = (a * TAPS + b) * 3;
-          red_add_i64(row + b * kChargeStride, q[c]);
-          red_add_i64(row + b * kChargeStride + 1, q[c + 1]);
-          red_add_i64(row + b * kChargeStride + 2, q[c + 2]);
+          red_add_i64(row + b * kChargeStride, __float2ll_rn(v[c] * g.qscale));
+          red_add_i64(row + b * kChargeStride + 1, __float2ll_rn(v[c + 1] * g.qscale));
+          red_add_i64(row + b * kChargeStride + 2, __float2ll_rn(v[c + 2] * g.qscale));
         }
       }
     }
@@ -330,13 +335,14 @@ scatter_kernel(const float2* __restrict__ y, const TsneInstance* __restrict__ in
   const int hu = min(kScatterTile, s_box[3] - oy + TAPS);
   for (int t = threadIdx.x; t < wu * hu; t += blockDim.x) {
     const int r = t / wu, c = t - r * wu;
-    const unsigned long long* src = tile + (r * kScatterTile + c) * 3;
-    const long long a0 = (long long)src[0], a1 = (long long)src[1], a2 = (long long)src[2];
+    const int* src = tile + (r * kScatterTile + c) * 3;
+    const int a0 = src[0], a1 = src[1], a2 = src[2];
     if (a0 != 0 || a1 != 0 || a2 != 0) {
       long long* dst = charges + ((long long)(oy + r) * grid + ox + c) * kChargeStride;
-      red_add_i64(dst, a0);
-      red_add_i64(dst + 1, a1);
-      red_add_i64(dst + 2, a2);
+      const int sh = g.tile_shift;
+      red_add_i64(dst, (long long)((unsigned long long)(long long)a0 << sh));
+      red_add_i64(dst + 1, (long long)((unsigned long long)(long long)a1 << sh));
+      red_add_i64(dst + 2, (long long)((unsigned long long)(long long)a2 << sh));
     }
   }
 }
@@ -638,9 +644,9 @@ rows_inverse_kernel(const float2* __restrict__ rows, const TsneInstance* __restr
 // Rows are taken in storage (spatial) order: slot_rows[s] = (begin, end) of the CSR row of the
 // point in slot s (rebuilt at every reorder), so a row is one contiguous segment of P and
 // consecutive rows of a warp belong to neighbouring points, whose neighbour sets overlap: their
-// y gathers hit L1. Warps take chunks of kAttrChunk consecutive slots from a counter (the last
-// warp to finish resets it for the next launch), which keeps every SM busy to the end whatever
-// the row lengths of a region. A row is read with 128-bit loads: lane l takes entries
+// y gathers hit L1. Warp w first takes chunk w of kAttrChunk consecutive slots, then further
+// chunks from a counter (the last warp to finish resets it for the next launch), which keeps
+// every SM busy to the end whatever the row lengths of a region. A row is read with 128-bit loads: lane l takes entries
 // c0 + 4 l .. + 3 of each 128-entry round (c0 = the row's first entry rounded down to a multiple
 // of 4; entries outside the row are masked), kAttrRounds rounds loaded before their gathers.
 // Lane 0 keeps a bulk L2 prefetch (cp.async.bulk.prefetch) of the row kAttrAhead rows ahead.
@@ -650,7 +656,7 @@ rows_inverse_kernel(const float2* __restrict__ rows, const TsneInstance* __restr
 constexpr int kAttrThreads = 256;
 constexpr int kAttrWarps = kAttrThreads / 32;
 constexpr int kAttrAhead = 2;
-constexpr int kAttrChunk = 32;  // slots per work item
+constexpr int kAttrChunk = 16;  // slots per work item
 constexpr int kAttrRounds = 2;  // 128-entry rounds loaded together
 
 __device__ __forceinline__ void prefetch_l2_range(const void* base, long long first, long long last, int elem) {
@@ -689,18 +695,19 @@ __device__ __forceinline__ void prefetch_row(const int2* __restrict__ slot_rows,
   prefetch_l2_range(val, se.x, se.y, 4);
 }
 
-__global__ void __launch_bounds__(kAttrThreads)
+#ifndef FE_ATTR_MIN_BLOCKS
+#define FE_ATTR_MIN_BLOCKS 1
+#endif
+__global__ void __launch_bounds__(kAttrThreads, FE_ATTR_MIN_BLOCKS)
 attractive_kernel(const int2* __restrict__ slot_rows, const int* __restrict__ col, const float* __restrict__ val,
                   const float2* __restrict__ y, int n, float exag, float2* __restrict__ attr,
                   unsigned* __restrict__ ctr) {
   const int lane = threadIdx.x & 31;
   const unsigned nchunks = (unsigned)((n + kAttrChunk - 1) / kAttrChunk);
-  unsigned c = 0, next = 0;
-  if (lane == 0) {
-    c = atomicAdd(ctr, 1u);
-    next = atomicAdd(ctr, 1u);
-  }
-  c = __shfl_sync(0xffffffffu, c, 0);
+  const unsigned nwarps = gridDim.x * kAttrWarps;
+  // chunk gw first, then chunks nwarps, nwarps + 1, ... from the counter
+  unsigned c = blockIdx.x * kAttrWarps + (threadIdx.x >> 5), next = 0;
+  if (lane == 0) next = nwarps + atomicAdd(ctr, 1u);
   next = __shfl_sync(0xffffffffu, next, 0);
   // slot at position t of chunk c (positions past the chunk run into chunk `next`), or -1
   auto slot_at = [&](int t) -> int {
@@ -769,7 +776,7 @@ attractive_kernel(const int2* __restrict__ slot_rows, const int* __restrict__ co
     }
     c = next;
     if (c < nchunks) {
-      if (lane == 0) next = atomicAdd(ctr, 1u);
+      if (lane == 0) next = nwarps + atomicAdd(ctr, 1u);
       next = __shfl_sync(0xffffffffu, next, 0);
     }
   }

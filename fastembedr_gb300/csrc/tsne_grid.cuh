@@ -25,6 +25,11 @@ struct GridState {
   // associative, so the grid, and with it every later step, is the same whatever order the
   // atomics land in.
   float qscale, inv_qscale;
+  // A scatter block (at most kPointBlock points) sums its tile in 32-bit fixed point at scale
+  // tscale = qscale / 2^tile_shift (also a power of two, chosen so the block's sums fit in 31
+  // bits) and adds each tile node to the grid as (sum << tile_shift).
+  float tscale;
+  int tile_shift;
 };
 
 // Fixed-point charges of one grid node: mass, mass * dx, mass * dy and a pad slot, so a node is
