@@ -464,55 +464,95 @@ __device__ void fft_dif(float2* buf, int count, int logm, const float2* __restri
 }
 
 // Forward transforms are decimation in frequency (natural order in, bit-reversed order out) and
-// inverse transforms decimation in time (bit-reversed in, natural out): the spectra of the
-// charges and of the kernel are multiplied element by element in the same bit-reversed order,
-// so no bit-reversal permutation is ever applied.
-// Row pass. Blocks [0, nodes): charge row r -> forward FFT of the two packed planes
-// A = (x-charge) + i (y-charge), B = mass (the charge row is cleared for the next scatter).
-// Blocks [nodes, 2 nodes): kernel row dy = r - nodes -> forward FFT of (q + i q^2), all M
-// spectral positions kept.
-// blockIdx.y selects the instance members[blockIdx.y] of the grid class.
+// inverse transforms decimation in time (bit-reversed in, natural out); spectra are stored in
+// natural frequency order between the passes (written from, and loaded into, bit-reversed
+// shared-memory positions), and the column pass multiplies its spectra element by element in
+// the bit-reversed order both of its operands share.
+//
+// Real-input savings (the three charge planes and the kernel are real):
+//   * the x and y charges travel as one complex plane A = x-charge + i y-charge (all M columns);
+//   * the mass plane B is real, so its row spectra are Hermitian: B^[r][M - f] = conj(B^[r][f]),
+//     and only f = 0 .. M/2 is kept. Rows are transformed in pairs (r, r + npairs): one complex
+//     FFT of m_r + i m_r2 gives both half spectra;
+//   * the kernel rows q + i q^2 are real and even in x: their spectra Kq + i Kq2 have real parts,
+//     and K^[dy][M - f] = K^[dy][f], so f = 0 .. M/2 is kept;
+//   * the column pass takes frequency columns in conjugate pairs (c, M - c): A_c, A_(M-c), B_c and
+//     one kernel column (K_(M-c) = K_c) are transformed, B_(M-c) being conj(B_c) row by row;
+//     the Parseval sum of the pair is twice that of column c (once for c = 0 and c = M/2);
+//   * the inverse row pass rebuilds each B row's full spectrum from its half and transforms two
+//     rows in one complex FFT (real parts: row r, imaginary parts: row r2).
+// Per pair of rows and pair of columns that is 3 + 4 + 3 + 3 transforms of length M where the
+// plain complex scheme needs 4 + 6 + 4 + 4 (and the kernel rows once per row in both).
+__device__ __forceinline__ int bitrev(int f, int logm) { return (int)(__brev((unsigned)f) >> (32 - logm)); }
+__device__ __forceinline__ float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
+
+// Row pass. Blocks [0, npairs): charge rows r1 = p and r2 = p + npairs (r2 < nodes or absent):
+// forward FFTs of A_r1, A_r2 and m_r1 + i m_r2; A spectra to arow (natural order, all M),
+// separated B half spectra to brow (f = 0 .. M/2); the charge rows are cleared for the next
+// scatter. Blocks [npairs, npairs + nodes): kernel row dy -> forward FFT of (q + i q^2), f = 0 .. M/2
+// kept. blockIdx.y selects the instance members[blockIdx.y] of the grid class.
 __global__ void __launch_bounds__(kFftThreads)
 rows_forward_kernel(const TsneInstance* __restrict__ inst, const int* __restrict__ members, int grid, int nodes,
                     int logm, const float2* __restrict__ tw, const GridState* __restrict__ cur,
-                    float2* __restrict__ rows, float2* __restrict__ krows) {
+                    float2* __restrict__ arow, float2* __restrict__ brow, float2* __restrict__ krow) {
   extern __shared__ float2 sbuf[];
-  const int m = 1 << logm;
-  const int r = blockIdx.x;
+  const int m = 1 << logm, hm = m >> 1;
+  const int npairs = (nodes + 1) >> 1;
   const int b = members[blockIdx.y];
   long long* __restrict__ charges = inst[b].charges;
   cur += b;
-  rows += (long long)blockIdx.y * 2 * nodes * m;
-  krows += (long long)blockIdx.y * nodes * m;
-  if (r < nodes) {
-    longlong2* crow = reinterpret_cast<longlong2*>(charges + (long long)r * grid * kChargeStride);
+  arow += (long long)blockIdx.y * nodes * m;
+  brow += (long long)blockIdx.y * nodes * (hm + 1);
+  krow += (long long)blockIdx.y * nodes * (hm + 1);
+  if ((int)blockIdx.x < npairs) {
+    const int r1 = blockIdx.x, r2 = blockIdx.x + npairs;
+    const bool has2 = r2 < nodes;
     const float inv_q = cur->inv_qscale;
+    longlong2* c1 = reinterpret_cast<longlong2*>(charges + (long long)r1 * grid * kChargeStride);
+    longlong2* c2 = reinterpret_cast<longlong2*>(charges + (long long)(has2 ? r2 : r1) * grid * kChargeStride);
     for (int c = threadIdx.x; c < m; c += blockDim.x) {
-      float2 a = make_float2(0.0f, 0.0f), b = make_float2(0.0f, 0.0f);
+      float2 a1 = make_float2(0.0f, 0.0f), a2 = a1, mm = a1;
       if (c < nodes) {
-        const longlong2 q0 = crow[2 * c], q1 = crow[2 * c + 1];
-        crow[2 * c] = make_longlong2(0, 0);
-        crow[2 * c + 1] = make_longlong2(0, 0);
-        a = make_float2((float)q0.y * inv_q, (float)q1.x * inv_q);
-        b = make_float2((float)q0.x * inv_q, 0.0f);
+        const longlong2 p0 = c1[2 * c], p1 = c1[2 * c + 1];
+        c1[2 * c] = make_longlong2(0, 0);
+        c1[2 * c + 1] = make_longlong2(0, 0);
+        a1 = make_float2((float)p0.y * inv_q, (float)p1.x * inv_q);
+        mm.x = (float)p0.x * inv_q;
+        if (has2) {
+          const longlong2 s0 = c2[2 * c], s1 = c2[2 * c + 1];
+          c2[2 * c] = make_longlong2(0, 0);
+          c2[2 * c + 1] = make_longlong2(0, 0);
+          a2 = make_float2((float)s0.y * inv_q, (float)s1.x * inv_q);
+          mm.y = (float)s0.x * inv_q;
+        }
       }
-      sbuf[sidx(c)] = a;
-      sbuf[sidx(m + c)] = b;
+      sbuf[sidx(c)] = a1;
+      sbuf[sidx(m + c)] = a2;
+      sbuf[sidx(2 * m + c)] = mm;
     }
     __syncthreads();
-    fft_dif<3>(sbuf, 2, logm, tw, false);
-    float2* outa = rows + (long long)r * m;
-    float2* outb = rows + (long long)(nodes + r) * m;
-    for (int c = threadIdx.x; c < m; c += blockDim.x) {
-      outa[c] = sbuf[sidx(c)];
-      outb[c] = sbuf[sidx(m + c)];
+    fft_dif<3>(sbuf, 3, logm, tw, false);
+    float2* o1 = arow + (long long)r1 * m;
+    float2* o2 = arow + (long long)r2 * m;
+    for (int f = threadIdx.x; f < m; f += blockDim.x) {
+      const int p = bitrev(f, logm);
+      o1[f] = sbuf[sidx(p)];
+      if (has2) o2[f] = sbuf[sidx(m + p)];
+    }
+    float2* b1 = brow + (long long)r1 * (hm + 1);
+    float2* b2 = brow + (long long)r2 * (hm + 1);
+    for (int f = threadIdx.x; f <= hm; f += blockDim.x) {
+      const float2 z = sbuf[sidx(2 * m + bitrev(f, logm))];
+      const float2 zc = conjf2(sbuf[sidx(2 * m + bitrev((m - f) & (m - 1), logm))]);
+      b1[f] = make_float2(0.5f * (z.x + zc.x), 0.5f * (z.y + zc.y));
+      if (has2) b2[f] = make_float2(0.5f * (z.y - zc.y), -0.5f * (z.x - zc.x));
     }
   } else {
-    const int kr = r - nodes;
+    const int kr = blockIdx.x - npairs;
     const float h = cur->h;
     const float yo = (float)kr * h;
     for (int c = threadIdx.x; c < m; c += blockDim.x) {
-      const int dx = c < (m >> 1) ? c : c - m;
+      const int dx = c < hm ? c : c - m;
       float2 v = make_float2(0.0f, 0.0f);
       if (dx <= nodes - 1 && dx >= -(nodes - 1)) {
         const float xo = (float)dx * h;
@@ -524,61 +564,63 @@ rows_forward_kernel(const TsneInstance* __restrict__ inst, const int* __restrict
     }
     __syncthreads();
     fft_dif<3>(sbuf, 1, logm, tw, false);
-    float2* out = krows + (long long)kr * m;
-    for (int c = threadIdx.x; c < m; c += blockDim.x) out[c] = sbuf[sidx(c)];
+    float2* out = krow + (long long)kr * (hm + 1);
+    for (int f = threadIdx.x; f <= hm; f += blockDim.x) out[f] = sbuf[sidx(bitrev(f, logm))];
   }
 }
 
-// Column pass for `cc` adjacent columns: transform the kernel column (giving the real
-// spectra Kq + i Kq2) and the two charge planes, accumulate sum |F_mass|^2 Kq (Parseval form
-// of sum_nodes mass * (mass conv q), i.e. Z + n up to the 1/M^2 scale), multiply the charge
-// spectra by Kq2 and transform back. Only rows < nodes of the result are written.
+// Column pass for the conjugate pair (c, c') = (j, M - j), j = 0 .. M/2 (c' = c for j = 0 and
+// M/2): column FFTs of A_c, A_c', B_c and the kernel column K_c (giving the real spectra
+// Kq + i Kq2), the Parseval sum of |B^|^2 Kq over both columns of the pair (Z + n up to the
+// 1 / M^2 scale), the products with Kq2 and their inverse column FFTs; rows < nodes of the
+// results go back to arow / brow.
 __global__ void __launch_bounds__(kColThreads)
-columns_convolve_kernel(float2* __restrict__ rows, const float2* __restrict__ krows, int nodes, int logm, int cc,
-                        const float2* __restrict__ tw, double* __restrict__ zpart) {
-  extern __shared__ float2 sbuf[];  // [2 cc charge sequences][cc kernel sequences]
+columns_convolve_kernel(float2* __restrict__ arow, float2* __restrict__ brow, const float2* __restrict__ krow,
+                        int nodes, int logm, const float2* __restrict__ tw, double* __restrict__ zpart) {
+  extern __shared__ float2 sbuf[];  // [A_c][A_c'][B_c][K_c]
   __shared__ double s_z[kColThreads / 32];
-  const int m = 1 << logm;
-  const int half = m >> 1;
-  rows += (long long)blockIdx.y * 2 * nodes * m;
-  krows += (long long)blockIdx.y * nodes * m;
+  const int m = 1 << logm, hm = m >> 1;
+  const int j = blockIdx.x;
+  const int c = j, c2 = (m - j) & (m - 1);
+  arow += (long long)blockIdx.y * nodes * m;
+  brow += (long long)blockIdx.y * nodes * (hm + 1);
+  krow += (long long)blockIdx.y * nodes * (hm + 1);
   zpart += (long long)blockIdx.y * gridDim.x;
-  const int c0 = blockIdx.x * cc;
-  const int kbase = 2 * cc << logm;  // kernel sequences follow the 2 cc charge sequences
-  for (int t = threadIdx.x; t < cc * m; t += blockDim.x) {
-    const int j = t % cc, r = t / cc;
-    const int c = c0 + j;
-    float2 a = make_float2(0.0f, 0.0f), b = make_float2(0.0f, 0.0f);
+  for (int r = threadIdx.x; r < m; r += blockDim.x) {
+    float2 a = make_float2(0.0f, 0.0f), a2 = a, bb = a;
     if (r < nodes) {
-      a = rows[(long long)r * m + c];
-      b = rows[(long long)(nodes + r) * m + c];
+      a = arow[(long long)r * m + c];
+      a2 = arow[(long long)r * m + c2];
+      bb = brow[(long long)r * (hm + 1) + c];
     }
-    sbuf[sidx(((2 * j) << logm) + r)] = a;
-    sbuf[sidx(((2 * j + 1) << logm) + r)] = b;
-    const int dy = r < half ? r : m - r;
-    sbuf[sidx(kbase + (j << logm) + r)] = dy <= nodes - 1 ? krows[(long long)dy * m + c] : make_float2(0.0f, 0.0f);
+    sbuf[sidx(r)] = a;
+    sbuf[sidx(m + r)] = a2;
+    sbuf[sidx(2 * m + r)] = bb;
+    const int dy = r < hm ? r : m - r;
+    sbuf[sidx(3 * m + r)] = dy <= nodes - 1 ? krow[(long long)dy * (hm + 1) + c] : make_float2(0.0f, 0.0f);
   }
   __syncthreads();
-  fft_dif(sbuf, 3 * cc, logm, tw, false);
+  fft_dif(sbuf, 4, logm, tw, false);
   double zl = 0.0;
-  for (int t = threadIdx.x; t < cc * m; t += blockDim.x) {
-    const int j = t / m, kr = t % m;
-    const float2 kk = sbuf[sidx(kbase + (j << logm) + kr)];
-    float2& a = sbuf[sidx(((2 * j) << logm) + kr)];
-    float2& b = sbuf[sidx(((2 * j + 1) << logm) + kr)];
-    zl += ((double)b.x * b.x + (double)b.y * b.y) * (double)kk.x;
+  for (int k = threadIdx.x; k < m; k += blockDim.x) {
+    const float2 kk = sbuf[sidx(3 * m + k)];
+    float2& a = sbuf[sidx(k)];
+    float2& a2 = sbuf[sidx(m + k)];
+    float2& bb = sbuf[sidx(2 * m + k)];
+    zl += ((double)bb.x * bb.x + (double)bb.y * bb.y) * (double)kk.x;
     a.x *= kk.y;
     a.y *= kk.y;
-    b.x *= kk.y;
-    b.y *= kk.y;
+    a2.x *= kk.y;
+    a2.y *= kk.y;
+    bb.x *= kk.y;
+    bb.y *= kk.y;
   }
   __syncthreads();
-  fft_dit(sbuf, 2 * cc, logm, tw, true);
-  for (int t = threadIdx.x; t < cc * nodes; t += blockDim.x) {
-    const int j = t % cc, r = t / cc;
-    const int c = c0 + j;
-    rows[(long long)r * m + c] = sbuf[sidx(((2 * j) << logm) + r)];
-    rows[(long long)(nodes + r) * m + c] = sbuf[sidx(((2 * j + 1) << logm) + r)];
+  fft_dit(sbuf, 3, logm, tw, true);
+  for (int r = threadIdx.x; r < nodes; r += blockDim.x) {
+    arow[(long long)r * m + c] = sbuf[sidx(r)];
+    if (c2 != c) arow[(long long)r * m + c2] = sbuf[sidx(m + r)];
+    brow[(long long)r * (hm + 1) + c] = sbuf[sidx(2 * m + r)];
   }
   zl = warp_sum(zl);
   if ((threadIdx.x & 31) == 0) s_z[threadIdx.x >> 5] = zl;
@@ -586,44 +628,60 @@ columns_convolve_kernel(float2* __restrict__ rows, const float2* __restrict__ kr
   if (threadIdx.x == 0) {
     double z = 0.0;
     for (int w = 0; w < (int)(blockDim.x / 32); ++w) z += s_z[w];
-    zpart[blockIdx.x] = z;
+    zpart[blockIdx.x] = c2 != c ? 2.0 * z : z;
   }
 }
 
-// Inverse row pass -> potentials (phi_q2, phi_x, phi_y) per node; block 0 also finalises
-// Z = sum_k |F_mass|^2 Kq / M^2 - n (the reference's sum_i q_grid(y_i) - n).
+// Inverse row pass for the row pair (r1, r2) -> potentials (phi_q2, phi_x, phi_y) per node; block
+// 0 also finalises Z = sum_k |F_mass|^2 Kq / M^2 - n (the reference's sum_i q_grid(y_i) - n).
 __global__ void __launch_bounds__(kFftThreads, 4)
-rows_inverse_kernel(const float2* __restrict__ rows, const TsneInstance* __restrict__ inst,
-                    const int* __restrict__ members, int grid, int nodes, int logm, const float2* __restrict__ tw,
-                    const double* __restrict__ zpart, int zblocks, GridState* __restrict__ cur) {
+rows_inverse_kernel(const float2* __restrict__ arow, const float2* __restrict__ brow,
+                    const TsneInstance* __restrict__ inst, const int* __restrict__ members, int grid, int nodes,
+                    int logm, const float2* __restrict__ tw, const double* __restrict__ zpart, int zblocks,
+                    GridState* __restrict__ cur) {
   extern __shared__ float2 sbuf[];
-  const int m = 1 << logm;
-  const int r = blockIdx.x;
+  const int m = 1 << logm, hm = m >> 1;
+  const int npairs = (nodes + 1) >> 1;
+  const int r1 = blockIdx.x, r2 = blockIdx.x + npairs;
+  const bool has2 = r2 < nodes;
   const int b = members[blockIdx.y];
   const TsneInstance& I = inst[b];
   float4* __restrict__ potential = I.potential;
   const int n = I.n;
   cur += b;
-  rows += (long long)blockIdx.y * 2 * nodes * m;
+  arow += (long long)blockIdx.y * nodes * m;
+  brow += (long long)blockIdx.y * nodes * (hm + 1);
   zpart += (long long)blockIdx.y * zblocks;
-  const float2* ina = rows + (long long)r * m;
-  const float2* inb = rows + (long long)(nodes + r) * m;
-  for (int c = threadIdx.x; c < m; c += blockDim.x) {
-    sbuf[sidx(c)] = ina[c];
-    sbuf[sidx(m + c)] = inb[c];
+  const float2* a1 = arow + (long long)r1 * m;
+  const float2* a2 = arow + (long long)r2 * m;
+  const float2* b1 = brow + (long long)r1 * (hm + 1);
+  const float2* b2 = brow + (long long)r2 * (hm + 1);
+  for (int f = threadIdx.x; f < m; f += blockDim.x) {
+    const int p = bitrev(f, logm);
+    sbuf[sidx(p)] = a1[f];
+    sbuf[sidx(m + p)] = has2 ? a2[f] : make_float2(0.0f, 0.0f);
+    // full spectra of the two real B rows from their halves, packed as X1 + i X2
+    const float2 x1 = f <= hm ? b1[f] : conjf2(b1[m - f]);
+    const float2 x2 = has2 ? (f <= hm ? b2[f] : conjf2(b2[m - f])) : make_float2(0.0f, 0.0f);
+    sbuf[sidx(2 * m + p)] = make_float2(x1.x - x2.y, x1.y + x2.x);
   }
   __syncthreads();
-  fft_dit(sbuf, 2, logm, tw, true);
+  fft_dit(sbuf, 3, logm, tw, true);
   const float scale = 1.0f / ((float)m * (float)m);
-  float4* out = potential + (long long)r * grid;
+  float4* o1 = potential + (long long)r1 * grid;
+  float4* o2 = potential + (long long)r2 * grid;
   for (int c = threadIdx.x; c < nodes; c += blockDim.x) {
-    const float2 a = sbuf[sidx(c)], b = sbuf[sidx(m + c)];
-    out[c] = make_float4(b.x * scale, a.x * scale, a.y * scale, 0.0f);
+    const float2 q1 = sbuf[sidx(c)], pb = sbuf[sidx(2 * m + c)];
+    o1[c] = make_float4(pb.x * scale, q1.x * scale, q1.y * scale, 0.0f);
+    if (has2) {
+      const float2 q2 = sbuf[sidx(m + c)];
+      o2[c] = make_float4(pb.y * scale, q2.x * scale, q2.y * scale, 0.0f);
+    }
   }
-  if (r == 0) {
+  if (r1 == 0) {
     __shared__ double s_z[kFftThreads];
     double z = 0.0;
-    for (int b = threadIdx.x; b < zblocks; b += blockDim.x) z += zpart[b];
+    for (int t = threadIdx.x; t < zblocks; t += blockDim.x) z += zpart[t];
     s_z[threadIdx.x] = z;
     __syncthreads();
     for (int w = blockDim.x / 2; w > 0; w >>= 1) {
@@ -1037,13 +1095,13 @@ void build_grid_classes(TsneDevice& d, const std::vector<int>& grids) {
     k.fft = 2 * k.grid;
     k.log_fft = log2_ceil(k.fft);
     k.count = (int)members[c].size();
-    k.cols_per_block = k.fft >= 512 ? 2 : 1;
-    k.col_blocks = k.fft / k.cols_per_block;
+    k.col_blocks = k.fft / 2 + 1;
     const std::size_t m = k.fft;
     d.grid_arena.reserve(&k.charges, (std::size_t)k.count * k.grid * k.grid * kChargeStride);
     d.grid_arena.reserve(&k.potential, (std::size_t)k.count * k.grid * k.grid);
-    d.grid_arena.reserve(&k.rows, (std::size_t)k.count * 2 * k.nodes * m);
-    d.grid_arena.reserve(&k.krows, (std::size_t)k.count * k.nodes * m);
+    d.grid_arena.reserve(&k.arow, (std::size_t)k.count * k.nodes * m);
+    d.grid_arena.reserve(&k.brow, (std::size_t)k.count * k.nodes * (m / 2 + 1));
+    d.grid_arena.reserve(&k.krow, (std::size_t)k.count * k.nodes * (m / 2 + 1));
     d.grid_arena.reserve(&k.twiddle, m / 2);
     d.grid_arena.reserve(&k.zpart, (std::size_t)k.count * k.col_blocks);
   }
@@ -1080,9 +1138,9 @@ void build_grid_classes(TsneDevice& d, const std::vector<int>& grids) {
   d.key_bits = 2 * log2_ceil(max_grid);
   d.sort_bits = d.key_bits + log2_ceil(ninst);
   if (d.sort_bits > 32) throw Error("t-SNE batch: too many instances for the spatial sort key");
-  const int big = padded(3 * (max_m >= 512 ? 2 : 1) * max_m) * (int)sizeof(float2);
+  const int big = padded(4 * max_m) * (int)sizeof(float2);
   FE_CUDA(cudaFuncSetAttribute(columns_convolve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  const int rowb = padded(2 * max_m) * (int)sizeof(float2);
+  const int rowb = padded(3 * max_m) * (int)sizeof(float2);
   FE_CUDA(cudaFuncSetAttribute(rows_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, rowb));
   FE_CUDA(cudaFuncSetAttribute(rows_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, rowb));
 }
@@ -1199,14 +1257,15 @@ void tsne_grid_stage(TsneDevice& d, cudaStream_t s) {
   FE_LAUNCH("scatter_kernel");
   for (const GridClass& c : d.classes) {
     const int m = c.fft;
-    rows_forward_kernel<<<dim3(2 * c.nodes, c.count), kFftThreads, padded(2 * m) * sizeof(float2), s>>>(
-        d.d_inst, c.members, c.grid, c.nodes, c.log_fft, c.twiddle, d.cur, c.rows, c.krows);
+    const int npairs = (c.nodes + 1) / 2;
+    rows_forward_kernel<<<dim3(npairs + c.nodes, c.count), kFftThreads, padded(3 * m) * sizeof(float2), s>>>(
+        d.d_inst, c.members, c.grid, c.nodes, c.log_fft, c.twiddle, d.cur, c.arow, c.brow, c.krow);
     FE_LAUNCH("rows_forward_kernel");
-    columns_convolve_kernel<<<dim3(c.col_blocks, c.count), m >= 2048 ? kColThreads : kFftThreads,
-                              padded(3 * c.cols_per_block * m) * sizeof(float2), s>>>(c.rows, c.krows, c.nodes, c.log_fft, c.cols_per_block, c.twiddle, c.zpart);
+    columns_convolve_kernel<<<dim3(c.col_blocks, c.count), kColThreads, padded(4 * m) * sizeof(float2), s>>>(
+        c.arow, c.brow, c.krow, c.nodes, c.log_fft, c.twiddle, c.zpart);
     FE_LAUNCH("columns_convolve_kernel");
-    rows_inverse_kernel<<<dim3(c.nodes, c.count), kFftThreads, padded(2 * m) * sizeof(float2), s>>>(
-        c.rows, d.d_inst, c.members, c.grid, c.nodes, c.log_fft, c.twiddle, c.zpart, c.col_blocks, d.cur);
+    rows_inverse_kernel<<<dim3(npairs, c.count), kFftThreads, padded(3 * m) * sizeof(float2), s>>>(
+        c.arow, c.brow, d.d_inst, c.members, c.grid, c.nodes, c.log_fft, c.twiddle, c.zpart, c.col_blocks, d.cur);
     FE_LAUNCH("rows_inverse_kernel");
   }
 }

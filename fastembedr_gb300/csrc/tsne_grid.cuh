@@ -57,10 +57,11 @@ struct GridClass {
   int grid = 0, nodes = 0, fft = 0, log_fft = 0;
   int count = 0;
   int* members = nullptr;     // device: the class's instance indices
-  int cols_per_block = 1, col_blocks = 0;
-  float2* rows = nullptr;     // count x (2 planes x nodes x M): row-transformed charges
-  float2* krows = nullptr;    // count x (nodes x (M/2 + 1)): row-transformed kernel (q, q^2)
-  double* zpart = nullptr;    // count x col_blocks
+  int col_blocks = 0;          // M / 2 + 1 conjugate column pairs
+  float2* arow = nullptr;      // count x (nodes x M): row spectra of A = x-charge + i y-charge
+  float2* brow = nullptr;      // count x (nodes x (M/2 + 1)): half row spectra of the mass plane
+  float2* krow = nullptr;      // count x (nodes x (M/2 + 1)): row spectra of the kernel (q + i q^2)
+  double* zpart = nullptr;     // count x col_blocks
   float2* twiddle = nullptr;  // M / 2 forward twiddles
   long long* charges = nullptr;  // count x G x G x kChargeStride
   float4* potential = nullptr;
