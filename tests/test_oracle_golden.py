@@ -105,3 +105,24 @@ def test_fp64_probability_oracle_tracks_fp32_reference(golden):
     _, _, v32, _ = O.csr_from_p(g["idx"], p32)
     _, _, v64, _ = O.csr_from_p(g["idx"], p64.astype(np.float32))
     assert np.abs(v32.astype(np.float64) - v64).sum() / np.abs(v64).sum() < 2e-6
+
+
+def test_knn_preservation_known_answers():
+    """15-NN preservation as knn_structure_score_cpp defines it (src/embedding_utils.cpp:1386-1579:
+    the preserve_k nearest layout points by (squared distance, index), counted against the first
+    preserve_k high-dimensional neighbours). Known answers: an unchanged embedding scores exactly 1
+    (the reference's tests/testthat/test-evaluation-core.R:1-13 and test-cuda-stages.R:101-115
+    set-up: a 30 x 2 layout scored against its own exact KNN, preserve_k = 6), and a five-point
+    case worked by hand scores 0.6."""
+    from fastembedr_gb300 import synthetic
+
+    layout = np.random.default_rng(13).standard_normal((30, 2)).astype(np.float32)
+    idx, _ = synthetic.exact_knn_numpy(layout, 7)
+    assert O.knn_preservation(layout, idx, preserve_k=6) == 1.0
+    # points on a line at x = 0, 1, 3, 6, 10; layout 2-NN: {1, 2}, {0, 2}, {1, 0}, {2, 4}, {3, 2}
+    line = np.array([[0, 0], [1, 0], [3, 0], [6, 0], [10, 0]], np.float32)
+    hi = np.array([[1, 3, 2], [2, 0, 3], [4, 3, 0], [2, 4, 1], [3, 0, 1]], np.int32)
+    # shared among the first two: 1 of {1, 3}; 2 of {2, 0}; 0 of {4, 3}; 2 of {2, 4}; 1 of {3, 0}
+    assert O.knn_preservation(line, hi, preserve_k=2) == pytest.approx((0.5 + 1.0 + 0.0 + 1.0 + 0.5) / 5, abs=1e-15)
+    # 1-based labels give the same score
+    assert O.knn_preservation(line, hi + 1, preserve_k=2, offset=1) == pytest.approx(0.6, abs=1e-15)

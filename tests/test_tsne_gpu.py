@@ -288,3 +288,35 @@ def test_plan_gradient_check_matches_diagnostic_and_oracle(c1):
     assert abs(chk["z_rel_err"]) < 1e-2
     assert chk["repulsion_rel_l2"] < 0.05, chk["repulsion_rel_l2"]
     assert chk["gradient_rel_l2"] < 0.25, chk["gradient_rel_l2"]
+
+
+def test_device_knn_entry_matches_reference_cpu(c1, monkeypatch):
+    """GPU-resident KNN ingestion: the device-pointer entry point on a column-major, 1-based
+    device KNN (the layout of the package's GPU KNN object) runs the full 250 + 750 schedule at the
+    reference CPU's grid and matches the reference CPU run (oracle): KL within 1 %, 15-NN
+    preservation within 0.01. It is also the host entry point's result bit for bit."""
+    import torch
+
+    idx, dist, _ = c1
+    n, k = idx.shape
+    init = synthetic.tsne_init(n, 7)
+    monkeypatch.setenv("FASTEMBEDR_TSNE_FFT_GRID", "128")
+    lib = _lib.require_gpu()
+    d_idx = torch.as_tensor(np.ascontiguousarray((idx + 1).T.astype(np.int32)), device="cuda")
+    d_dist = torch.as_tensor(np.ascontiguousarray(dist.T.astype(np.float32)), device="cuda")
+    torch.cuda.synchronize()
+    out = np.zeros((n, 2), np.float32)
+    st = lib.fastembedr_cuda_opentsne_fft_from_device_knn_float(
+        d_idx.data_ptr(), d_dist.data_ptr(), init.ctypes.data, 1, n, k, 2, 30.0, 250, 750, 12.0, 1.0, n / 12.0, 0,
+        0.8, 0.8, 0.01, 5.0, 4, 1, out.ctypes.data)
+    _lib.check(st, "t-SNE from device KNN")
+    host = api.tsne_knn(idx, dist, perplexity=30, Y_init=init, early_exaggeration_iter=250, n_iter=750)
+    assert np.array_equal(out, host.layout)
+    cpu = O.tsne_run(idx, dist, init, perplexity=30, early_iter=250, n_iter=750, learning_rate=n / 12.0)
+    rp, col, val, _ = O.tsne_csr(idx, dist, 30.0)
+    keep = np.arange(0, n, 5, dtype=np.int32)
+    kl_cpu, kl_gpu = O.kl(rp, col, val, cpu), O.kl(rp, col, val, out)
+    assert abs(kl_gpu - kl_cpu) / kl_cpu < 0.01, (kl_gpu, kl_cpu)
+    pc = O.knn_preservation(cpu, idx, keep=keep, preserve_k=15)
+    pg = O.knn_preservation(out, idx, keep=keep, preserve_k=15)
+    assert abs(pg - pc) < 0.01, (pg, pc)

@@ -261,3 +261,41 @@ def test_umap_knn_with_gpu_spectral_start_matches_reference_cpu():
     assert np.all(np.isfinite(fit.layout)) and np.abs(fit.layout).max() <= 16.0
     assert abs(pg - pc) < 0.01, (pg, pc)
     assert pg > p0 + 0.02, (pg, p0)
+
+
+def test_sgd_preservation_matches_reference_cpu_at_100k_500_epochs():
+    """The plain umap_knn workload at full size (100,000 x 50 mixture of 20 log-normal clusters,
+    exact k = 15 KNN, 500 epochs, the package's spectral start): 15-NN preservation of the GPU
+    layout within 0.01 of the reference CPU SGD on the same graph and start. At this size the
+    package runs the reference's multi-threaded SGD branch (min(4, cores) workers), restated in
+    the oracle."""
+    import os
+
+    import torch
+
+    x, _ = synthetic.plain_umap_100k()
+    i_t, d_t = synthetic.exact_knn_torch(x, 15, device="cuda")
+    idx = np.asfortranarray(i_t.cpu().numpy())
+    dist = np.asfortranarray(d_t.cpu().numpy())
+    del i_t, d_t
+    torch.cuda.empty_cache()
+    n = idx.shape[0]
+    rounds = api.umap_spectral_n_iter(n, 15)
+    init = np.ascontiguousarray(api.umap_spectral_start(idx, dist, rounds, 42).astype(np.float32))
+    fit = api.umap_knn(idx, dist, init, n_epochs=500)
+    off, nb, w, e, mw = O.umap_graph(np.ascontiguousarray(idx), np.ascontiguousarray(dist))
+    a, b = O.umap_ab(0.01)
+    emb = np.ascontiguousarray(init.T.astype(np.float64)).ravel().copy()
+    workers = max(1, min(4, os.cpu_count() or 1))
+    if workers > 1:
+        O.orc().orc_umap_sgd_threaded(n, off, nb, w, emb, 500, a, b, 5, 1.0, 1.0, 42, workers)
+    else:
+        O.orc().orc_umap_sgd_serial(n, off, nb, w, emb, 500, a, b, 5, 1.0, 1.0, 42)
+    cpu = emb.reshape(2, n).T.astype(np.float32)
+    keep = np.arange(0, n, 10, dtype=np.int32)
+    pc = O.knn_preservation(cpu, np.ascontiguousarray(idx), keep=keep, preserve_k=15)
+    pg = O.knn_preservation(fit.layout, np.ascontiguousarray(idx), keep=keep, preserve_k=15)
+    p0 = O.knn_preservation(init, np.ascontiguousarray(idx), keep=keep, preserve_k=15)
+    assert np.all(np.isfinite(fit.layout)) and np.abs(fit.layout).max() <= 16.0
+    assert abs(pg - pc) < 0.01, (pg, pc)
+    assert pg > p0 + 0.02, (pg, p0)
