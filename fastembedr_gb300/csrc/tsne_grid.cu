@@ -77,14 +77,17 @@ __device__ void finish_layout_stats(const StepPartial* __restrict__ part, int nb
   __shared__ double s_sx[kStepThreads], s_sy[kStepThreads];
   float mnx = FLT_MAX, mxx = -FLT_MAX, mny = FLT_MAX, mxy = -FLT_MAX;
   double sx = 0.0, sy = 0.0;
+  // partials written by the other blocks of this launch: read through L2, eight loads in flight
+#pragma unroll 8
   for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
-    const StepPartial p = part[b];
-    mnx = fminf(mnx, p.min_x);
-    mxx = fmaxf(mxx, p.max_x);
-    mny = fminf(mny, p.min_y);
-    mxy = fmaxf(mxy, p.max_y);
-    sx += p.sum_x;
-    sy += p.sum_y;
+    const float4 mm = __ldcg(reinterpret_cast<const float4*>(part + b));
+    const double2 ss = __ldcg(reinterpret_cast<const double2*>(part + b) + 1);
+    mnx = fminf(mnx, mm.x);
+    mxx = fmaxf(mxx, mm.y);
+    mny = fminf(mny, mm.z);
+    mxy = fmaxf(mxy, mm.w);
+    sx += ss.x;
+    sy += ss.y;
   }
   s_min_x[threadIdx.x] = mnx;
   s_max_x[threadIdx.x] = mxx;
@@ -489,8 +492,9 @@ __device__ __forceinline__ float2 conjf2(float2 a) { return make_float2(a.x, -a.
 // Row pass. Blocks [0, npairs): charge rows r1 = p and r2 = p + npairs (r2 < nodes or absent):
 // forward FFTs of A_r1, A_r2 and m_r1 + i m_r2; A spectra to arow (natural order, all M),
 // separated B half spectra to brow (f = 0 .. M/2); the charge rows are cleared for the next
-// scatter. Blocks [npairs, npairs + nodes): kernel row dy -> forward FFT of (q + i q^2), f = 0 .. M/2
-// kept. blockIdx.y selects the instance members[blockIdx.y] of the grid class.
+// scatter. Blocks [npairs, 2 npairs): kernel rows dy1 = p and dy2 = p + npairs -> forward FFTs of
+// (q + i q^2), f = 0 .. M/2 kept. blockIdx.y selects the instance members[blockIdx.y] of the grid
+// class.
 __global__ void __launch_bounds__(kFftThreads)
 rows_forward_kernel(const TsneInstance* __restrict__ inst, const int* __restrict__ members, int grid, int nodes,
                     int logm, const float2* __restrict__ tw, const GridState* __restrict__ cur,
@@ -548,24 +552,32 @@ rows_forward_kernel(const TsneInstance* __restrict__ inst, const int* __restrict
       if (has2) b2[f] = make_float2(0.5f * (z.y - zc.y), -0.5f * (z.x - zc.x));
     }
   } else {
-    const int kr = blockIdx.x - npairs;
+    const int k1 = blockIdx.x - npairs, k2 = k1 + npairs;
+    const bool has2 = k2 < nodes;
     const float h = cur->h;
-    const float yo = (float)kr * h;
+    const float yo1 = (float)k1 * h, yo2 = (float)k2 * h;
     for (int c = threadIdx.x; c < m; c += blockDim.x) {
       const int dx = c < hm ? c : c - m;
-      float2 v = make_float2(0.0f, 0.0f);
+      float2 v1 = make_float2(0.0f, 0.0f), v2 = v1;
       if (dx <= nodes - 1 && dx >= -(nodes - 1)) {
         const float xo = (float)dx * h;
-        const float d2 = xo * xo + yo * yo;
-        const float q = 1.0f / (1.0f + d2);
-        v = make_float2(q, q * q);
+        const float q1 = 1.0f / (1.0f + (xo * xo + yo1 * yo1));
+        const float q2 = 1.0f / (1.0f + (xo * xo + yo2 * yo2));
+        v1 = make_float2(q1, q1 * q1);
+        v2 = make_float2(q2, q2 * q2);
       }
-      sbuf[sidx(c)] = v;
+      sbuf[sidx(c)] = v1;
+      sbuf[sidx(m + c)] = v2;
     }
     __syncthreads();
-    fft_dif<3>(sbuf, 1, logm, tw, false);
-    float2* out = krow + (long long)kr * (hm + 1);
-    for (int f = threadIdx.x; f <= hm; f += blockDim.x) out[f] = sbuf[sidx(bitrev(f, logm))];
+    fft_dif<3>(sbuf, 2, logm, tw, false);
+    float2* o1 = krow + (long long)k1 * (hm + 1);
+    float2* o2 = krow + (long long)k2 * (hm + 1);
+    for (int f = threadIdx.x; f <= hm; f += blockDim.x) {
+      const int p = bitrev(f, logm);
+      o1[f] = sbuf[sidx(p)];
+      if (has2) o2[f] = sbuf[sidx(m + p)];
+    }
   }
 }
 
@@ -1258,7 +1270,7 @@ void tsne_grid_stage(TsneDevice& d, cudaStream_t s) {
   for (const GridClass& c : d.classes) {
     const int m = c.fft;
     const int npairs = (c.nodes + 1) / 2;
-    rows_forward_kernel<<<dim3(npairs + c.nodes, c.count), kFftThreads, padded(3 * m) * sizeof(float2), s>>>(
+    rows_forward_kernel<<<dim3(2 * npairs, c.count), kFftThreads, padded(3 * m) * sizeof(float2), s>>>(
         d.d_inst, c.members, c.grid, c.nodes, c.log_fft, c.twiddle, d.cur, c.arow, c.brow, c.krow);
     FE_LAUNCH("rows_forward_kernel");
     columns_convolve_kernel<<<dim3(c.col_blocks, c.count), kColThreads, padded(4 * m) * sizeof(float2), s>>>(
