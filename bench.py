@@ -333,6 +333,7 @@ def run_gpu(args):
     kl = plan.kl() if not args.no_kl else None
     gcheck = gradient_summary(plan, args) if not args.no_kl else None
     normal_layout = plan.layout()  # start of the CPU baseline's normal-phase iterations
+    tuning = plan.tuning()
     ms = replica_time_ms(ms, world, device)
     plan.close()
     value = aggregate_rate(args.steps, ms, world)
@@ -424,6 +425,7 @@ def run_gpu(args):
                    "parallelism": f"replicas x{world}"},
         "clocks": clk, "e2e": e2e, "roofline": roofline, "gpu_launches": launches,
         "stage_ms_per_step": {k_: v / args.steps for k_, v in prof.items()},
+        "attractive_launch_tuning": tuning,
         "setup": {"affinities_and_state_s": setup_s, "early_phase_ms_per_iter": early_s * 1e3 / 250,
                   "note": "device KNN -> P and optimizer state; 250 early-exaggeration iterations incl. graph capture"},
     }

@@ -59,6 +59,7 @@ SIGNATURES = {
     "fastembedr_tsne_plan_stream": (vp, [vp]),
     "fastembedr_tsne_plan_layout": (I, [vp, vp]),
     "fastembedr_tsne_plan_info": (I, [vp, C.POINTER(L), C.POINTER(I), C.POINTER(I), C.POINTER(I), C.POINTER(I)]),
+    "fastembedr_tsne_plan_tuning": (I, [vp, C.POINTER(I), C.POINTER(I), I, C.POINTER(I), vp, vp, vp]),
     "fastembedr_tsne_plan_kl": (I, [vp, C.POINTER(D)]),
     "fastembedr_cuda_umap_spectral_init_from_knn": (I, [vp, vp, I, I, I, I, D, I, vp]),
     "fastembedr_cuda_umap_spectral_init_csr": (I, [vp, vp, vp, I, I, D, I, vp]),

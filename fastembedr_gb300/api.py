@@ -245,6 +245,18 @@ class TsnePlan:
         return dict(nnz=nnz.value, grid_size=g.value, interpolation=it.value, launches_per_iteration=la.value,
                     launches_per_reorder=lr.value)
 
+    def tuning(self):
+        """The attractive pass's run-time launch choice and the candidates it timed."""
+        ch, bl, cnt = C.c_int(), C.c_int(), C.c_int()
+        cap = 16
+        cc, cb, cm = np.zeros(cap, np.int32), np.zeros(cap, np.int32), np.zeros(cap, np.float32)
+        _lib.check(self.lib.fastembedr_tsne_plan_tuning(self.h, C.byref(ch), C.byref(bl), cap, C.byref(cnt),
+                                                        cc.ctypes.data, cb.ctypes.data, cm.ctypes.data),
+                   "t-SNE plan tuning")
+        m = min(cnt.value, cap)
+        return dict(chunk=ch.value, blocks=bl.value,
+                    candidates=[dict(chunk=int(cc[i]), blocks=int(cb[i]), ms=float(cm[i])) for i in range(m)])
+
     def kl(self):
         v = C.c_double()
         _lib.check(self.lib.fastembedr_tsne_plan_kl(self.h, C.byref(v)), "t-SNE plan KL")

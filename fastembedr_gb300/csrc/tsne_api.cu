@@ -43,6 +43,11 @@ bool reorder_enabled() {
   return !(env && env[0] == '0');
 }
 
+bool autotune_enabled() {
+  const char* env = std::getenv("FASTEMBEDR_TSNE_AUTOTUNE");
+  return !(env && env[0] == '0');
+}
+
 bool graph_capture_enabled() {
   const char* env = std::getenv("FASTEMBEDR_CUDA_GRAPH_CAPTURE");
   if (!env || !env[0]) return true;
@@ -312,6 +317,11 @@ struct TsneJob {
     if (iters <= 0) return;
     constexpr int kChunk = 25;
     const bool graph = use_graph && graph_capture_enabled();
+    // the attractive pass's launch is tuned once, on the first normal-phase run (the compact
+    // early-exaggeration layout would time differently)
+    if (!D.tuned && exag <= 1.0f && iters >= 25 && autotune_enabled()) {
+      if (tsne_tune_attractive(D, P, exag, s)) clear_graphs();
+    }
     int left = iters;
     while (left > 0) {
       const int c = std::min(kChunk, left);
@@ -719,6 +729,22 @@ int fastembedr_tsne_plan_profile(fastembedr_tsne_plan* plan, int iters, float ex
     if (ms_total) *ms_total = tot;
     if (ms_step_kernel) *ms_step_kernel = stp;
     if (ms_grid_stage) *ms_grid_stage = grd;
+  });
+}
+
+int fastembedr_tsne_plan_tuning(fastembedr_tsne_plan* plan, int* chunk, int* blocks, int capacity, int* count,
+                                int* cand_chunk, int* cand_blocks, float* cand_ms) {
+  return fe::guarded([&] {
+    if (!plan) throw fe::Error("null CUDA t-SNE plan");
+    const fe::TsneDevice& D = plan->job.D;
+    if (chunk) *chunk = D.attr_chunk;
+    if (blocks) *blocks = D.attr_blocks;
+    if (count) *count = (int)D.tuning.size();
+    for (int t = 0; t < (int)D.tuning.size() && t < capacity; ++t) {
+      if (cand_chunk) cand_chunk[t] = D.tuning[t].chunk;
+      if (cand_blocks) cand_blocks[t] = D.tuning[t].blocks;
+      if (cand_ms) cand_ms[t] = D.tuning[t].ms;
+    }
   });
 }
 

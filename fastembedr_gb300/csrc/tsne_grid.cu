@@ -714,9 +714,11 @@ rows_inverse_kernel(const float2* __restrict__ arow, const float2* __restrict__ 
 // Rows are taken in storage (spatial) order: slot_rows[s] = (begin, end) of the CSR row of the
 // point in slot s (rebuilt at every reorder), so a row is one contiguous segment of P and
 // consecutive rows of a warp belong to neighbouring points, whose neighbour sets overlap: their
-// y gathers hit L1. Warp w first takes chunk w of kAttrChunk consecutive slots, then further
+// y gathers hit L1. Warp w first takes chunk w of `chunk` consecutive slots, then further
 // chunks from a counter (the last warp to finish resets it for the next launch), which keeps
-// every SM busy to the end whatever the row lengths of a region. A row is read with 128-bit loads: lane l takes entries
+// every SM busy to the end whatever the row lengths of a region. The chunk size and the number of
+// resident blocks are launch parameters chosen at run time by timing (tsne_tune_attractive): the
+// result does not depend on them. A row is read with 128-bit loads: lane l takes entries
 // c0 + 4 l .. + 3 of each 128-entry round (c0 = the row's first entry rounded down to a multiple
 // of 4; entries outside the row are masked), kAttrRounds rounds loaded before their gathers.
 // Lane 0 keeps a bulk L2 prefetch (cp.async.bulk.prefetch) of the row kAttrAhead rows ahead.
@@ -726,7 +728,7 @@ rows_inverse_kernel(const float2* __restrict__ arow, const float2* __restrict__ 
 constexpr int kAttrThreads = 256;
 constexpr int kAttrWarps = kAttrThreads / 32;
 constexpr int kAttrAhead = 2;
-constexpr int kAttrChunk = 16;  // slots per work item
+constexpr int kAttrChunk = 8;  // default slots per work item
 constexpr int kAttrRounds = 2;  // 128-entry rounds loaded together
 
 __device__ __forceinline__ void prefetch_l2_range(const void* base, long long first, long long last, int elem) {
@@ -766,14 +768,14 @@ __device__ __forceinline__ void prefetch_row(const int2* __restrict__ slot_rows,
 }
 
 #ifndef FE_ATTR_MIN_BLOCKS
-#define FE_ATTR_MIN_BLOCKS 1
+#define FE_ATTR_MIN_BLOCKS 5
 #endif
 __global__ void __launch_bounds__(kAttrThreads, FE_ATTR_MIN_BLOCKS)
 attractive_kernel(const int2* __restrict__ slot_rows, const int* __restrict__ col, const float* __restrict__ val,
                   const float2* __restrict__ y, int n, float exag, float2* __restrict__ attr,
-                  unsigned* __restrict__ ctr) {
+                  unsigned* __restrict__ ctr, int chunk) {
   const int lane = threadIdx.x & 31;
-  const unsigned nchunks = (unsigned)((n + kAttrChunk - 1) / kAttrChunk);
+  const unsigned nchunks = (unsigned)((n + chunk - 1) / chunk);
   const unsigned nwarps = gridDim.x * kAttrWarps;
   // chunk gw first, then chunks nwarps, nwarps + 1, ... from the counter
   unsigned c = blockIdx.x * kAttrWarps + (threadIdx.x >> 5), next = 0;
@@ -781,9 +783,9 @@ attractive_kernel(const int2* __restrict__ slot_rows, const int* __restrict__ co
   next = __shfl_sync(0xffffffffu, next, 0);
   // slot at position t of chunk c (positions past the chunk run into chunk `next`), or -1
   auto slot_at = [&](int t) -> int {
-    const unsigned ch = t < kAttrChunk ? c : next;
+    const unsigned ch = t < chunk ? c : next;
     if (ch >= nchunks) return -1;
-    const int sl = (int)ch * kAttrChunk + (t < kAttrChunk ? t : t - kAttrChunk);
+    const int sl = (int)ch * chunk + (t < chunk ? t : t - chunk);
     return sl < n ? sl : -1;
   };
   if (lane == 0)
@@ -792,7 +794,7 @@ attractive_kernel(const int2* __restrict__ slot_rows, const int* __restrict__ co
       if (t >= 0) prefetch_row(slot_rows, col, val, t);
     }
   while (c < nchunks) {
-    for (int t = 0; t < kAttrChunk; ++t) {
+    for (int t = 0; t < chunk; ++t) {
       const int s = slot_at(t);
       if (s < 0) break;
       if (lane == 0) {
@@ -1290,8 +1292,55 @@ void tsne_bind_rows(TsneDevice& d, const DeviceCsr& P, cudaStream_t s) {
 
 void tsne_attractive_stage(TsneDevice& d, const DeviceCsr& P, float exag, cudaStream_t s) {
   attractive_kernel<<<d.attr_blocks, kAttrThreads, 0, s>>>(d.slot_rows, P.col, P.val, d.y, d.n, exag, d.attr,
-                                                           d.attr_ctr);
+                                                           d.attr_ctr, d.attr_chunk);
   FE_LAUNCH("attractive_kernel");
+}
+
+// Run-time tuning of the attractive pass's launch: every (chunk, resident blocks per SM)
+// candidate is launched once as warm-up and timed over `reps` launches with CUDA events on s, on
+// the current layout (the pass only writes the attractive force, which the next iteration
+// overwrites, so the optimizer state is untouched); the fastest is kept. Returns true when the
+// choice changed (captured graphs hold the old launch).
+bool tsne_tune_attractive(TsneDevice& d, const DeviceCsr& P, float exag, cudaStream_t s) {
+  int per_sm = 0;
+  FE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, attractive_kernel, kAttrThreads, 0));
+  per_sm = std::max(1, per_sm);
+  const int chunks[] = {4, 8, 16};
+  const int old_chunk = d.attr_chunk, old_blocks = d.attr_blocks;
+  cudaEvent_t e0, e1;
+  FE_CUDA(cudaEventCreate(&e0));
+  FE_CUDA(cudaEventCreate(&e1));
+  constexpr int reps = 2;
+  float best = -1.0f;
+  int best_chunk = old_chunk, best_blocks = old_blocks;
+  d.tuning.clear();
+  for (int per = per_sm; per >= std::max(1, per_sm - 1); --per) {
+    const int blocks = std::max(1, std::min(per * sm_count(), ceil_div(d.n, kAttrThreads / 32)));
+    for (int chunk : chunks) {
+      d.attr_chunk = chunk;
+      d.attr_blocks = blocks;
+      tsne_attractive_stage(d, P, exag, s);
+      FE_CUDA(cudaEventRecord(e0, s));
+      for (int r = 0; r < reps; ++r) tsne_attractive_stage(d, P, exag, s);
+      FE_CUDA(cudaEventRecord(e1, s));
+      FE_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.0f;
+      FE_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      ms /= reps;
+      d.tuning.push_back({chunk, blocks, ms});
+      if (best < 0.0f || ms < best) {
+        best = ms;
+        best_chunk = chunk;
+        best_blocks = blocks;
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  d.attr_chunk = best_chunk;
+  d.attr_blocks = best_blocks;
+  d.tuned = true;
+  return best_chunk != old_chunk || best_blocks != old_blocks;
 }
 
 void tsne_update_stage(TsneDevice& d, float lr, float mom, float min_gain, float max_step, cudaStream_t s) {

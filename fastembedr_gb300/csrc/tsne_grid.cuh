@@ -97,6 +97,13 @@ struct TsneDevice {
   int* inv = nullptr;
   int2* slot_rows = nullptr;     // CSR segment (begin, end) of the point in each storage slot
   unsigned* attr_ctr = nullptr;  // work counters of the attractive pass (zero between launches)
+  int attr_chunk = 8;            // slots per work item of the attractive pass
+  struct Tuning {
+    int chunk, blocks;
+    float ms;
+  };
+  std::vector<Tuning> tuning;    // timings of the run-time launch tuning (tsne_tune_attractive)
+  bool tuned = false;
   unsigned* keys = nullptr;
   unsigned* keys_tmp = nullptr;
   int* order = nullptr;
@@ -143,6 +150,9 @@ void tsne_iteration(TsneDevice& d, const DeviceCsr& P, float exaggeration, float
 // Stages, for profiling: scatter + FFT convolution, attractive (1), update (1).
 void tsne_grid_stage(TsneDevice& d, cudaStream_t s);
 void tsne_attractive_stage(TsneDevice& d, const DeviceCsr& P, float exaggeration, cudaStream_t s);
+// Time the attractive pass's launch candidates on the current layout and keep the fastest;
+// true when the launch changed.
+bool tsne_tune_attractive(TsneDevice& d, const DeviceCsr& P, float exaggeration, cudaStream_t s);
 void tsne_update_stage(TsneDevice& d, float learning_rate, float momentum, float min_gain, float max_step_norm,
                        cudaStream_t s);
 // Sort each instance's points by the Morton code of their stencil anchor on the current grid and

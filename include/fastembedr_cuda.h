@@ -346,6 +346,12 @@ int fastembedr_tsne_plan_layout(fastembedr_tsne_plan* plan, float* out);
  * reorder that starts every chunk of 25 iterations */
 int fastembedr_tsne_plan_info(fastembedr_tsne_plan* plan, long long* nnz, int* grid_size, int* interpolation,
                               int* launches_per_iteration, int* launches_per_reorder);
+/* The attractive pass's launch as tuned at run time (on the first normal-phase run of at least 25
+ * iterations, unless FASTEMBEDR_TSNE_AUTOTUNE=0): slots per work item and resident blocks, and up
+ * to `capacity` timed candidates (count receives how many were timed; 0 before tuning). The
+ * launch does not change any result. No counterpart in the reference. */
+int fastembedr_tsne_plan_tuning(fastembedr_tsne_plan* plan, int* chunk, int* blocks, int capacity, int* count,
+                                int* cand_chunk, int* cand_blocks, float* cand_ms);
 /* exact KL of the current layout (all-pairs Z on the GPU) */
 int fastembedr_tsne_plan_kl(fastembedr_tsne_plan* plan, double* kl);
 /* Gradient check of the plan's current layout at selected points (the force part of

@@ -320,3 +320,30 @@ def test_device_knn_entry_matches_reference_cpu(c1, monkeypatch):
     pc = O.knn_preservation(cpu, idx, keep=keep, preserve_k=15)
     pg = O.knn_preservation(out, idx, keep=keep, preserve_k=15)
     assert abs(pg - pc) < 0.01, (pg, pc)
+
+
+def test_attractive_launch_tuning_changes_no_result(small, monkeypatch):
+    """The run-time tuner of the attractive pass times (chunk size, resident blocks) candidates on
+    the first normal-phase run and keeps the fastest; the pass's result does not depend on the
+    launch, so a tuned plan and an untuned one give the same bits."""
+    import torch
+
+    idx, dist, _ = small
+    n, k = idx.shape
+    d_idx = torch.as_tensor(np.ascontiguousarray(idx.T), device="cuda")
+    d_dist = torch.as_tensor(np.ascontiguousarray(dist.T), device="cuda")
+    init = synthetic.tsne_init(n, 9)
+    outs, tunes = [], []
+    for flag in ("1", "0"):
+        monkeypatch.setenv("FASTEMBEDR_TSNE_AUTOTUNE", flag)
+        plan = api.TsnePlan(d_idx, d_dist, n, k, 15.0, init=init)
+        plan.run(50, 12.0, n / 12.0)
+        plan.run(50, 1.0, n / 12.0)
+        outs.append(plan.layout())
+        tunes.append(plan.tuning())
+        plan.close()
+    assert len(tunes[0]["candidates"]) == 6 and all(c["ms"] > 0 for c in tunes[0]["candidates"])
+    best = min(tunes[0]["candidates"], key=lambda c: c["ms"])
+    assert (tunes[0]["chunk"], tunes[0]["blocks"]) == (best["chunk"], best["blocks"])
+    assert tunes[1]["candidates"] == []
+    assert np.array_equal(outs[0], outs[1])
