@@ -722,14 +722,17 @@ rows_inverse_kernel(const float2* __restrict__ arow, const float2* __restrict__ 
 // c0 + 4 l .. + 3 of each 128-entry round (c0 = the row's first entry rounded down to a multiple
 // of 4; entries outside the row are masked), kAttrRounds rounds loaded before their gathers.
 // Lane 0 keeps a bulk L2 prefetch (cp.async.bulk.prefetch) of the row kAttrAhead rows ahead.
-// Each lane sums its entries in a fixed order, groups of rounds past the first 256 entries are
+// Each lane sums its entries in a fixed order, the rounds of a row longer than one group are
 // added with Kahan compensation, and the warp sum is a fixed butterfly: the force depends only
 // on the row and its entries' positions modulo 4, not on the schedule.
 constexpr int kAttrThreads = 256;
 constexpr int kAttrWarps = kAttrThreads / 32;
 constexpr int kAttrAhead = 2;
 constexpr int kAttrChunk = 8;  // default slots per work item
-constexpr int kAttrRounds = 2;  // 128-entry rounds loaded together
+#ifndef FE_ATTR_ROUNDS
+#define FE_ATTR_ROUNDS 1
+#endif
+constexpr int kAttrRounds = FE_ATTR_ROUNDS;  // 128-entry rounds loaded together
 
 __device__ __forceinline__ void prefetch_l2_range(const void* base, long long first, long long last, int elem) {
   // [first, last) elements of a 4-byte array, widened to 16-byte boundaries (the arena pads
@@ -768,7 +771,7 @@ __device__ __forceinline__ void prefetch_row(const int2* __restrict__ slot_rows,
 }
 
 #ifndef FE_ATTR_MIN_BLOCKS
-#define FE_ATTR_MIN_BLOCKS 5
+#define FE_ATTR_MIN_BLOCKS 6
 #endif
 __global__ void __launch_bounds__(kAttrThreads, FE_ATTR_MIN_BLOCKS)
 attractive_kernel(const int2* __restrict__ slot_rows, const int* __restrict__ col, const float* __restrict__ val,
