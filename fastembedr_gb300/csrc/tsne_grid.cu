@@ -728,11 +728,13 @@ rows_inverse_kernel(const float2* __restrict__ arow, const float2* __restrict__ 
 constexpr int kAttrThreads = 256;
 constexpr int kAttrWarps = kAttrThreads / 32;
 constexpr int kAttrAhead = 2;
-constexpr int kAttrChunk = 8;  // default slots per work item
+// Compile-time shape of the pass (measured alternatives in the attractive-pass variants profile):
+// 128-entry rounds loaded together (1: 40 registers) and the register cap that allows six
+// resident blocks per SM.
 #ifndef FE_ATTR_ROUNDS
 #define FE_ATTR_ROUNDS 1
 #endif
-constexpr int kAttrRounds = FE_ATTR_ROUNDS;  // 128-entry rounds loaded together
+constexpr int kAttrRounds = FE_ATTR_ROUNDS;
 
 __device__ __forceinline__ void prefetch_l2_range(const void* base, long long first, long long last, int elem) {
   // [first, last) elements of a 4-byte array, widened to 16-byte boundaries (the arena pads
