@@ -347,3 +347,24 @@ def test_attractive_launch_tuning_changes_no_result(small, monkeypatch):
     assert (tunes[0]["chunk"], tunes[0]["blocks"]) == (best["chunk"], best["blocks"])
     assert tunes[1]["candidates"] == []
     assert np.array_equal(outs[0], outs[1])
+
+
+def test_double_distance_entry_matches_float_entry(small):
+    """The double-distance entry point (R's numeric KNN distances; the reference casts them to
+    float, copy_distances_float_sexp in src/tsne_neighbors.cpp:338-363) gives the float entry
+    point's layout bit for bit on float-exact distances, with 1-based labels as R passes them."""
+    idx, dist, _ = small
+    n, k = idx.shape
+    lib = _lib.require_gpu()
+    init = synthetic.tsne_init(n, 11)
+    idx_cm = np.asfortranarray((idx + 1).astype(np.int32))
+    outs = []
+    for fn, d in ((lib.fastembedr_cuda_opentsne_fft_from_knn_float, np.asfortranarray(dist.astype(np.float32))),
+                  (lib.fastembedr_cuda_opentsne_fft_from_knn, np.asfortranarray(dist.astype(np.float32).astype(np.float64)))):
+        out = np.zeros((n, 2), np.float32)
+        st = fn(idx_cm.ctypes.data, d.ctypes.data, init.ctypes.data, 1, n, k, 2, 15.0, 60, 60, 12.0, 1.0, n / 12.0, 0,
+                0.8, 0.8, 0.01, 5.0, 4, 1, out.ctypes.data)
+        _lib.check(st, "t-SNE entry")
+        outs.append(out)
+    assert np.all(np.isfinite(outs[0])) and outs[0].std() > 1e-3
+    assert np.array_equal(outs[0], outs[1])
