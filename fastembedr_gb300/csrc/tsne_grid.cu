@@ -7,17 +7,19 @@
 // back, combine with the sparse attractive term and apply the gains/momentum update.
 //
 // GB300 layout of one iteration (6 launches, two streams, captured in a CUDA graph):
-//   side stream:  attractive_kernel        warp-per-row CSR attractive force (HBM stream of P)
-//   main stream:  scatter_kernel           points -> float4 charges (vector red, L2-resident grid)
-//                 rows_forward_kernel      row FFTs of the charges (2 packed planes) and kernel
-//                 columns_convolve_kernel  column FFTs of kernel + charges, Z by Parseval,
-//                                          multiply, inverse column FFT, all in shared memory
+//   side stream:  attractive_kernel        warp-per-row CSR attractive force, rows in storage
+//                                          (spatial) order (stream of P + L1/L2 gathers of y)
+//   main stream:  scatter_kernel           points -> 64-bit fixed-point charges (deterministic)
+//                 rows_forward_kernel      row FFTs of the charges (x + i y plane, paired mass
+//                                          rows as half spectra) and of the kernel rows
+//                 columns_convolve_kernel  column FFTs per conjugate column pair, Z by Parseval,
+//                                          multiply, inverse column FFTs, all in shared memory
 //                 rows_inverse_kernel      inverse row FFTs -> float4 potentials, Z finalised
 //   join:         update_kernel            potential gather + gains/momentum/step clip +
 //                                          recentring; epilogue reduces the new bounding box and
 //                                          mean into the next iteration's grid
-// The attractive pass (bandwidth-bound) overlaps the grid stage (latency/shared-memory bound).
-// Interpolation: the reference bilinear splat on G shared nodes, or (default) 3 equispaced
+// The attractive pass (load-latency-bound) runs beside the grid stage (shared-memory bound).
+// Interpolation: the reference bilinear splat on G shared nodes (default), or 3 equispaced
 // Lagrange nodes per box over floor(G / 3) boxes, as in FIt-SNE-style interpolation.
 #include <cfloat>
 #include <climits>
