@@ -38,6 +38,7 @@ SIGNATURES = {
     "fastembedr_cuda_umap_graph_from_knn": (I, [vp, vp, I, I, I, vp, vp, vp, vp, L, C.POINTER(L), C.POINTER(F)]),
     "fastembedr_cuda_umap_from_knn": (I, [vp, vp, vp, I, I, I, I, I, F, F, F, U, vp]),
     "fastembedr_cuda_umap_batch_from_knn": (I, [I, vp, vp, vp, vp, I, I, I, I, F, F, F, U, vp, C.POINTER(F)]),
+    "fastembedr_cuda_umap_batch_from_knn_rows": (I, [I, vp, vp, vp, vp, I, I, I, I, F, F, F, U, vp, C.POINTER(F)]),
     "fastembedr_cuda_umap_from_knn_profile": (I, [vp, vp, vp, I, I, I, I, I, F, F, F, U, vp, C.POINTER(F),
                                                   C.POINTER(F)]),
     "fastembedr_cuda_tsne_exact_repulsion_noalloc": (I, [vp, I, vp, vp, vp]),

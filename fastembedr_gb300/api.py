@@ -767,7 +767,7 @@ class TransformServer:
 
 def umap_knn_batch(knns, inits, seed=42, n_epochs=500, min_dist=0.01, negative_sample_rate=5, learning_rate=1.0,
                    repulsion_strength=1.0, return_time=False):
-    """umap_knn over many instances at once (C ABI fastembedr_cuda_umap_batch_from_knn): every
+    """umap_knn over many instances at once (C ABI fastembedr_cuda_umap_batch_from_knn_rows): every
     instance gets its own fuzzy graph and the package's SGD; one epoch is one launch over all
     instances' edges. Returns one (n_b, 2) layout per instance (and the SGD device time in ms)."""
     if not knns:
@@ -779,19 +779,22 @@ def umap_knn_batch(knns, inits, seed=42, n_epochs=500, min_dist=0.01, negative_s
     sizes = np.array([np.asarray(i).shape[0] for i, _ in knns], np.int32)
     offs = {knn_index_offset(i) for i, _ in knns}
     off = 1 if offs == {1} else 0
-    idx, dist = _concat_knn(knns)
-    y0 = np.concatenate([np.ascontiguousarray(y, np.float32).ravel() for y in inits])
-    if y0.size != 2 * sizes.sum():
+    # one row-major array per instance, passed by pointer (no concatenated copy)
+    idx = [np.ascontiguousarray(i, np.int32) for i, _ in knns]
+    dist = [np.ascontiguousarray(d, np.float32) for _, d in knns]
+    ys = [np.ascontiguousarray(y, np.float32) for y in inits]
+    if len(ys) != len(knns) or any(y.shape != (n, 2) for y, n in zip(ys, sizes)):
         raise ValueError("init row counts must match the KNN graphs")
-    out = np.zeros((int(sizes.sum()), 2), np.float32)
+    lays = [np.zeros((int(n), 2), np.float32) for n in sizes]
+    ptrs = lambda arrs: (C.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
     ms = C.c_float()
     lib = _lib.require_gpu()
-    st = lib.fastembedr_cuda_umap_batch_from_knn(len(knns), sizes.ctypes.data, idx.ctypes.data, dist.ctypes.data,
-                                                 y0.ctypes.data, k, off, int(n_epochs), int(negative_sample_rate),
-                                                 float(learning_rate), float(min_dist), float(repulsion_strength),
-                                                 int(seed) & 0xFFFFFFFF, out.ctypes.data, C.byref(ms))
+    st = lib.fastembedr_cuda_umap_batch_from_knn_rows(len(knns), sizes.ctypes.data, ptrs(idx), ptrs(dist), ptrs(ys),
+                                                      k, off, int(n_epochs), int(negative_sample_rate),
+                                                      float(learning_rate), float(min_dist),
+                                                      float(repulsion_strength), int(seed) & 0xFFFFFFFF, ptrs(lays),
+                                                      C.byref(ms))
     _lib.check(st, "CUDA UMAP batch")
-    lays = np.split(out, np.cumsum(sizes)[:-1])
     return (lays, ms.value) if return_time else lays
 
 

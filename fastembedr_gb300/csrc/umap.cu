@@ -1206,89 +1206,168 @@ int fastembedr_cuda_umap_from_knn_profile(const int* indices, const float* dista
   });
 }
 
+}  // extern "C"
+
+namespace fe {
+
+// Row-major nb x k block -> column-major (the layout the graph build reads).
+__global__ void umap_rows_to_cols_kernel(const int* __restrict__ idx_rm, const float* __restrict__ dist_rm, int nb,
+                                         int k, int* __restrict__ idx_cm, float* __restrict__ dist_cm) {
+  const long long total = (long long)nb * k;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long i = t / k, j = t - i * k;
+    idx_cm[j * nb + i] = idx_rm[t];
+    dist_cm[j * nb + i] = dist_rm[t];
+  }
+}
+
+// The batched UMAP job: instance b's KNN from idx_u[b] / dist_u[b] (column-major n_b x k, or
+// row-major when row_major), its start from init_u[b] (row-major n_b x 2), its layout to
+// out_u[b]. One fuzzy graph per instance, appended with vertex offsets, then every epoch one
+// launch over all instances' edges.
+void umap_batch_job(int n_instances, const int* sizes, const std::vector<const int*>& idx_u,
+                    const std::vector<const float*>& dist_u, const std::vector<const float*>& init_u,
+                    const std::vector<float*>& out_u, bool row_major, int k, int index_offset, int n_epochs,
+                    int negative_sample_rate, float learning_rate, float min_dist, float repulsion_strength,
+                    unsigned seed, float* sgd_ms) {
+  if (n_instances < 1 || k < 1 || n_epochs < 1 || negative_sample_rate < 0 || !(learning_rate > 0.0f) ||
+      min_dist < 0.0f || !(repulsion_strength > 0.0f))
+    throw Error("invalid CUDA UMAP batch parameters");
+  std::vector<int> vb(n_instances + 1, 0);
+  int max_n = 0;
+  for (int b = 0; b < n_instances; ++b) {
+    if (sizes[b] < 2) throw Error("UMAP batch: every instance needs at least two points");
+    if ((long long)vb[b] + sizes[b] > INT_MAX / 2) throw Error("UMAP batch: too many points");
+    vb[b + 1] = vb[b] + sizes[b];
+    max_n = std::max(max_n, sizes[b]);
+  }
+  const int n = vb[n_instances];
+  UmapJob job;
+  job.alloc(n);
+  cudaStream_t s = job.stream.s;
+  // one fuzzy graph per instance, then appended with vertex offsets
+  std::vector<std::unique_ptr<UmapGraph>> graphs(n_instances);
+  std::vector<long long> eb(n_instances + 1, 0);
+  {
+    int *d_idx = nullptr, *d_irm = nullptr;
+    float *d_dist = nullptr, *d_drm = nullptr;
+    Arena in;
+    in.reserve(&d_idx, (std::size_t)max_n * k);
+    in.reserve(&d_dist, (std::size_t)max_n * k);
+    if (row_major) {
+      in.reserve(&d_irm, (std::size_t)max_n * k);
+      in.reserve(&d_drm, (std::size_t)max_n * k);
+    }
+    in.commit("UMAP batch input");
+    for (int b = 0; b < n_instances; ++b) {
+      const std::size_t items = (std::size_t)sizes[b] * k;
+      if (row_major) {
+        FE_CUDA(cudaMemcpyAsync(d_irm, idx_u[b], sizeof(int) * items, cudaMemcpyHostToDevice, s));
+        FE_CUDA(cudaMemcpyAsync(d_drm, dist_u[b], sizeof(float) * items, cudaMemcpyHostToDevice, s));
+        umap_rows_to_cols_kernel<<<std::max(1, std::min(ceil_div((long long)items, 256), sm_count() * 8)), 256, 0,
+                                   s>>>(d_irm, d_drm, sizes[b], k, d_idx, d_dist);
+        FE_LAUNCH("umap_rows_to_cols_kernel");
+      } else {
+        FE_CUDA(cudaMemcpyAsync(d_idx, idx_u[b], sizeof(int) * items, cudaMemcpyHostToDevice, s));
+        FE_CUDA(cudaMemcpyAsync(d_dist, dist_u[b], sizeof(float) * items, cudaMemcpyHostToDevice, s));
+      }
+      validate_knn(d_idx, d_dist, sizes[b], k, index_offset, s);
+      graphs[b] = std::make_unique<UmapGraph>();
+      umap_build_graph(d_idx, d_dist, sizes[b], k, index_offset, *graphs[b], s);
+      eb[b + 1] = eb[b] + graphs[b]->nnz;
+    }
+  }
+  const long long n_edges = eb[n_instances];
+  int *heads = nullptr, *tails = nullptr, *d_vb = nullptr;
+  float* period = nullptr;
+  long long* d_eb = nullptr;
+  Arena ga;
+  ga.reserve(&heads, (std::size_t)std::max<long long>(n_edges, 1));
+  ga.reserve(&tails, (std::size_t)std::max<long long>(n_edges, 1));
+  ga.reserve(&period, (std::size_t)std::max<long long>(n_edges, 1));
+  ga.reserve(&d_eb, n_instances + 1);
+  ga.reserve(&d_vb, n_instances + 1);
+  ga.commit("UMAP batch graph");
+  for (int b = 0; b < n_instances; ++b) {
+    const UmapGraph& g = *graphs[b];
+    const int blocks = std::max(1, std::min(ceil_div(g.nnz, 256), sm_count() * 8));
+    umap_offset_edges_kernel<<<blocks, 256, 0, s>>>(g.heads, g.neighbors, g.nnz, vb[b], heads + eb[b],
+                                                    tails + eb[b]);
+    FE_LAUNCH("umap_offset_edges_kernel");
+    FE_CUDA(cudaMemcpyAsync(period + eb[b], g.eps, sizeof(float) * g.nnz, cudaMemcpyDeviceToDevice, s));
+  }
+  FE_CUDA(cudaMemcpyAsync(d_eb, eb.data(), sizeof(long long) * eb.size(), cudaMemcpyHostToDevice, s));
+  FE_CUDA(cudaMemcpyAsync(d_vb, vb.data(), sizeof(int) * vb.size(), cudaMemcpyHostToDevice, s));
+  for (int b = 0; b < n_instances; ++b)
+    FE_CUDA(cudaMemcpyAsync(job.y + vb[b], init_u[b], sizeof(float) * 2 * (std::size_t)sizes[b],
+                            cudaMemcpyHostToDevice, s));
+  FE_CUDA(cudaStreamSynchronize(s));
+  graphs.clear();
+  double av = 0.0, bv = 0.0;
+  umap_ab_params(1.0, min_dist, &av, &bv);
+  const UmapParams p{n, n_epochs, negative_sample_rate, seed, learning_rate, (float)av, (float)bv,
+                     repulsion_strength};
+  job.edge_begin = d_eb;
+  job.vert_begin = d_vb;
+  job.ninst = n_instances;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  for (auto& e : ev) FE_CUDA(cudaEventCreate(&e));
+  FE_CUDA(cudaEventRecord(ev[0], s));
+  job.run(heads, tails, period, n_edges, p);
+  FE_CUDA(cudaEventRecord(ev[1], s));
+  for (int b = 0; b < n_instances; ++b)
+    FE_CUDA(cudaMemcpyAsync(out_u[b], job.y + vb[b], sizeof(float) * 2 * (std::size_t)sizes[b],
+                            cudaMemcpyDeviceToHost, s));
+  FE_CUDA(cudaStreamSynchronize(s));
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, ev[0], ev[1]);
+  for (auto& e : ev) cudaEventDestroy(e);
+  if (sgd_ms) *sgd_ms = ms;
+}
+
+}  // namespace fe
+
+extern "C" {
+
 int fastembedr_cuda_umap_batch_from_knn(int n_instances, const int* sizes, const int* indices, const float* distances,
                                         const float* init, int k, int index_offset, int n_epochs,
                                         int negative_sample_rate, float learning_rate, float min_dist,
                                         float repulsion_strength, unsigned int seed, float* out, float* sgd_ms) {
   return fe::guarded([&] {
     if (!sizes || !indices || !distances || !init || !out) throw fe::Error("null UMAP batch pointer");
-    if (n_instances < 1 || k < 1 || n_epochs < 1 || negative_sample_rate < 0 || !(learning_rate > 0.0f) ||
-        min_dist < 0.0f || !(repulsion_strength > 0.0f))
-      throw fe::Error("invalid CUDA UMAP batch parameters");
-    std::vector<int> vb(n_instances + 1, 0);
-    int max_n = 0;
+    if (n_instances < 1) throw fe::Error("invalid CUDA UMAP batch parameters");
+    std::vector<const int*> iu(n_instances);
+    std::vector<const float*> du(n_instances), yu(n_instances);
+    std::vector<float*> ou(n_instances);
+    std::size_t at = 0;
     for (int b = 0; b < n_instances; ++b) {
-      if (sizes[b] < 2) throw fe::Error("UMAP batch: every instance needs at least two points");
-      if ((long long)vb[b] + sizes[b] > INT_MAX / 2) throw fe::Error("UMAP batch: too many points");
-      vb[b + 1] = vb[b] + sizes[b];
-      max_n = std::max(max_n, sizes[b]);
+      iu[b] = indices + at * k;
+      du[b] = distances + at * k;
+      yu[b] = init + 2 * at;
+      ou[b] = out + 2 * at;
+      at += (std::size_t)std::max(sizes[b], 0);
     }
-    const int n = vb[n_instances];
-    fe::UmapJob job;
-    job.alloc(n);
-    cudaStream_t s = job.stream.s;
-    // one fuzzy graph per instance, then appended with vertex offsets
-    std::vector<std::unique_ptr<fe::UmapGraph>> graphs(n_instances);
-    std::vector<long long> eb(n_instances + 1, 0);
-    {
-      int* d_idx = nullptr;
-      float* d_dist = nullptr;
-      fe::Arena in;
-      in.reserve(&d_idx, (std::size_t)max_n * k);
-      in.reserve(&d_dist, (std::size_t)max_n * k);
-      in.commit("UMAP batch input");
-      for (int b = 0; b < n_instances; ++b) {
-        const std::size_t items = (std::size_t)sizes[b] * k, at = (std::size_t)vb[b] * k;
-        FE_CUDA(cudaMemcpyAsync(d_idx, indices + at, sizeof(int) * items, cudaMemcpyHostToDevice, s));
-        FE_CUDA(cudaMemcpyAsync(d_dist, distances + at, sizeof(float) * items, cudaMemcpyHostToDevice, s));
-        fe::validate_knn(d_idx, d_dist, sizes[b], k, index_offset, s);
-        graphs[b] = std::make_unique<fe::UmapGraph>();
-        fe::umap_build_graph(d_idx, d_dist, sizes[b], k, index_offset, *graphs[b], s);
-        eb[b + 1] = eb[b] + graphs[b]->nnz;
-      }
-    }
-    const long long n_edges = eb[n_instances];
-    int *heads = nullptr, *tails = nullptr, *d_vb = nullptr;
-    float* period = nullptr;
-    long long* d_eb = nullptr;
-    fe::Arena ga;
-    ga.reserve(&heads, (std::size_t)std::max<long long>(n_edges, 1));
-    ga.reserve(&tails, (std::size_t)std::max<long long>(n_edges, 1));
-    ga.reserve(&period, (std::size_t)std::max<long long>(n_edges, 1));
-    ga.reserve(&d_eb, n_instances + 1);
-    ga.reserve(&d_vb, n_instances + 1);
-    ga.commit("UMAP batch graph");
-    for (int b = 0; b < n_instances; ++b) {
-      const fe::UmapGraph& g = *graphs[b];
-      const int blocks = std::max(1, std::min(fe::ceil_div(g.nnz, 256), fe::sm_count() * 8));
-      fe::umap_offset_edges_kernel<<<blocks, 256, 0, s>>>(g.heads, g.neighbors, g.nnz, vb[b], heads + eb[b],
-                                                          tails + eb[b]);
-      FE_LAUNCH("umap_offset_edges_kernel");
-      FE_CUDA(cudaMemcpyAsync(period + eb[b], g.eps, sizeof(float) * g.nnz, cudaMemcpyDeviceToDevice, s));
-    }
-    FE_CUDA(cudaMemcpyAsync(d_eb, eb.data(), sizeof(long long) * eb.size(), cudaMemcpyHostToDevice, s));
-    FE_CUDA(cudaMemcpyAsync(d_vb, vb.data(), sizeof(int) * vb.size(), cudaMemcpyHostToDevice, s));
-    FE_CUDA(cudaMemcpyAsync(job.y, init, sizeof(float) * 2 * (std::size_t)n, cudaMemcpyHostToDevice, s));
-    FE_CUDA(cudaStreamSynchronize(s));
-    graphs.clear();
-    double av = 0.0, bv = 0.0;
-    fe::umap_ab_params(1.0, min_dist, &av, &bv);
-    const fe::UmapParams p{n, n_epochs, negative_sample_rate, seed, learning_rate, (float)av, (float)bv,
-                           repulsion_strength};
-    job.edge_begin = d_eb;
-    job.vert_begin = d_vb;
-    job.ninst = n_instances;
-    cudaEvent_t ev[2] = {nullptr, nullptr};
-    for (auto& e : ev) FE_CUDA(cudaEventCreate(&e));
-    FE_CUDA(cudaEventRecord(ev[0], s));
-    job.run(heads, tails, period, n_edges, p);
-    FE_CUDA(cudaEventRecord(ev[1], s));
-    FE_CUDA(cudaMemcpyAsync(out, job.y, sizeof(float) * 2 * (std::size_t)n, cudaMemcpyDeviceToHost, s));
-    FE_CUDA(cudaStreamSynchronize(s));
-    float ms = 0.0f;
-    cudaEventElapsedTime(&ms, ev[0], ev[1]);
-    for (auto& e : ev) cudaEventDestroy(e);
-    if (sgd_ms) *sgd_ms = ms;
+    fe::umap_batch_job(n_instances, sizes, iu, du, yu, ou, false, k, index_offset, n_epochs, negative_sample_rate,
+                       learning_rate, min_dist, repulsion_strength, seed, sgd_ms);
+  });
+}
+
+int fastembedr_cuda_umap_batch_from_knn_rows(int n_instances, const int* sizes, const int* const* indices,
+                                             const float* const* distances, const float* const* inits, int k,
+                                             int index_offset, int n_epochs, int negative_sample_rate,
+                                             float learning_rate, float min_dist, float repulsion_strength,
+                                             unsigned int seed, float* const* outs, float* sgd_ms) {
+  return fe::guarded([&] {
+    if (!sizes || !indices || !distances || !inits || !outs || n_instances < 1)
+      throw fe::Error("null UMAP batch pointer");
+    std::vector<const int*> iu(indices, indices + n_instances);
+    std::vector<const float*> du(distances, distances + n_instances), yu(inits, inits + n_instances);
+    std::vector<float*> ou(outs, outs + n_instances);
+    for (int b = 0; b < n_instances; ++b)
+      if (!iu[b] || !du[b] || !yu[b] || !ou[b]) throw fe::Error("null UMAP batch pointer");
+    fe::umap_batch_job(n_instances, sizes, iu, du, yu, ou, true, k, index_offset, n_epochs, negative_sample_rate,
+                       learning_rate, min_dist, repulsion_strength, seed, sgd_ms);
   });
 }
 

@@ -199,6 +199,14 @@ int fastembedr_cuda_umap_batch_from_knn(int n_instances, const int* sizes, const
                                         const float* init, int k, int index_offset, int n_epochs,
                                         int negative_sample_rate, float learning_rate, float min_dist,
                                         float repulsion_strength, unsigned int seed, float* out, float* sgd_ms);
+/* No reference counterpart: the same batched UMAP job from one host pointer per instance, so a
+ * host whose instances sit in separate arrays makes no concatenated copy: indices[b] /
+ * distances[b] row-major (C order) n_b x k, inits[b] and outs[b] row-major n_b x 2. */
+int fastembedr_cuda_umap_batch_from_knn_rows(int n_instances, const int* sizes, const int* const* indices,
+                                             const float* const* distances, const float* const* inits, int k,
+                                             int index_offset, int n_epochs, int negative_sample_rate,
+                                             float learning_rate, float min_dist, float repulsion_strength,
+                                             unsigned int seed, float* const* outs, float* sgd_ms);
 /* The same job, reporting device time (CUDA events on the job's stream) of the graph build and
  * of the n_epochs SGD epochs; either output may be NULL. */
 int fastembedr_cuda_umap_from_knn_profile(const int* indices, const float* distances, const float* init, int n,

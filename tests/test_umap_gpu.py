@@ -114,6 +114,35 @@ def test_batched_umap_matches_each_instance_alone():
         assert abs(pa - pb[j]) < 0.01, (idx.shape[0], pa, pb[j])
 
 
+def test_batched_umap_column_major_entry_matches_rows_entry():
+    """The concatenated column-major batch entry and the per-instance row-major one run the same
+    job: mean 15-NN preservation of two runs each within 0.01 per instance (Hogwild runs differ)."""
+    import ctypes as C
+
+    knns, inits = [], []
+    for j, n in enumerate([4000, 9000]):
+        x, _ = synthetic.mixture(n, 20, 6, 320 + j, centre_sd=3.0)
+        knns.append(synthetic.exact_knn_numpy(x, 15))
+        inits.append(_pca_init(x, 420 + j))
+    sizes = np.array([i.shape[0] for i, _ in knns], np.int32)
+    idx, dist = api._concat_knn(knns)
+    y0 = np.concatenate([y.ravel() for y in inits]).astype(np.float32)
+    lib = _lib.require_gpu()
+    keeps = [np.arange(0, s_, 2, dtype=np.int32) for s_ in sizes]
+    pc, pr = np.zeros(2), np.zeros(2)
+    for _ in range(2):
+        out = np.zeros((int(sizes.sum()), 2), np.float32)
+        _lib.check(lib.fastembedr_cuda_umap_batch_from_knn(2, sizes.ctypes.data, idx.ctypes.data, dist.ctypes.data,
+                                                           y0.ctypes.data, 15, 0, 200, 5, 1.0, 0.01, 1.0, 42,
+                                                           out.ctypes.data, C.byref(C.c_float())), "column-major batch")
+        cm = np.split(out, np.cumsum(sizes)[:-1])
+        rows = api.umap_knn_batch(knns, inits, n_epochs=200)
+        for j, (i, _) in enumerate(knns):
+            pc[j] += O.knn_preservation(cm[j], i, keep=keeps[j], preserve_k=15) / 2
+            pr[j] += O.knn_preservation(rows[j], i, keep=keeps[j], preserve_k=15) / 2
+    assert np.all(np.abs(pc - pr) < 0.01), (pc, pr)
+
+
 @pytest.mark.parametrize("tag", ["3k", "200"])
 def test_diffusion_start_matches_reference_golden(golden, tag):
     """fastembedr_cuda_spectral_init_from_knn against the reference's CPU statement of its GPU
