@@ -1,6 +1,10 @@
 // Error state, arena and device queries shared by the kernels of this library.
 #include "common.cuh"
 
+#include <cstring>
+#include <mutex>
+#include <thread>
+
 namespace fe {
 
 namespace {
@@ -44,6 +48,76 @@ void Arena::release() {
   base_ = nullptr;
   total_ = 0;
   plan_.clear();
+}
+
+namespace {
+// Two pinned staging buffers of kChunk bytes, allocated on the first large upload and kept for
+// the life of the process; a mutex serialises uploads from different host threads.
+constexpr std::size_t kChunk = std::size_t(32) << 20;
+constexpr int kCopyThreads = 4;
+
+struct Stager {
+  std::mutex mu;
+  char* buf[2] = {nullptr, nullptr};
+  cudaEvent_t done[2] = {nullptr, nullptr};
+  int next = 0;
+  void ensure() {
+    for (int b = 0; b < 2; ++b) {
+      if (!buf[b]) FE_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&buf[b]), kChunk, cudaHostAllocDefault));
+      if (!done[b]) FE_CUDA(cudaEventCreateWithFlags(&done[b], cudaEventDisableTiming));
+    }
+  }
+};
+
+Stager& stager() {
+  static Stager* st = new Stager();  // never destroyed: the driver frees pinned memory at exit
+  return *st;
+}
+
+// memcpy of one staging chunk, split over a few host threads (one memory stream per thread
+// reaches only a fraction of the host's bandwidth)
+void parallel_copy(char* to, const char* from, std::size_t n) {
+  const std::size_t part = (n + kCopyThreads - 1) / kCopyThreads;
+  if (n < (std::size_t(4) << 20)) {
+    std::memcpy(to, from, n);
+    return;
+  }
+  std::thread th[kCopyThreads - 1];
+  int started = 0;
+  for (int t = 1; t < kCopyThreads; ++t) {
+    const std::size_t off = (std::size_t)t * part;
+    if (off >= n) break;
+    const std::size_t len = std::min(part, n - off);
+    th[started++] = std::thread([=] { std::memcpy(to + off, from + off, len); });
+  }
+  std::memcpy(to, from, std::min(part, n));
+  for (int t = 0; t < started; ++t) th[t].join();
+}
+}  // namespace
+
+void upload(void* dst, const void* src, std::size_t bytes, cudaStream_t s) {
+  if (bytes == 0) return;
+  cudaPointerAttributes attr{};
+  const bool pinned = cudaPointerGetAttributes(&attr, src) == cudaSuccess && attr.type == cudaMemoryTypeHost;
+  cudaGetLastError();
+  if (bytes < kStagedUploadMin || pinned) {  // pinned sources are copied by DMA directly
+    FE_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+    return;
+  }
+  Stager& st = stager();
+  std::lock_guard<std::mutex> lock(st.mu);
+  st.ensure();
+  const char* from = static_cast<const char*>(src);
+  char* to = static_cast<char*>(dst);
+  for (std::size_t off = 0; off < bytes; off += kChunk) {
+    const std::size_t n = std::min(kChunk, bytes - off);
+    const int b = st.next;
+    st.next ^= 1;
+    FE_CUDA(cudaEventSynchronize(st.done[b]));  // the last copy out of this buffer has finished
+    parallel_copy(st.buf[b], from + off, n);
+    FE_CUDA(cudaMemcpyAsync(to + off, st.buf[b], n, cudaMemcpyHostToDevice, s));
+    FE_CUDA(cudaEventRecord(st.done[b], s));
+  }
 }
 
 int sm_count() {

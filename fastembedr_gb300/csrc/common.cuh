@@ -97,6 +97,16 @@ inline int ceil_div(long long a, long long b) { return static_cast<int>((a + b -
 void order_after_legacy_stream(cudaStream_t s);
 int sm_count();
 
+// ---------------------------------------------------------------- host uploads
+// Host -> device copy of caller memory (pageable or not), ordered on stream s. Copies of at
+// least kStagedUploadMin bytes go through a process-wide pair of pinned staging buffers: host
+// threads fill one buffer while the copy engine drains the other, so large inputs move at
+// pinned-copy speed rather than through the driver's pageable path. The source may be reused
+// when the call returns. Smaller copies, and copies from pinned memory, are plain
+// cudaMemcpyAsync calls.
+constexpr std::size_t kStagedUploadMin = std::size_t(8) << 20;
+void upload(void* dst, const void* src, std::size_t bytes, cudaStream_t s);
+
 // ---------------------------------------------------------------- device helpers
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll

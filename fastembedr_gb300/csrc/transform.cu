@@ -554,8 +554,8 @@ extern "C" int fastembedr_cuda_transform_tsne(const double* reference_layout, in
     a.reserve(&d_jump, 1);
     a.commit("CUDA t-SNE transform");
     FE_CUDA(cudaMemcpyAsync(d_ref_cm, reference_layout, sizeof(double) * 2 * n_reference, cudaMemcpyHostToDevice, s));
-    FE_CUDA(cudaMemcpyAsync(d_idx, indices, sizeof(int) * items, cudaMemcpyHostToDevice, s));
-    FE_CUDA(cudaMemcpyAsync(d_dist, distances, sizeof(double) * items, cudaMemcpyHostToDevice, s));
+    fe::upload(d_idx, indices, sizeof(int) * items, s);
+    fe::upload(d_dist, distances, sizeof(double) * items, s);
     if (have_init)
       FE_CUDA(cudaMemcpyAsync(d_init, y_init, sizeof(double) * 2 * n_query, cudaMemcpyHostToDevice, s));
     fe::TransformSegment seg{d_idx, nullptr, d_dist, have_init ? d_init : nullptr, d_nb, d_p, d_state, d_opt,

@@ -23,6 +23,11 @@ struct DeviceCsr {
 
 // Validate KNN input (column-major n x k); throws with the reference CPU messages.
 void validate_knn(const int* d_idx, const float* d_dist, int n, int k, int offset, cudaStream_t s);
+// Stream-ordered form: ORs the failure bits into *d_flags (bit 0 index range, bit 1 distance)
+// without waiting; knn_flags_check throws the matching error for flags read back later.
+void validate_knn_async(const int* d_idx, const float* d_dist, int n, int k, int offset, unsigned* d_flags,
+                        cudaStream_t s);
+void knn_flags_check(unsigned flags);
 
 // Per-row perplexity bisection (FP32 exp, FP64 sums); writes directed P row-major n x k and,
 // when non-null, the entropy reached by each row.

@@ -39,20 +39,29 @@ __global__ void validate_knn_kernel(const int* __restrict__ idx, const float* __
   if (local) atomicOr(flags, local);
 }
 
-void validate_knn(const int* d_idx, const float* d_dist, int n, int k, int offset, cudaStream_t s) {
-  unsigned* d_flags = nullptr;
-  FE_CUDA(cudaMallocAsync(&d_flags, sizeof(unsigned), s));
-  FE_CUDA(cudaMemsetAsync(d_flags, 0, sizeof(unsigned), s));
+void validate_knn_async(const int* d_idx, const float* d_dist, int n, int k, int offset, unsigned* d_flags,
+                        cudaStream_t s) {
   const long long total = (long long)n * k;
   const int blocks = std::max(1, std::min(ceil_div(total, 256), sm_count() * 8));
   validate_knn_kernel<<<blocks, 256, 0, s>>>(d_idx, d_dist, total, n, offset, d_flags);
   FE_LAUNCH("validate_knn_kernel");
+}
+
+void knn_flags_check(unsigned flags) {
+  if (flags & 1u) throw Error("KNN indices are out of range.");
+  if (flags & 2u) throw Error("KNN distances must be finite and non-negative.");
+}
+
+void validate_knn(const int* d_idx, const float* d_dist, int n, int k, int offset, cudaStream_t s) {
+  unsigned* d_flags = nullptr;
+  FE_CUDA(cudaMallocAsync(&d_flags, sizeof(unsigned), s));
+  FE_CUDA(cudaMemsetAsync(d_flags, 0, sizeof(unsigned), s));
+  validate_knn_async(d_idx, d_dist, n, k, offset, d_flags, s);
   unsigned flags = 0u;
   FE_CUDA(cudaMemcpyAsync(&flags, d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
   FE_CUDA(cudaStreamSynchronize(s));
   FE_CUDA(cudaFreeAsync(d_flags, s));
-  if (flags & 1u) throw Error("KNN indices are out of range.");
-  if (flags & 2u) throw Error("KNN distances must be finite and non-negative.");
+  knn_flags_check(flags);
 }
 
 // ---------------------------------------------------------------- bisection

@@ -260,15 +260,18 @@ struct TsneJob {
       tmp.reserve(&d_p, items);
       tmp.commit("t-SNE batch affinities");
       int* d_range = nullptr;
+      unsigned* d_flags = nullptr;
       Arena rng;
       rng.reserve(&d_range, 2);
+      rng.reserve(&d_flags, 1);
       rng.commit("t-SNE batch label range");
+      FE_CUDA(cudaMemsetAsync(d_flags, 0, sizeof(unsigned), s));
       for (int t = 0; t < ninst; ++t) {
         const int u = user[t], nb = sz[t];
         const std::size_t cnt = (std::size_t)nb * k;
         const std::size_t loc = (std::size_t)first[t] * k;
-        FE_CUDA(cudaMemcpyAsync(d_loc_idx + loc, idx_u[u], sizeof(int) * cnt, cudaMemcpyHostToDevice, s));
-        FE_CUDA(cudaMemcpyAsync(d_loc_dist + loc, dist_u[u], sizeof(float) * cnt, cudaMemcpyHostToDevice, s));
+        fe::upload(d_loc_idx + loc, idx_u[u], sizeof(int) * cnt, s);
+        fe::upload(d_loc_dist + loc, dist_u[u], sizeof(float) * cnt, s);
         const int blocks = std::max(1, std::min(ceil_div((long long)cnt, 256), sm_count() * 8));
         int off = offset;
         if (off < 0) {
@@ -281,11 +284,16 @@ struct TsneJob {
           FE_CUDA(cudaStreamSynchronize(s));
           off = (h_range[0] >= 1 && h_range[1] <= nb) ? 1 : 0;
         }
-        validate_knn(d_loc_idx + loc, d_loc_dist + loc, nb, k, off, s);
+        validate_knn_async(d_loc_idx + loc, d_loc_dist + loc, nb, k, off, d_flags, s);
         globalize_knn_kernel<<<blocks, 256, 0, s>>>(d_loc_idx + loc, d_loc_dist + loc, nb, k, off, row_major ? 1 : 0,
                                                     first[t], n, d_idx, d_dist);
         FE_LAUNCH("globalize_knn_kernel");
       }
+      // every instance's KNN is checked before the global labels are used
+      unsigned flags = 0u;
+      FE_CUDA(cudaMemcpyAsync(&flags, d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+      FE_CUDA(cudaStreamSynchronize(s));
+      knn_flags_check(flags);
       row_probabilities(d_idx, d_dist, n, k, perplexity, d_p, nullptr, s);
       symmetrise_batch(d_idx, d_p, n, k, 0, first, P, nullptr, s);
     }
@@ -410,12 +418,12 @@ std::vector<float> pca_start(const void* values, bool is_double, int n, int p, c
   a.reserve(&init, n);
   a.commit("device PCA input");
   if (is_double) {
-    FE_CUDA(cudaMemcpyAsync(raw, values, sizeof(double) * items, cudaMemcpyHostToDevice, s));
+    fe::upload(raw, values, sizeof(double) * items, s);
     double_to_float_kernel<<<std::max(1, std::min(ceil_div((long long)items, 256), sm_count() * 8)), 256, 0, s>>>(
         raw, X, (long long)items);
     FE_LAUNCH("double_to_float_kernel");
   } else {
-    FE_CUDA(cudaMemcpyAsync(X, values, sizeof(float) * items, cudaMemcpyHostToDevice, s));
+    fe::upload(X, values, sizeof(float) * items, s);
   }
   pca_tsne_start(X, n, p, init, s);
   std::vector<float> h(2 * (std::size_t)n);
@@ -454,19 +462,19 @@ int run_tsne_from_knn(const int* indices, const DistT* distances, bool on_device
     if (!on_device && !std::is_same<DistT, float>::value) in.reserve(&d_raw, items);
     in.commit("CUDA openTSNE KNN input");
     const int* idx_ptr = on_device ? indices : d_idx;
-    if (!on_device) FE_CUDA(cudaMemcpyAsync(d_idx, indices, sizeof(int) * items, cudaMemcpyHostToDevice, s));
+    if (!on_device) fe::upload(d_idx, indices, sizeof(int) * items, s);
     const float* dist_ptr = nullptr;
     if constexpr (std::is_same<DistT, float>::value) {
       if (on_device) {
         dist_ptr = distances;
       } else {
-        FE_CUDA(cudaMemcpyAsync(d_dist, distances, sizeof(float) * items, cudaMemcpyHostToDevice, s));
+        fe::upload(d_dist, distances, sizeof(float) * items, s);
         dist_ptr = d_dist;
       }
     } else {
       const DistT* src = distances;
       if (!on_device) {
-        FE_CUDA(cudaMemcpyAsync(d_raw, distances, sizeof(DistT) * items, cudaMemcpyHostToDevice, s));
+        fe::upload(d_raw, distances, sizeof(DistT) * items, s);
         src = d_raw;
       }
       double_to_float_kernel<<<std::max(1, std::min(ceil_div((long long)items, 256), sm_count() * 8)), 256, 0, s>>>(
@@ -587,8 +595,8 @@ int fastembedr_cuda_tsne_affinities(const int* indices, const float* distances, 
     a.reserve(&d_p, items);
     a.reserve(&d_h, n);
     a.commit("t-SNE affinity diagnostic");
-    FE_CUDA(cudaMemcpyAsync(d_idx, indices, sizeof(int) * items, cudaMemcpyHostToDevice, st.s));
-    FE_CUDA(cudaMemcpyAsync(d_dist, distances, sizeof(float) * items, cudaMemcpyHostToDevice, st.s));
+    fe::upload(d_idx, indices, sizeof(int) * items, st.s);
+    fe::upload(d_dist, distances, sizeof(float) * items, st.s);
     fe::validate_knn(d_idx, d_dist, n, k, index_offset, st.s);
     fe::row_probabilities(d_idx, d_dist, n, k, perplexity, d_p, d_h, st.s);
     fe::DeviceCsr P;
@@ -644,8 +652,8 @@ int fastembedr_cuda_tsne_force_diagnostic(const int* indices, const float* dista
     a.reserve(&d_work, n);
     a.reserve(&d_sc, 4);
     a.commit("t-SNE force diagnostic");
-    FE_CUDA(cudaMemcpyAsync(d_idx, indices, sizeof(int) * items, cudaMemcpyHostToDevice, s));
-    FE_CUDA(cudaMemcpyAsync(d_dist, distances, sizeof(float) * items, cudaMemcpyHostToDevice, s));
+    fe::upload(d_idx, indices, sizeof(int) * items, s);
+    fe::upload(d_dist, distances, sizeof(float) * items, s);
     FE_CUDA(cudaMemcpyAsync(d_y, layout, sizeof(float) * 2 * n, cudaMemcpyHostToDevice, s));
     FE_CUDA(cudaStreamSynchronize(s));
     job.prepare(d_idx, d_dist, layout, n, k, perplexity, index_offset, grid, mode, 0u);

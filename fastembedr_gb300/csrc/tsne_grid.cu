@@ -374,7 +374,52 @@ __device__ __forceinline__ float2 twiddle(const float2* __restrict__ tw, int x, 
   return w;
 }
 
-// Decimation in time: stages s .. s + R - 1 (input of the FFT in bit-reversed order).
+// Radix-2 butterflies of one work item held in registers: v[e] is element i0 + e * h of its
+// sequence, h = 2^s, j = i0 mod h. Decimation in time: stages s .. s + R - 1 (input of the FFT
+// in bit-reversed order).
+template <int R>
+__device__ __forceinline__ void dit_regs(float2 (&v)[1 << R], int j, int s, int logm, const float2* __restrict__ tw,
+                                         bool inverse) {
+  constexpr int E = 1 << R;
+  const int h = 1 << s;
+#pragma unroll
+  for (int st = 0; st < R; ++st) {
+    const int span = 1 << st;               // partner distance in units of h
+    const int shift = logm - 1 - (s + st);  // twiddle stride for block length 2^(s+st+1)
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      if (e & span) continue;
+      const float2 w = twiddle(tw, j + (e & (span - 1)) * h, shift, inverse);
+      const float2 x = cmul(v[e + span], w);
+      const float2 u = v[e];
+      v[e] = make_float2(u.x + x.x, u.y + x.y);
+      v[e + span] = make_float2(u.x - x.x, u.y - x.y);
+    }
+  }
+}
+
+// Decimation in frequency: stages s + R - 1 down to s (output in bit-reversed order).
+template <int R>
+__device__ __forceinline__ void dif_regs(float2 (&v)[1 << R], int j, int s, int logm, const float2* __restrict__ tw,
+                                         bool inverse) {
+  constexpr int E = 1 << R;
+  const int h = 1 << s;
+#pragma unroll
+  for (int st = R - 1; st >= 0; --st) {
+    const int span = 1 << st;
+    const int shift = logm - 1 - (s + st);
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      if (e & span) continue;
+      const float2 w = twiddle(tw, j + (e & (span - 1)) * h, shift, inverse);
+      const float2 u = v[e], x = v[e + span];
+      v[e] = make_float2(u.x + x.x, u.y + x.y);
+      v[e + span] = cmul(make_float2(u.x - x.x, u.y - x.y), w);
+    }
+  }
+}
+
+// One shared-memory pass of R stages starting at stage s over `count` sequences.
 template <int R>
 __device__ __forceinline__ void dit_pass(float2* buf, int count, int logm, int s, const float2* __restrict__ tw,
                                          bool inverse) {
@@ -389,26 +434,12 @@ __device__ __forceinline__ void dit_pass(float2* buf, int count, int logm, int s
     float2 v[E];
 #pragma unroll
     for (int e = 0; e < E; ++e) v[e] = buf[sidx(i0 + e * h)];
-#pragma unroll
-    for (int st = 0; st < R; ++st) {
-      const int span = 1 << st;            // partner distance in units of h
-      const int shift = logm - 1 - (s + st);  // twiddle stride for block length 2^(s+st+1)
-#pragma unroll
-      for (int e = 0; e < E; ++e) {
-        if (e & span) continue;
-        const float2 w = twiddle(tw, j + (e & (span - 1)) * h, shift, inverse);
-        const float2 x = cmul(v[e + span], w);
-        const float2 u = v[e];
-        v[e] = make_float2(u.x + x.x, u.y + x.y);
-        v[e + span] = make_float2(u.x - x.x, u.y - x.y);
-      }
-    }
+    dit_regs<R>(v, j, s, logm, tw, inverse);
 #pragma unroll
     for (int e = 0; e < E; ++e) buf[sidx(i0 + e * h)] = v[e];
   }
 }
 
-// Decimation in frequency: stages s + R - 1 down to s (output in bit-reversed order).
 template <int R>
 __device__ __forceinline__ void dif_pass(float2* buf, int count, int logm, int s, const float2* __restrict__ tw,
                                          bool inverse) {
@@ -423,28 +454,20 @@ __device__ __forceinline__ void dif_pass(float2* buf, int count, int logm, int s
     float2 v[E];
 #pragma unroll
     for (int e = 0; e < E; ++e) v[e] = buf[sidx(i0 + e * h)];
-#pragma unroll
-    for (int st = R - 1; st >= 0; --st) {
-      const int span = 1 << st;
-      const int shift = logm - 1 - (s + st);
-#pragma unroll
-      for (int e = 0; e < E; ++e) {
-        if (e & span) continue;
-        const float2 w = twiddle(tw, j + (e & (span - 1)) * h, shift, inverse);
-        const float2 u = v[e], x = v[e + span];
-        v[e] = make_float2(u.x + x.x, u.y + x.y);
-        v[e + span] = cmul(make_float2(u.x - x.x, u.y - x.y), w);
-      }
-    }
+    dif_regs<R>(v, j, s, logm, tw, inverse);
 #pragma unroll
     for (int e = 0; e < E; ++e) buf[sidx(i0 + e * h)] = v[e];
   }
 }
 
+// Stages lo .. hi - 1 (decimation in time) or top down to lo (decimation in frequency), at most
+// MAXR per shared-memory pass; each pass ends with a barrier.
 template <int MAXR = 4>
-__device__ void fft_dit(float2* buf, int count, int logm, const float2* __restrict__ tw, bool inverse) {
-  for (int s = 0; s < logm;) {
-    const int r = min(MAXR, logm - s);
+__device__ void fft_dit(float2* buf, int count, int logm, const float2* __restrict__ tw, bool inverse, int lo = 0,
+                        int hi = -1) {
+  if (hi < 0) hi = logm;
+  for (int s = lo; s < hi;) {
+    const int r = min(MAXR, hi - s);
     if (r == 4) dit_pass<4>(buf, count, logm, s, tw, inverse);
     else if (r == 3) dit_pass<3>(buf, count, logm, s, tw, inverse);
     else if (r == 2) dit_pass<2>(buf, count, logm, s, tw, inverse);
@@ -455,9 +478,11 @@ __device__ void fft_dit(float2* buf, int count, int logm, const float2* __restri
 }
 
 template <int MAXR = 4>
-__device__ void fft_dif(float2* buf, int count, int logm, const float2* __restrict__ tw, bool inverse) {
-  for (int top = logm - 1; top >= 0;) {
-    const int r = min(MAXR, top + 1);
+__device__ void fft_dif(float2* buf, int count, int logm, const float2* __restrict__ tw, bool inverse, int top = -1,
+                        int lo = 0) {
+  if (top < 0) top = logm - 1;
+  while (top >= lo) {
+    const int r = min(MAXR, top - lo + 1);
     const int s = top - r + 1;
     if (r == 4) dif_pass<4>(buf, count, logm, s, tw, inverse);
     else if (r == 3) dif_pass<3>(buf, count, logm, s, tw, inverse);
@@ -588,7 +613,74 @@ rows_forward_kernel(const TsneInstance* __restrict__ inst, const int* __restrict
 // Kq + i Kq2), the Parseval sum of |B^|^2 Kq over both columns of the pair (Z + n up to the
 // 1 / M^2 scale), the products with Kq2 and their inverse column FFTs; rows < nodes of the
 // results go back to arow / brow.
-__global__ void __launch_bounds__(kColThreads)
+//
+// Three shared-memory round trips of the plain scheme are kept in registers, with the same
+// radix-2 butterflies: the top forward pass takes its inputs straight from global memory, the
+// last forward pass (stages 2 .. 0, groups of 8 consecutive positions), the products and the
+// first inverse pass (stages 0 .. 2, the same groups) run in one pass, and the top inverse pass
+// writes its outputs straight to global memory.
+constexpr int kColBottom = 3;
+
+template <int R>
+__device__ __forceinline__ void col_load_dif_top(float2* sbuf, const float2* __restrict__ arow,
+                                                 const float2* __restrict__ brow, const float2* __restrict__ krow,
+                                                 int c, int c2, int nodes, int logm, const float2* __restrict__ tw) {
+  constexpr int E = 1 << R;
+  const int m = 1 << logm, hm = m >> 1;
+  const int s = logm - R, h = 1 << s;
+  const int items = 4 << s;
+  for (int t = threadIdx.x; t < items; t += blockDim.x) {
+    const int seq = t >> s, j = t & (h - 1);
+    float2 v[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const int r = j + e * h;
+      float2 x = make_float2(0.0f, 0.0f);
+      if (seq == 3) {
+        const int dy = r < hm ? r : m - r;
+        if (dy <= nodes - 1) x = krow[(long long)dy * (hm + 1) + c];
+      } else if (r < nodes) {
+        x = seq == 2 ? brow[(long long)r * (hm + 1) + c] : arow[(long long)r * m + (seq == 0 ? c : c2)];
+      }
+      v[e] = x;
+    }
+    dif_regs<R>(v, j, s, logm, tw, false);
+#pragma unroll
+    for (int e = 0; e < E; ++e) sbuf[sidx((seq << logm) + j + e * h)] = v[e];
+  }
+}
+
+template <int R>
+__device__ __forceinline__ void col_dit_top_store(const float2* sbuf, float2* __restrict__ arow,
+                                                  float2* __restrict__ brow, int c, int c2, int nodes, int logm,
+                                                  const float2* __restrict__ tw) {
+  constexpr int E = 1 << R;
+  const int m = 1 << logm, hm = m >> 1;
+  const int s = logm - R, h = 1 << s;
+  const int items = 3 << s;
+  for (int t = threadIdx.x; t < items; t += blockDim.x) {
+    const int seq = t >> s, j = t & (h - 1);
+    if (seq == 1 && c2 == c) continue;
+    float2 v[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) v[e] = sbuf[sidx((seq << logm) + j + e * h)];
+    dit_regs<R>(v, j, s, logm, tw, true);
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const int r = j + e * h;
+      if (r < nodes) {
+        if (seq == 2) brow[(long long)r * (hm + 1) + c] = v[e];
+        else arow[(long long)r * m + (seq == 0 ? c : c2)] = v[e];
+      }
+    }
+  }
+}
+
+// 3 blocks per SM, as the 4 x M complex shared-memory buffer allows at M = 2048
+#ifndef FE_COL_MIN_BLOCKS
+#define FE_COL_MIN_BLOCKS 3
+#endif
+__global__ void __launch_bounds__(kColThreads, FE_COL_MIN_BLOCKS)
 columns_convolve_kernel(float2* __restrict__ arow, float2* __restrict__ brow, const float2* __restrict__ krow,
                         int nodes, int logm, const float2* __restrict__ tw, double* __restrict__ zpart) {
   extern __shared__ float2 sbuf[];  // [A_c][A_c'][B_c][K_c]
@@ -600,42 +692,45 @@ columns_convolve_kernel(float2* __restrict__ arow, float2* __restrict__ brow, co
   brow += (long long)blockIdx.y * nodes * (hm + 1);
   krow += (long long)blockIdx.y * nodes * (hm + 1);
   zpart += (long long)blockIdx.y * gridDim.x;
-  for (int r = threadIdx.x; r < m; r += blockDim.x) {
-    float2 a = make_float2(0.0f, 0.0f), a2 = a, bb = a;
-    if (r < nodes) {
-      a = arow[(long long)r * m + c];
-      a2 = arow[(long long)r * m + c2];
-      bb = brow[(long long)r * (hm + 1) + c];
-    }
-    sbuf[sidx(r)] = a;
-    sbuf[sidx(m + r)] = a2;
-    sbuf[sidx(2 * m + r)] = bb;
-    const int dy = r < hm ? r : m - r;
-    sbuf[sidx(3 * m + r)] = dy <= nodes - 1 ? krow[(long long)dy * (hm + 1) + c] : make_float2(0.0f, 0.0f);
-  }
+  // logm >= 4 (M >= 16): the top pass has 1 .. 4 stages above the fused bottom three
+  const int rt = min(4, logm - kColBottom);
+  if (rt == 4) col_load_dif_top<4>(sbuf, arow, brow, krow, c, c2, nodes, logm, tw);
+  else if (rt == 3) col_load_dif_top<3>(sbuf, arow, brow, krow, c, c2, nodes, logm, tw);
+  else if (rt == 2) col_load_dif_top<2>(sbuf, arow, brow, krow, c, c2, nodes, logm, tw);
+  else col_load_dif_top<1>(sbuf, arow, brow, krow, c, c2, nodes, logm, tw);
   __syncthreads();
-  fft_dif(sbuf, 4, logm, tw, false);
+  fft_dif(sbuf, 4, logm, tw, false, logm - rt - 1, kColBottom);
   double zl = 0.0;
-  for (int k = threadIdx.x; k < m; k += blockDim.x) {
-    const float2 kk = sbuf[sidx(3 * m + k)];
-    float2& a = sbuf[sidx(k)];
-    float2& a2 = sbuf[sidx(m + k)];
-    float2& bb = sbuf[sidx(2 * m + k)];
-    zl += ((double)bb.x * bb.x + (double)bb.y * bb.y) * (double)kk.x;
-    a.x *= kk.y;
-    a.y *= kk.y;
-    a2.x *= kk.y;
-    a2.y *= kk.y;
-    bb.x *= kk.y;
-    bb.y *= kk.y;
+  constexpr int E = 1 << kColBottom;
+  for (int g = threadIdx.x; g < (m >> kColBottom); g += blockDim.x) {
+    const int i0 = g << kColBottom;
+    float2 kv[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) kv[e] = sbuf[sidx(3 * m + i0 + e)];
+    dif_regs<kColBottom>(kv, 0, 0, logm, tw, false);
+#pragma unroll
+    for (int seq = 0; seq < 3; ++seq) {
+      float2 v[E];
+#pragma unroll
+      for (int e = 0; e < E; ++e) v[e] = sbuf[sidx(seq * m + i0 + e)];
+      dif_regs<kColBottom>(v, 0, 0, logm, tw, false);
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        if (seq == 2) zl += ((double)v[e].x * v[e].x + (double)v[e].y * v[e].y) * (double)kv[e].x;
+        v[e].x *= kv[e].y;
+        v[e].y *= kv[e].y;
+      }
+      dit_regs<kColBottom>(v, 0, 0, logm, tw, true);
+#pragma unroll
+      for (int e = 0; e < E; ++e) sbuf[sidx(seq * m + i0 + e)] = v[e];
+    }
   }
   __syncthreads();
-  fft_dit(sbuf, 3, logm, tw, true);
-  for (int r = threadIdx.x; r < nodes; r += blockDim.x) {
-    arow[(long long)r * m + c] = sbuf[sidx(r)];
-    if (c2 != c) arow[(long long)r * m + c2] = sbuf[sidx(m + r)];
-    brow[(long long)r * (hm + 1) + c] = sbuf[sidx(2 * m + r)];
-  }
+  fft_dit(sbuf, 3, logm, tw, true, kColBottom, logm - rt);
+  if (rt == 4) col_dit_top_store<4>(sbuf, arow, brow, c, c2, nodes, logm, tw);
+  else if (rt == 3) col_dit_top_store<3>(sbuf, arow, brow, c, c2, nodes, logm, tw);
+  else if (rt == 2) col_dit_top_store<2>(sbuf, arow, brow, c, c2, nodes, logm, tw);
+  else col_dit_top_store<1>(sbuf, arow, brow, c, c2, nodes, logm, tw);
   zl = warp_sum(zl);
   if ((threadIdx.x & 31) == 0) s_z[threadIdx.x >> 5] = zl;
   __syncthreads();

@@ -397,57 +397,77 @@ struct UmapGraph {
   Arena arena;
 };
 
-void umap_build_graph(const int* d_idx, const float* d_dist, int n, int k, int offset, UmapGraph& g, cudaStream_t s) {
-  const long long directed = (long long)n * k;
-  const int nscan = std::max(1, ceil_div(n, 1024));
+// Workspace of the fuzzy-graph build for instances of up to cap_n points with k neighbours. A
+// batch reuses one workspace for every instance, in stream order.
+struct UmapGraphWork {
+  int cap_n = 0, k = 0;
   float *sig = nullptr, *rho = nullptr, *row_max = nullptr, *d_max = nullptr;
   double* acc = nullptr;
   int *counts = nullptr, *ucount = nullptr, *big_rows = nullptr, *big_count = nullptr;
   long long *offs = nullptr, *scan_tmp = nullptr, *out64 = nullptr;
   unsigned long long *cursor = nullptr, *bucket = nullptr;
-  Arena w;
-  w.reserve(&sig, n);
-  w.reserve(&rho, n);
-  w.reserve(&row_max, n);
-  w.reserve(&d_max, 1);
-  w.reserve(&acc, 2);
-  w.reserve(&counts, n);
-  w.reserve(&ucount, n);
-  w.reserve(&big_rows, n);
-  w.reserve(&big_count, 1);
-  w.reserve(&offs, n + 1);
-  w.reserve(&scan_tmp, nscan);
-  w.reserve(&out64, n + 1);
-  w.reserve(&cursor, n);
-  w.reserve(&bucket, 2 * directed);
-  w.commit("UMAP graph workspace");
-  const int grid = std::max(1, std::min(ceil_div(directed, 256), sm_count() * 16));
-  FE_CUDA(cudaMemsetAsync(acc, 0, 2 * sizeof(double), s));
-  FE_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * n, s));
-  FE_CUDA(cudaMemsetAsync(big_count, 0, sizeof(int), s));
-  umap_distance_sum_kernel<<<grid, 256, 0, s>>>(d_dist, directed, acc);
-  FE_LAUNCH("umap_distance_sum_kernel");
-  smooth_knn(d_dist, n, k, acc, sig, rho, s);
-  umap_count_kernel<<<grid, 256, 0, s>>>(d_idx, d_dist, sig, rho, n, k, offset, counts);
-  FE_LAUNCH("umap_count_kernel");
-  exclusive_scan(counts, offs, n, scan_tmp, s);
-  FE_CUDA(cudaMemcpyAsync(cursor, offs, sizeof(long long) * n, cudaMemcpyDeviceToDevice, s));
-  umap_fill_kernel<<<grid, 256, 0, s>>>(d_idx, d_dist, sig, rho, n, k, offset, cursor, bucket);
-  FE_LAUNCH("umap_fill_kernel");
-  const std::size_t smem = kUmapSortCap * sizeof(unsigned long long);
-  FE_CUDA(cudaFuncSetAttribute(umap_union_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  umap_union_rows_kernel<<<std::min(n, sm_count() * 8), kUmapSortThreads, smem, s>>>(bucket, offs, n, ucount, row_max,
-                                                                                     big_rows, big_count);
-  FE_LAUNCH("umap_union_rows_kernel");
-  umap_union_big_rows_kernel<<<sm_count(), 1024, 0, s>>>(bucket, offs, big_rows, big_count, ucount, row_max);
-  FE_LAUNCH("umap_union_big_rows_kernel");
-  exclusive_scan(ucount, out64, n, scan_tmp, s);
-  umap_max_kernel<<<1, 1024, 0, s>>>(row_max, n, d_max);
-  FE_LAUNCH("umap_max_kernel");
+  Arena arena;
+
+  void alloc(int max_n, int kk) {
+    cap_n = max_n;
+    k = kk;
+    const long long directed = (long long)max_n * k;
+    arena.reserve(&sig, max_n);
+    arena.reserve(&rho, max_n);
+    arena.reserve(&row_max, max_n);
+    arena.reserve(&d_max, 1);
+    arena.reserve(&acc, 2);
+    arena.reserve(&counts, max_n);
+    arena.reserve(&ucount, max_n);
+    arena.reserve(&big_rows, max_n);
+    arena.reserve(&big_count, 1);
+    arena.reserve(&offs, max_n + 1);
+    arena.reserve(&scan_tmp, std::max(1, ceil_div(max_n, 1024)));
+    arena.reserve(&out64, max_n + 1);
+    arena.reserve(&cursor, max_n);
+    arena.reserve(&bucket, 2 * directed);
+    arena.commit("UMAP graph workspace");
+  }
+
+  // Enqueues the build of one instance (n <= cap_n) up to its union rows: out64 holds the row
+  // offsets of the union graph (out64[n] = its entry count), d_max its largest weight, and the
+  // rows' entries sit in bucket at offs.
+  void enqueue(const int* d_idx, const float* d_dist, int n, int offset, cudaStream_t s) {
+    const long long directed = (long long)n * k;
+    const int grid = std::max(1, std::min(ceil_div(directed, 256), sm_count() * 16));
+    FE_CUDA(cudaMemsetAsync(acc, 0, 2 * sizeof(double), s));
+    FE_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * n, s));
+    FE_CUDA(cudaMemsetAsync(big_count, 0, sizeof(int), s));
+    umap_distance_sum_kernel<<<grid, 256, 0, s>>>(d_dist, directed, acc);
+    FE_LAUNCH("umap_distance_sum_kernel");
+    smooth_knn(d_dist, n, k, acc, sig, rho, s);
+    umap_count_kernel<<<grid, 256, 0, s>>>(d_idx, d_dist, sig, rho, n, k, offset, counts);
+    FE_LAUNCH("umap_count_kernel");
+    exclusive_scan(counts, offs, n, scan_tmp, s);
+    FE_CUDA(cudaMemcpyAsync(cursor, offs, sizeof(long long) * n, cudaMemcpyDeviceToDevice, s));
+    umap_fill_kernel<<<grid, 256, 0, s>>>(d_idx, d_dist, sig, rho, n, k, offset, cursor, bucket);
+    FE_LAUNCH("umap_fill_kernel");
+    const std::size_t smem = kUmapSortCap * sizeof(unsigned long long);
+    FE_CUDA(cudaFuncSetAttribute(umap_union_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    umap_union_rows_kernel<<<std::min(n, sm_count() * 8), kUmapSortThreads, smem, s>>>(bucket, offs, n, ucount,
+                                                                                       row_max, big_rows, big_count);
+    FE_LAUNCH("umap_union_rows_kernel");
+    umap_union_big_rows_kernel<<<sm_count(), 1024, 0, s>>>(bucket, offs, big_rows, big_count, ucount, row_max);
+    FE_LAUNCH("umap_union_big_rows_kernel");
+    exclusive_scan(ucount, out64, n, scan_tmp, s);
+    umap_max_kernel<<<1, 1024, 0, s>>>(row_max, n, d_max);
+    FE_LAUNCH("umap_max_kernel");
+  }
+};
+
+void umap_build_graph(const int* d_idx, const float* d_dist, int n, int k, int offset, UmapGraph& g, cudaStream_t s) {
+  UmapGraphWork w;
+  w.alloc(n, k);
+  w.enqueue(d_idx, d_dist, n, offset, s);
   long long nnz = 0;
   float mw = 0.0f;
-  FE_CUDA(cudaMemcpyAsync(&nnz, out64 + n, sizeof(long long), cudaMemcpyDeviceToHost, s));
-  FE_CUDA(cudaMemcpyAsync(&mw, d_max, sizeof(float), cudaMemcpyDeviceToHost, s));
+  FE_CUDA(cudaMemcpyAsync(&nnz, w.out64 + n, sizeof(long long), cudaMemcpyDeviceToHost, s));
+  FE_CUDA(cudaMemcpyAsync(&mw, w.d_max, sizeof(float), cudaMemcpyDeviceToHost, s));
   FE_CUDA(cudaStreamSynchronize(s));
   if (nnz <= 0 || !(mw > 0.0f)) throw Error("The CSR graph has no usable UMAP edges.");
   if (nnz > INT_MAX) throw Error("UMAP graph exceeds 2^31 - 1 entries.");
@@ -461,10 +481,43 @@ void umap_build_graph(const int* d_idx, const float* d_dist, int n, int k, int o
   g.arena.reserve(&g.weights, nnz);
   g.arena.reserve(&g.eps, nnz);
   g.arena.commit("UMAP graph");
-  umap_fill_csr_kernel<<<ceil_div((long long)(n + 1) * 32, 256), 256, 0, s>>>(bucket, offs, out64, n, d_max, g.offsets,
-                                                                              g.heads, g.neighbors, g.weights, g.eps);
+  umap_fill_csr_kernel<<<ceil_div((long long)(n + 1) * 32, 256), 256, 0, s>>>(
+      w.bucket, w.offs, w.out64, n, w.d_max, g.offsets, g.heads, g.neighbors, g.weights, g.eps);
   FE_LAUNCH("umap_fill_csr_kernel");
   FE_CUDA(cudaStreamSynchronize(s));
+}
+
+// Batch form of the CSR fill. The instance's first edge is computed on the device from the
+// previous instance's (edge_begin[b + 1] = edge_begin[b] + entries of b), with its largest
+// weight kept for the host's checks, so consecutive instances need no host round trip.
+__global__ void umap_batch_edge_begin_kernel(const long long* __restrict__ entries, const float* __restrict__ max_w,
+                                             long long* __restrict__ edge_begin, float* __restrict__ inst_max) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    edge_begin[1] = edge_begin[0] + *entries;
+    *inst_max = *max_w;
+  }
+}
+
+// One warp per row: the row's union entries written as COO edges shifted by the instance's first
+// vertex v0, with their sampling periods (largest weight / weight, as umap_fill_csr_kernel).
+__global__ void umap_fill_batch_kernel(const unsigned long long* __restrict__ bucket,
+                                       const long long* __restrict__ offs, const long long* __restrict__ out64, int n,
+                                       const float* __restrict__ max_w, const long long* __restrict__ edge_begin,
+                                       int v0, int* __restrict__ heads, int* __restrict__ tails,
+                                       float* __restrict__ period) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  const float mw = *max_w;
+  const long long src = offs[warp], dst = *edge_begin + out64[warp];
+  const int cnt = (int)(out64[warp + 1] - out64[warp]);
+  for (int t = lane; t < cnt; t += 32) {
+    const unsigned long long e = bucket[src + t];
+    const float w = __uint_as_float((unsigned)e);
+    heads[dst + t] = warp + v0;
+    tails[dst + t] = (int)(e >> 32) + v0;
+    period[dst + t] = mw > 0.0f ? mw / fmaxf(w, 1.0e-6f) : INFINITY;
+  }
 }
 
 // ---------------------------------------------------------------- SGD epoch
@@ -800,16 +853,6 @@ struct UmapJob {
   }
 };
 
-// Append one instance's edges to a batch: heads and tails shifted by its first vertex.
-__global__ void umap_offset_edges_kernel(const int* __restrict__ heads, const int* __restrict__ tails,
-                                         long long nnz, int v0, int* __restrict__ heads_out,
-                                         int* __restrict__ tails_out) {
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nnz; e += (long long)gridDim.x * blockDim.x) {
-    heads_out[e] = heads[e] + v0;
-    tails_out[e] = tails[e] + v0;
-  }
-}
-
 // ---------------------------------------------------------------- diffusion start
 // The reference's GPU spectral start (fastembedr_cuda_spectral_init_from_knn,
 // src/embedding_cuda_kernels.cpp:4801-4960; kernels :1178-1335), stated for the CPU by the
@@ -1074,11 +1117,11 @@ int umap_spectral_host(const int* indices, const DistT* distances, int n, int k,
     if (!std::is_same<DistT, float>::value) in.reserve(&d_raw, items);
     in.reserve(&d_dist, items);
     in.commit("fused CUDA UMAP input");
-    FE_CUDA(cudaMemcpyAsync(d_idx, indices, sizeof(int) * items, cudaMemcpyHostToDevice, s));
+    fe::upload(d_idx, indices, sizeof(int) * items, s);
     if constexpr (std::is_same<DistT, float>::value) {
-      FE_CUDA(cudaMemcpyAsync(d_dist, distances, sizeof(float) * items, cudaMemcpyHostToDevice, s));
+      fe::upload(d_dist, distances, sizeof(float) * items, s);
     } else {
-      FE_CUDA(cudaMemcpyAsync(d_raw, distances, sizeof(double) * items, cudaMemcpyHostToDevice, s));
+      fe::upload(d_raw, distances, sizeof(double) * items, s);
       fe::umap_double_to_float_kernel<<<std::max(1, std::min(fe::ceil_div((long long)items, 256),
                                                               fe::sm_count() * 8)),
                                         256, 0, s>>>(d_raw, d_dist, (long long)items);
@@ -1112,9 +1155,9 @@ int fastembedr_cuda_umap_optimize_coo(const int* heads, const int* tails, const 
     in.reserve(&d_t, n_edges_capacity);
     in.reserve(&d_e, n_edges_capacity);
     in.commit("CUDA COO UMAP edges");
-    FE_CUDA(cudaMemcpyAsync(d_h, heads, sizeof(int) * n_edges_capacity, cudaMemcpyHostToDevice, s));
-    FE_CUDA(cudaMemcpyAsync(d_t, tails, sizeof(int) * n_edges_capacity, cudaMemcpyHostToDevice, s));
-    FE_CUDA(cudaMemcpyAsync(d_e, epochs_per_sample, sizeof(float) * n_edges_capacity, cudaMemcpyHostToDevice, s));
+    fe::upload(d_h, heads, sizeof(int) * n_edges_capacity, s);
+    fe::upload(d_t, tails, sizeof(int) * n_edges_capacity, s);
+    fe::upload(d_e, epochs_per_sample, sizeof(float) * n_edges_capacity, s);
     FE_CUDA(cudaMemcpyAsync(job.y, init, sizeof(float) * 2 * n, cudaMemcpyHostToDevice, s));
     const fe::UmapParams p{n, n_epochs, negative_sample_rate, seed, learning_rate, a, b, repulsion_strength};
     job.run(d_h, d_t, d_e, n_edges_capacity, p);
@@ -1137,8 +1180,8 @@ int fastembedr_cuda_umap_graph_from_knn(const int* indices, const float* distanc
     a.reserve(&d_idx, items);
     a.reserve(&d_dist, items);
     a.commit("UMAP graph input");
-    FE_CUDA(cudaMemcpyAsync(d_idx, indices, sizeof(int) * items, cudaMemcpyHostToDevice, st.s));
-    FE_CUDA(cudaMemcpyAsync(d_dist, distances, sizeof(float) * items, cudaMemcpyHostToDevice, st.s));
+    fe::upload(d_idx, indices, sizeof(int) * items, st.s);
+    fe::upload(d_dist, distances, sizeof(float) * items, st.s);
     fe::validate_knn(d_idx, d_dist, n, k, index_offset, st.s);
     fe::UmapGraph g;
     fe::umap_build_graph(d_idx, d_dist, n, k, index_offset, g, st.s);
@@ -1173,8 +1216,8 @@ int fastembedr_cuda_umap_from_knn_profile(const int* indices, const float* dista
     a.reserve(&d_idx, items);
     a.reserve(&d_dist, items);
     a.commit("UMAP input");
-    FE_CUDA(cudaMemcpyAsync(d_idx, indices, sizeof(int) * items, cudaMemcpyHostToDevice, s));
-    FE_CUDA(cudaMemcpyAsync(d_dist, distances, sizeof(float) * items, cudaMemcpyHostToDevice, s));
+    fe::upload(d_idx, indices, sizeof(int) * items, s);
+    fe::upload(d_dist, distances, sizeof(float) * items, s);
     FE_CUDA(cudaMemcpyAsync(job.y, init, sizeof(float) * 2 * n, cudaMemcpyHostToDevice, s));
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     const bool timed = graph_ms || sgd_ms;
@@ -1246,10 +1289,30 @@ void umap_batch_job(int n_instances, const int* sizes, const std::vector<const i
   UmapJob job;
   job.alloc(n);
   cudaStream_t s = job.stream.s;
-  // one fuzzy graph per instance, then appended with vertex offsets
-  std::vector<std::unique_ptr<UmapGraph>> graphs(n_instances);
-  std::vector<long long> eb(n_instances + 1, 0);
+  long long n_edges = 0;
+  // Every instance's fuzzy graph is built in one reused workspace and written straight into the
+  // batch's edge list at a first edge the device computes; the host reads the checks of all
+  // instances back once, after the last build. An instance's union graph has at most twice as
+  // many entries as it has directed edges.
+  const long long cap_edges = std::max(2LL * n * k, 1LL);
+  int *heads = nullptr, *tails = nullptr, *d_vb = nullptr;
+  float *period = nullptr, *inst_max = nullptr;
+  long long* d_eb = nullptr;
+  unsigned* flags = nullptr;
+  Arena ga;
+  ga.reserve(&heads, (std::size_t)cap_edges);
+  ga.reserve(&tails, (std::size_t)cap_edges);
+  ga.reserve(&period, (std::size_t)cap_edges);
+  ga.reserve(&d_eb, n_instances + 1);
+  ga.reserve(&d_vb, n_instances + 1);
+  ga.reserve(&inst_max, n_instances);
+  ga.reserve(&flags, 1);
+  ga.commit("UMAP batch graph");
+  FE_CUDA(cudaMemsetAsync(d_eb, 0, sizeof(long long), s));
+  FE_CUDA(cudaMemsetAsync(flags, 0, sizeof(unsigned), s));
   {
+    UmapGraphWork w;
+    w.alloc(max_n, k);
     int *d_idx = nullptr, *d_irm = nullptr;
     float *d_dist = nullptr, *d_drm = nullptr;
     Arena in;
@@ -1261,49 +1324,46 @@ void umap_batch_job(int n_instances, const int* sizes, const std::vector<const i
     }
     in.commit("UMAP batch input");
     for (int b = 0; b < n_instances; ++b) {
-      const std::size_t items = (std::size_t)sizes[b] * k;
+      const int nb = sizes[b];
+      const std::size_t items = (std::size_t)nb * k;
       if (row_major) {
-        FE_CUDA(cudaMemcpyAsync(d_irm, idx_u[b], sizeof(int) * items, cudaMemcpyHostToDevice, s));
-        FE_CUDA(cudaMemcpyAsync(d_drm, dist_u[b], sizeof(float) * items, cudaMemcpyHostToDevice, s));
+        fe::upload(d_irm, idx_u[b], sizeof(int) * items, s);
+        fe::upload(d_drm, dist_u[b], sizeof(float) * items, s);
         umap_rows_to_cols_kernel<<<std::max(1, std::min(ceil_div((long long)items, 256), sm_count() * 8)), 256, 0,
-                                   s>>>(d_irm, d_drm, sizes[b], k, d_idx, d_dist);
+                                   s>>>(d_irm, d_drm, nb, k, d_idx, d_dist);
         FE_LAUNCH("umap_rows_to_cols_kernel");
       } else {
-        FE_CUDA(cudaMemcpyAsync(d_idx, idx_u[b], sizeof(int) * items, cudaMemcpyHostToDevice, s));
-        FE_CUDA(cudaMemcpyAsync(d_dist, dist_u[b], sizeof(float) * items, cudaMemcpyHostToDevice, s));
+        fe::upload(d_idx, idx_u[b], sizeof(int) * items, s);
+        fe::upload(d_dist, dist_u[b], sizeof(float) * items, s);
       }
-      validate_knn(d_idx, d_dist, sizes[b], k, index_offset, s);
-      graphs[b] = std::make_unique<UmapGraph>();
-      umap_build_graph(d_idx, d_dist, sizes[b], k, index_offset, *graphs[b], s);
-      eb[b + 1] = eb[b] + graphs[b]->nnz;
+      validate_knn_async(d_idx, d_dist, nb, k, index_offset, flags, s);
+      w.enqueue(d_idx, d_dist, nb, index_offset, s);
+      umap_batch_edge_begin_kernel<<<1, 32, 0, s>>>(w.out64 + nb, w.d_max, d_eb + b, inst_max + b);
+      FE_LAUNCH("umap_batch_edge_begin_kernel");
+      umap_fill_batch_kernel<<<ceil_div((long long)nb * 32, 256), 256, 0, s>>>(
+          w.bucket, w.offs, w.out64, nb, w.d_max, d_eb + b, vb[b], heads, tails, period);
+      FE_LAUNCH("umap_fill_batch_kernel");
     }
+    std::vector<long long> eb(n_instances + 1, 0);
+    std::vector<float> mx(n_instances, 0.0f);
+    unsigned hflags = 0u;
+    FE_CUDA(cudaMemcpyAsync(eb.data(), d_eb, sizeof(long long) * eb.size(), cudaMemcpyDeviceToHost, s));
+    FE_CUDA(cudaMemcpyAsync(mx.data(), inst_max, sizeof(float) * mx.size(), cudaMemcpyDeviceToHost, s));
+    FE_CUDA(cudaMemcpyAsync(&hflags, flags, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    FE_CUDA(cudaStreamSynchronize(s));
+    knn_flags_check(hflags);
+    for (int b = 0; b < n_instances; ++b) {
+      const long long nnz = eb[b + 1] - eb[b];
+      if (nnz <= 0 || !(mx[b] > 0.0f)) throw Error("The CSR graph has no usable UMAP edges.");
+      if (nnz > INT_MAX) throw Error("UMAP graph exceeds 2^31 - 1 entries.");
+    }
+    n_edges = eb[n_instances];
   }
-  const long long n_edges = eb[n_instances];
-  int *heads = nullptr, *tails = nullptr, *d_vb = nullptr;
-  float* period = nullptr;
-  long long* d_eb = nullptr;
-  Arena ga;
-  ga.reserve(&heads, (std::size_t)std::max<long long>(n_edges, 1));
-  ga.reserve(&tails, (std::size_t)std::max<long long>(n_edges, 1));
-  ga.reserve(&period, (std::size_t)std::max<long long>(n_edges, 1));
-  ga.reserve(&d_eb, n_instances + 1);
-  ga.reserve(&d_vb, n_instances + 1);
-  ga.commit("UMAP batch graph");
-  for (int b = 0; b < n_instances; ++b) {
-    const UmapGraph& g = *graphs[b];
-    const int blocks = std::max(1, std::min(ceil_div(g.nnz, 256), sm_count() * 8));
-    umap_offset_edges_kernel<<<blocks, 256, 0, s>>>(g.heads, g.neighbors, g.nnz, vb[b], heads + eb[b],
-                                                    tails + eb[b]);
-    FE_LAUNCH("umap_offset_edges_kernel");
-    FE_CUDA(cudaMemcpyAsync(period + eb[b], g.eps, sizeof(float) * g.nnz, cudaMemcpyDeviceToDevice, s));
-  }
-  FE_CUDA(cudaMemcpyAsync(d_eb, eb.data(), sizeof(long long) * eb.size(), cudaMemcpyHostToDevice, s));
   FE_CUDA(cudaMemcpyAsync(d_vb, vb.data(), sizeof(int) * vb.size(), cudaMemcpyHostToDevice, s));
   for (int b = 0; b < n_instances; ++b)
     FE_CUDA(cudaMemcpyAsync(job.y + vb[b], init_u[b], sizeof(float) * 2 * (std::size_t)sizes[b],
                             cudaMemcpyHostToDevice, s));
   FE_CUDA(cudaStreamSynchronize(s));
-  graphs.clear();
   double av = 0.0, bv = 0.0;
   umap_ab_params(1.0, min_dist, &av, &bv);
   const UmapParams p{n, n_epochs, negative_sample_rate, seed, learning_rate, (float)av, (float)bv,
@@ -1393,8 +1453,8 @@ int fastembedr_cuda_umap_spectral_init_from_knn(const int* indices, const float*
     a.reserve(&d_idx, items);
     a.reserve(&d_dist, items);
     a.commit("UMAP spectral start input");
-    FE_CUDA(cudaMemcpyAsync(d_idx, indices, sizeof(int) * items, cudaMemcpyHostToDevice, st.s));
-    FE_CUDA(cudaMemcpyAsync(d_dist, distances, sizeof(float) * items, cudaMemcpyHostToDevice, st.s));
+    fe::upload(d_idx, indices, sizeof(int) * items, st.s);
+    fe::upload(d_dist, distances, sizeof(float) * items, st.s);
     FE_CUDA(cudaStreamSynchronize(st.s));
     fe::umap_knn_spectral_job(d_idx, d_dist, n, k, index_offset, 0, 0, 1.0f, 0.01f, 1.0f, spectral_n_iter,
                               init_scale, (unsigned)seed, out, nullptr, &draws);
@@ -1452,8 +1512,8 @@ int fastembedr_cuda_umap_spectral_init_csr(const int* offsets, const int* neighb
     a.commit("UMAP spectral start (CSR)");
     FE_CUDA(cudaMemcpyAsync(d_off, offsets, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s));
     if (nnz > 0) {
-      FE_CUDA(cudaMemcpyAsync(d_nb, nb0.data(), sizeof(int) * nnz, cudaMemcpyHostToDevice, s));
-      FE_CUDA(cudaMemcpyAsync(d_w, weights, sizeof(float) * nnz, cudaMemcpyHostToDevice, s));
+      fe::upload(d_nb, nb0.data(), sizeof(int) * nnz, s);
+      fe::upload(d_w, weights, sizeof(float) * nnz, s);
     }
     fe::umap_spectral_start(d_off, d_nb, d_w, n, nnz, spectral_n_iter, init_scale, seed, d_out, s);
     FE_CUDA(cudaMemcpyAsync(out, d_out, sizeof(double) * 2 * (std::size_t)n, cudaMemcpyDeviceToHost, s));
@@ -1479,8 +1539,8 @@ int fastembedr_cuda_umap_knn_spectral(const int* indices, const float* distances
     a.reserve(&d_idx, items);
     a.reserve(&d_dist, items);
     a.commit("UMAP input");
-    FE_CUDA(cudaMemcpyAsync(d_idx, indices, sizeof(int) * items, cudaMemcpyHostToDevice, st.s));
-    FE_CUDA(cudaMemcpyAsync(d_dist, distances, sizeof(float) * items, cudaMemcpyHostToDevice, st.s));
+    fe::upload(d_idx, indices, sizeof(int) * items, st.s);
+    fe::upload(d_dist, distances, sizeof(float) * items, st.s);
     FE_CUDA(cudaStreamSynchronize(st.s));
     fe::umap_knn_spectral_job(d_idx, d_dist, n, k, index_offset, n_epochs, negative_sample_rate, learning_rate,
                               min_dist, repulsion_strength, spectral_n_iter, init_scale, seed, nullptr, out, &draws);
@@ -1506,8 +1566,8 @@ int fastembedr_cuda_spectral_init_from_knn(const int* indices, const double* dis
     a.reserve(&d_dist, items);
     a.reserve(&d_y, n);
     a.commit("CUDA spectral initialization");
-    FE_CUDA(cudaMemcpyAsync(d_idx, indices, sizeof(int) * items, cudaMemcpyHostToDevice, s));
-    FE_CUDA(cudaMemcpyAsync(d_dd, distances, sizeof(double) * items, cudaMemcpyHostToDevice, s));
+    fe::upload(d_idx, indices, sizeof(int) * items, s);
+    fe::upload(d_dd, distances, sizeof(double) * items, s);
     fe::umap_double_to_float_kernel<<<std::max(1, std::min(fe::ceil_div((long long)items, 256), fe::sm_count() * 8)),
                                       256, 0, s>>>(d_dd, d_dist, (long long)items);
     FE_LAUNCH("umap_double_to_float_kernel");

@@ -136,3 +136,13 @@ def test_invalid_batches_raise():
     oob[0, 0] = 5000
     with pytest.raises(_lib.CudaEmbeddingError, match="out of range"):
         api.TsneBatch([(oob, dist)])
+    # a bad instance after a good one fails the whole batch (checked once, before P is built)
+    with pytest.raises(_lib.CudaEmbeddingError, match="out of range"):
+        api.TsneBatch([knns[1], (oob, dist)])
+    neg = dist.copy()
+    neg[3, 2] = -1.0
+    with pytest.raises(_lib.CudaEmbeddingError, match="finite and non-negative"):
+        api.TsneBatch([knns[1], (idx, neg)])
+    with api.TsneBatch(knns) as b:
+        b.iterate(5, 12.0, 1.0 / 12.0)
+        assert all(np.all(np.isfinite(y)) for y in b.layouts())
