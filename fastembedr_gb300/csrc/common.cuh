@@ -104,7 +104,7 @@ int sm_count();
 // pinned-copy speed rather than through the driver's pageable path. The source may be reused
 // when the call returns. Smaller copies, and copies from pinned memory, are plain
 // cudaMemcpyAsync calls.
-constexpr std::size_t kStagedUploadMin = std::size_t(8) << 20;
+constexpr std::size_t kStagedUploadMin = std::size_t(1) << 20;
 void upload(void* dst, const void* src, std::size_t bytes, cudaStream_t s);
 
 // ---------------------------------------------------------------- device helpers

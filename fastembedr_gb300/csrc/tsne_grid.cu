@@ -516,13 +516,105 @@ __device__ void fft_dif(float2* buf, int count, int logm, const float2* __restri
 __device__ __forceinline__ int bitrev(int f, int logm) { return (int)(__brev((unsigned)f) >> (32 - logm)); }
 __device__ __forceinline__ float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
 
+// The row pass's top forward pass (stages logm - 1 .. logm - kRowTop) runs on values loaded or
+// computed straight into registers rather than staged in shared memory first; the butterflies
+// are those of dif_pass.
+constexpr int kRowTop = 3;
+
+// Charge rows: the fixed-point charges of nodes j + e h of rows r1 (c1) and r2 (c2) are read,
+// cleared for the next scatter and converted, then transformed as A_r1, A_r2 and m_r1 + i m_r2.
+template <int R>
+__device__ __forceinline__ void rows_charges_dif_top(float2* sbuf, longlong2* __restrict__ c1,
+                                                     longlong2* __restrict__ c2, bool has2, int nodes, float inv_q,
+                                                     int logm, const float2* __restrict__ tw) {
+  constexpr int E = 1 << R;
+  const int m = 1 << logm, s = logm - R, h = 1 << s;
+  for (int j = threadIdx.x; j < h; j += blockDim.x) {
+    float2 a[E];
+    float mx[E], my[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const int c = j + e * h;
+      a[e] = make_float2(0.0f, 0.0f);
+      mx[e] = 0.0f;
+      if (c < nodes) {
+        const longlong2 p0 = c1[2 * c], p1 = c1[2 * c + 1];
+        c1[2 * c] = make_longlong2(0, 0);
+        c1[2 * c + 1] = make_longlong2(0, 0);
+        a[e] = make_float2((float)p0.y * inv_q, (float)p1.x * inv_q);
+        mx[e] = (float)p0.x * inv_q;
+      }
+    }
+    dif_regs<R>(a, j, s, logm, tw, false);
+#pragma unroll
+    for (int e = 0; e < E; ++e) sbuf[sidx(j + e * h)] = a[e];
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const int c = j + e * h;
+      a[e] = make_float2(0.0f, 0.0f);
+      my[e] = 0.0f;
+      if (has2 && c < nodes) {
+        const longlong2 p0 = c2[2 * c], p1 = c2[2 * c + 1];
+        c2[2 * c] = make_longlong2(0, 0);
+        c2[2 * c + 1] = make_longlong2(0, 0);
+        a[e] = make_float2((float)p0.y * inv_q, (float)p1.x * inv_q);
+        my[e] = (float)p0.x * inv_q;
+      }
+    }
+    dif_regs<R>(a, j, s, logm, tw, false);
+#pragma unroll
+    for (int e = 0; e < E; ++e) sbuf[sidx(m + j + e * h)] = a[e];
+#pragma unroll
+    for (int e = 0; e < E; ++e) a[e] = make_float2(mx[e], my[e]);
+    dif_regs<R>(a, j, s, logm, tw, false);
+#pragma unroll
+    for (int e = 0; e < E; ++e) sbuf[sidx(2 * m + j + e * h)] = a[e];
+  }
+}
+
+// Kernel rows dy1 and dy2 (offsets yo1, yo2): (q, q^2) of columns j + e h, q = 1 / (1 + d^2),
+// zero beyond +-(nodes - 1) columns.
+template <int R>
+__device__ __forceinline__ void rows_kernel_dif_top(float2* sbuf, int nodes, float h_node, float yo1, float yo2,
+                                                    int logm, const float2* __restrict__ tw) {
+  constexpr int E = 1 << R;
+  const int m = 1 << logm, hm = m >> 1, s = logm - R, h = 1 << s;
+  for (int j = threadIdx.x; j < h; j += blockDim.x) {
+    float2 v1[E], v2[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const int c = j + e * h;
+      const int dx = c < hm ? c : c - m;
+      v1[e] = make_float2(0.0f, 0.0f);
+      v2[e] = v1[e];
+      if (dx <= nodes - 1 && dx >= -(nodes - 1)) {
+        const float xo = (float)dx * h_node;
+        const float q1 = 1.0f / (1.0f + (xo * xo + yo1 * yo1));
+        const float q2 = 1.0f / (1.0f + (xo * xo + yo2 * yo2));
+        v1[e] = make_float2(q1, q1 * q1);
+        v2[e] = make_float2(q2, q2 * q2);
+      }
+    }
+    dif_regs<R>(v1, j, s, logm, tw, false);
+    dif_regs<R>(v2, j, s, logm, tw, false);
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      sbuf[sidx(j + e * h)] = v1[e];
+      sbuf[sidx(m + j + e * h)] = v2[e];
+    }
+  }
+}
+
 // Row pass. Blocks [0, npairs): charge rows r1 = p and r2 = p + npairs (r2 < nodes or absent):
 // forward FFTs of A_r1, A_r2 and m_r1 + i m_r2; A spectra to arow (natural order, all M),
 // separated B half spectra to brow (f = 0 .. M/2); the charge rows are cleared for the next
 // scatter. Blocks [npairs, 2 npairs): kernel rows dy1 = p and dy2 = p + npairs -> forward FFTs of
 // (q + i q^2), f = 0 .. M/2 kept. blockIdx.y selects the instance members[blockIdx.y] of the grid
 // class.
-__global__ void __launch_bounds__(kFftThreads)
+#ifndef FE_ROW_MIN_BLOCKS
+#define FE_ROW_MIN_BLOCKS 4
+#endif
+__global__ void __launch_bounds__(kFftThreads, FE_ROW_MIN_BLOCKS)
 rows_forward_kernel(const TsneInstance* __restrict__ inst, const int* __restrict__ members, int grid, int nodes,
                     int logm, const float2* __restrict__ tw, const GridState* __restrict__ cur,
                     float2* __restrict__ arow, float2* __restrict__ brow, float2* __restrict__ krow) {
@@ -541,28 +633,9 @@ rows_forward_kernel(const TsneInstance* __restrict__ inst, const int* __restrict
     const float inv_q = cur->inv_qscale;
     longlong2* c1 = reinterpret_cast<longlong2*>(charges + (long long)r1 * grid * kChargeStride);
     longlong2* c2 = reinterpret_cast<longlong2*>(charges + (long long)(has2 ? r2 : r1) * grid * kChargeStride);
-    for (int c = threadIdx.x; c < m; c += blockDim.x) {
-      float2 a1 = make_float2(0.0f, 0.0f), a2 = a1, mm = a1;
-      if (c < nodes) {
-        const longlong2 p0 = c1[2 * c], p1 = c1[2 * c + 1];
-        c1[2 * c] = make_longlong2(0, 0);
-        c1[2 * c + 1] = make_longlong2(0, 0);
-        a1 = make_float2((float)p0.y * inv_q, (float)p1.x * inv_q);
-        mm.x = (float)p0.x * inv_q;
-        if (has2) {
-          const longlong2 s0 = c2[2 * c], s1 = c2[2 * c + 1];
-          c2[2 * c] = make_longlong2(0, 0);
-          c2[2 * c + 1] = make_longlong2(0, 0);
-          a2 = make_float2((float)s0.y * inv_q, (float)s1.x * inv_q);
-          mm.y = (float)s0.x * inv_q;
-        }
-      }
-      sbuf[sidx(c)] = a1;
-      sbuf[sidx(m + c)] = a2;
-      sbuf[sidx(2 * m + c)] = mm;
-    }
+    rows_charges_dif_top<kRowTop>(sbuf, c1, c2, has2, nodes, inv_q, logm, tw);
     __syncthreads();
-    fft_dif<3>(sbuf, 3, logm, tw, false);
+    fft_dif<3>(sbuf, 3, logm, tw, false, logm - kRowTop - 1, 0);
     float2* o1 = arow + (long long)r1 * m;
     float2* o2 = arow + (long long)r2 * m;
     for (int f = threadIdx.x; f < m; f += blockDim.x) {
@@ -583,21 +656,9 @@ rows_forward_kernel(const TsneInstance* __restrict__ inst, const int* __restrict
     const bool has2 = k2 < nodes;
     const float h = cur->h;
     const float yo1 = (float)k1 * h, yo2 = (float)k2 * h;
-    for (int c = threadIdx.x; c < m; c += blockDim.x) {
-      const int dx = c < hm ? c : c - m;
-      float2 v1 = make_float2(0.0f, 0.0f), v2 = v1;
-      if (dx <= nodes - 1 && dx >= -(nodes - 1)) {
-        const float xo = (float)dx * h;
-        const float q1 = 1.0f / (1.0f + (xo * xo + yo1 * yo1));
-        const float q2 = 1.0f / (1.0f + (xo * xo + yo2 * yo2));
-        v1 = make_float2(q1, q1 * q1);
-        v2 = make_float2(q2, q2 * q2);
-      }
-      sbuf[sidx(c)] = v1;
-      sbuf[sidx(m + c)] = v2;
-    }
+    rows_kernel_dif_top<kRowTop>(sbuf, nodes, h, yo1, yo2, logm, tw);
     __syncthreads();
-    fft_dif<3>(sbuf, 2, logm, tw, false);
+    fft_dif<3>(sbuf, 2, logm, tw, false, logm - kRowTop - 1, 0);
     float2* o1 = krow + (long long)k1 * (hm + 1);
     float2* o2 = krow + (long long)k2 * (hm + 1);
     for (int f = threadIdx.x; f <= hm; f += blockDim.x) {
