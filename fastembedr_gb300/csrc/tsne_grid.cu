@@ -33,8 +33,8 @@ namespace fe {
 
 constexpr int kStepThreads = 256;
 constexpr int kFftThreads = 256;
-constexpr int kColThreads = 256;  // the column pass holds 104 KB of shared memory: 2 blocks per SM;
-                                  // 256 threads take its 3 x 256 radix-16 work items in 3 rounds
+constexpr int kColThreads = 256;  // the column pass holds 4 x M complex values of shared memory
+                                  // (70 KB at M = 2048: 3 blocks per SM)
 
 // ---------------------------------------------------------------- stencils
 template <int TAPS>
