@@ -138,6 +138,10 @@ def ref() -> C.CDLL:
         lib.ref_umap_spectral_init.argtypes = [i32p, i32p, f64p, I, L, I, D, I, f64p]
         lib.ref_umap_spectral_knn.restype = I
         lib.ref_umap_spectral_knn.argtypes = [i32p, f64p, I, I, I, I, f64p]
+        lib.ref_knn_structure_score.restype = I
+        lib.ref_knn_structure_score.argtypes = [f64p, I, i32p, I, i32p, I, I, f64p]
+        lib.ref_project_affine.restype = I
+        lib.ref_project_affine.argtypes = [f64p, I, f64p, I, I, f64p, i32p, f64p, I, I, D, D, f64p, f64p, i32p]
         _REF = lib
     return _REF
 

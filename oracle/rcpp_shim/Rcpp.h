@@ -1,7 +1,9 @@
 // Test-only stand-in for the small part of the Rcpp API that fastEmbedR's CPU cores
-// (src/tsne_neighbors.cpp, src/fast_knn_umap.cpp) use, so that those files compile
-// unchanged into the CPU reference library under oracle/_ref. R is not needed: a SEXP
-// here is a tagged, reference-counted numeric/integer vector or matrix (column-major).
+// (src/tsne_neighbors.cpp, src/fast_knn_umap.cpp, src/embedding_utils.cpp) use, so that those
+// files compile unchanged into the CPU reference library under oracle/_ref. R-level objects
+// the bridge never reads (S4 payloads, R function calls, named list access) only compile.
+// R is not needed: a SEXP here is a tagged, reference-counted numeric/integer vector or matrix
+// (column-major).
 // Written for this project; it shares only names and call signatures with Rcpp.
 #ifndef FASTEMBEDR_TEST_RCPP_SHIM_H
 #define FASTEMBEDR_TEST_RCPP_SHIM_H
@@ -37,8 +39,10 @@ typedef SEXPREC* SEXP;
 static const int NA_INTEGER = INT_MIN;
 static const double NA_REAL = std::numeric_limits<double>::quiet_NaN();
 static const double R_NaReal = std::numeric_limits<double>::quiet_NaN();
+static const double R_NaN = std::numeric_limits<double>::quiet_NaN();
 static SEXPREC shim_dim_symbol_storage;
 static const SEXP R_DimSymbol = &shim_dim_symbol_storage;
+static const SEXP R_NilValue = nullptr;
 
 inline int TYPEOF(SEXP x) { return x == nullptr ? NILSXP : x->type; }
 inline bool Rf_isNull(SEXP x) { return x == nullptr || x->type == NILSXP; }
@@ -48,6 +52,11 @@ inline bool Rf_isMatrix(SEXP x) { return x != nullptr && x->nrow >= 0 && x->ncol
 inline SEXP Rf_getAttrib(SEXP x, SEXP) { return Rf_isMatrix(x) ? x : nullptr; }
 inline int* INTEGER(SEXP x) { return x->ints.data(); }
 inline double* REAL(SEXP x) { return x->dbl.data(); }
+inline R_xlen_t Rf_xlength(SEXP x) {
+  if (x == nullptr) return 0;
+  return static_cast<R_xlen_t>(x->type == REALSXP ? x->dbl.size() : x->ints.size());
+}
+inline int Rf_length(SEXP x) { return static_cast<int>(Rf_xlength(x)); }
 
 namespace Rcpp {
 
@@ -71,6 +80,39 @@ inline void warning(const std::string&) {}
 inline void checkUserInterrupt() {}
 static std::ostream& Rcout = std::cout;
 
+struct NamedArg {
+  std::string name;
+  std::any value;
+};
+
+// Element of a create() call: a plain value, or the value of a Named(...) = value argument
+// (names are not kept).
+template <typename T, typename A>
+T shim_item(const A& a) {
+  return static_cast<T>(a);
+}
+template <typename T>
+T shim_item(const NamedArg& a) {
+  if (auto p = std::any_cast<double>(&a.value)) return static_cast<T>(*p);
+  if (auto p = std::any_cast<int>(&a.value)) return static_cast<T>(*p);
+  if (auto p = std::any_cast<float>(&a.value)) return static_cast<T>(*p);
+  if (auto p = std::any_cast<bool>(&a.value)) return static_cast<T>(*p);
+  throw std::runtime_error("shim: unsupported named element " + a.name);
+}
+
+// Stand-in for any R object the test bridge never reads (results of R calls, S4 slots, list
+// elements by name): assignments are dropped and reading it throws.
+struct ShimOpaque {
+  template <typename T>
+  ShimOpaque& operator=(const T&) {
+    return *this;
+  }
+  template <typename T>
+  operator T() const {
+    throw std::runtime_error("shim: R objects are not available");
+  }
+};
+
 template <int RTYPE, typename T>
 class VectorBase {
  public:
@@ -80,6 +122,8 @@ class VectorBase {
   VectorBase() : p_(std::make_shared<SEXPREC>()) { p_->type = RTYPE; }
   template <typename I, typename = typename std::enable_if<std::is_integral<I>::value>::type>
   VectorBase(I n) : VectorBase() { store().assign(static_cast<std::size_t>(n), T()); }
+  template <typename I, typename = typename std::enable_if<std::is_integral<I>::value>::type>
+  VectorBase(I n, const T& fill) : VectorBase() { store().assign(static_cast<std::size_t>(n), fill); }
   VectorBase(SEXP x) {
     if (x == nullptr || x->type != RTYPE) throw std::runtime_error("shim: SEXP type mismatch");
     p_ = x->shared_from_this();
@@ -91,7 +135,7 @@ class VectorBase {
   template <typename... Args>
   static VectorBase create(Args... args) {
     VectorBase out;
-    (out.store().push_back(static_cast<T>(args)), ...);
+    (out.store().push_back(shim_item<T>(args)), ...);
     return out;
   }
   operator SEXP() const { return p_.get(); }
@@ -147,11 +191,6 @@ typedef VectorBase<INTSXP, int> IntegerVector;
 typedef MatrixBase<REALSXP, double> NumericMatrix;
 typedef MatrixBase<INTSXP, int> IntegerMatrix;
 
-struct NamedArg {
-  std::string name;
-  std::any value;
-};
-
 struct Named {
   explicit Named(const std::string& n) : name(n) {}
   template <typename T>
@@ -180,6 +219,7 @@ class List {
       if (it.name == n) return it.value;
     throw std::runtime_error("shim: list element not found: " + n);
   }
+  ShimOpaque operator[](const char*) { return ShimOpaque(); }
 
  private:
   std::vector<NamedArg> items_;
@@ -188,9 +228,44 @@ class List {
 class S4 {
  public:
   explicit S4(SEXP) {}
+  explicit S4(const char*) {}
   bool is(const char*) const { return false; }
-  SEXP slot(const char*) const { throw std::runtime_error("shim: S4 slots are not available"); }
+  ShimOpaque slot(const char*) const { return ShimOpaque(); }
+  operator SEXP() const { throw std::runtime_error("shim: S4 objects are not available"); }
 };
+
+// R-level calls (base::qr, base::svd, ...) are not available; only their call syntax compiles.
+class Function {
+ public:
+  Function() = default;
+  template <typename... Args>
+  ShimOpaque operator()(Args...) const {
+    throw std::runtime_error("shim: R functions are not available");
+  }
+};
+
+class Environment {
+ public:
+  static Environment base_env() { return Environment(); }
+  Function operator[](const char*) const { return Function(); }
+};
+
+template <typename T, typename X>
+T as(const X&) {
+  throw std::runtime_error("shim: Rcpp::as is not available");
+}
+
+struct CharacterVector {
+  template <typename... Args>
+  static CharacterVector create(Args...) {
+    return CharacterVector();
+  }
+};
+
+template <typename M>
+ShimOpaque colnames(M&) {
+  return ShimOpaque();
+}
 
 inline IntegerVector wrap(const std::vector<int>& v) { return IntegerVector(v.begin(), v.end()); }
 inline NumericVector wrap(const std::vector<float>& v) { return NumericVector(v.begin(), v.end()); }

@@ -1,6 +1,6 @@
 // C entry points over the reference's own exported CPU functions (fastEmbedR
-// src/tsne_neighbors.cpp and src/fast_knn_umap.cpp, compiled unchanged against the
-// test-only Rcpp shim). TEST INFRASTRUCTURE ONLY: used to generate golden vectors and
+// src/tsne_neighbors.cpp, src/fast_knn_umap.cpp and src/embedding_utils.cpp, compiled
+// unchanged against the test-only Rcpp shim). TEST INFRASTRUCTURE ONLY: used to generate golden vectors and
 // to pin the plain-C oracle; never part of the product library.
 #include <Rcpp.h>
 
@@ -33,6 +33,10 @@ NumericMatrix fast_knn_umap_csr_cpp(IntegerVector, IntegerVector, SEXP, int, int
                                     int, double, int, bool);
 NumericMatrix fast_knn_umap_range_cpp(IntegerMatrix, NumericMatrix, int, int, int, int, double, int, double, double,
                                       int, int, double, int, bool);
+// src/embedding_utils.cpp:1386, :2120
+NumericVector knn_structure_score_cpp(NumericMatrix, IntegerMatrix, IntegerVector, int, IntegerVector, int);
+List project_embedding_affine_cpp(NumericMatrix, NumericMatrix, NumericMatrix, IntegerMatrix, NumericMatrix, int,
+                                  double, double);
 
 namespace {
 thread_local std::string last_error;
@@ -245,6 +249,47 @@ int ref_umap_spectral_knn(const int* idx, const double* dist, int n, int k, int 
       out[2 * i] = r(i, 0);
       out[2 * i + 1] = r(i, 1);
     }
+    return 0;
+  } catch (const std::exception& e) {
+    last_error = e.what();
+    return 1;
+  }
+}
+
+// knn_structure_score_cpp: layout n x 2, high-dimensional KNN n x k (1-based), keep (1-based rows),
+// no labels. out: preservation, trustworthiness, continuity, structure score (4 values).
+int ref_knn_structure_score(const double* layout, int n, const int* idx, int k, const int* keep, int n_keep,
+                            int preserve_k, double* out) {
+  try {
+    IntegerVector kv(n_keep);
+    std::copy(keep, keep + n_keep, kv.begin());
+    NumericVector r = knn_structure_score_cpp(num_matrix(layout, n, 2), int_matrix(idx, n, k), kv, preserve_k,
+                                              IntegerVector(0), 0);
+    for (int i = 0; i < 4; ++i) out[i] = r[i];
+    return 0;
+  } catch (const std::exception& e) {
+    last_error = e.what();
+    return 1;
+  }
+}
+
+// project_embedding_affine_cpp: reference data n_ref x f, query data n_query x f, reference
+// layout n_ref x 2, projection KNN n_query x k (1-based) with distances. out_layout n_query x 2;
+// fallback per query (1 where the weighted mean was used).
+int ref_project_affine(const double* ref_data, int n_ref, const double* query_data, int n_query, int n_features,
+                       const double* ref_layout, const int* idx, const double* dist, int k, int max_neighbors,
+                       double ridge, double max_extrapolation, double* out_layout, double* confidence,
+                       int* fallback) {
+  try {
+    List r = project_embedding_affine_cpp(num_matrix(ref_data, n_ref, n_features),
+                                          num_matrix(query_data, n_query, n_features), num_matrix(ref_layout, n_ref, 2),
+                                          int_matrix(idx, n_query, k), num_matrix(dist, n_query, k), max_neighbors,
+                                          ridge, max_extrapolation);
+    copy_out(get<NumericMatrix>(r, "layout"), out_layout);
+    const NumericVector c = get<NumericVector>(r, "confidence");
+    std::copy(c.begin(), c.end(), confidence);
+    const IntegerVector f = get<IntegerVector>(r, "fallback");
+    std::copy(f.begin(), f.end(), fallback);
     return 0;
   } catch (const std::exception& e) {
     last_error = e.what();

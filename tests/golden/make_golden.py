@@ -1,7 +1,7 @@
 """Generate tests/golden/*.npz from the reference's own CPU code.
 
-Runs fastEmbedR's src/tsne_neighbors.cpp and src/fast_knn_umap.cpp, compiled where
-they lie against the test-only Rcpp shim (``make -C oracle ref``), on small seeded
+Runs fastEmbedR's src/tsne_neighbors.cpp, src/fast_knn_umap.cpp and src/embedding_utils.cpp,
+compiled where they lie against the test-only Rcpp shim (``make -C oracle ref``), on small seeded
 inputs and stores inputs + outputs. The fixtures travel with the repository; the
 reference sources do not. Re-run with
     FASTEMBEDR_REFERENCE_SRC=<the reference's src/ directory> python tests/golden/make_golden.py
@@ -201,6 +201,63 @@ def transform_case():
                         y_exact=outs["exact"], y_sampled=outs["sampled"])
 
 
+def structure_case():
+    """knn_structure_score_cpp (src/embedding_utils.cpp:1386-1579) on 400 points of a 20-d
+    mixture against their exact 24-NN: two layouts (two data coordinates, random normal), every
+    row or every 7th row, preserve_k 10 and 15. Stores preservation, trustworthiness,
+    continuity and the structure score per case."""
+    lib = O.ref()
+    x, _ = S.mixture(400, 20, 5, 71, centre_sd=3.0)
+    idx, _ = S.exact_knn_numpy(x, 24)
+    layouts = np.stack([(x[:, :2] * 2.0).astype(np.float32),
+                        np.random.default_rng(72).standard_normal((400, 2)).astype(np.float32)])
+    keeps = [np.arange(400, dtype=np.int32), np.arange(0, 400, 7, dtype=np.int32)]
+    scores = np.zeros((2, 2, 2, 4))
+    for a, lay in enumerate(layouts):
+        for b, keep in enumerate(keeps):
+            keep1 = np.ascontiguousarray(keep + 1, np.int32)
+            for c, pk in enumerate((10, 15)):
+                r = np.zeros(4)
+                st = lib.ref_knn_structure_score(cm(lay, np.float64), 400, cm(idx + 1, np.int32), 24, keep1,
+                                                 keep1.size, pk, r)
+                assert st == 0, lib.ref_last_error()
+                scores[a, b, c] = r
+    np.savez_compressed(os.path.join(OUT, "knn_structure.npz"), idx=idx, layouts=layouts, keep_all=keeps[0],
+                        keep_sub=keeps[1], preserve_k=np.array([10, 15]), scores=scores)
+
+
+def affine_case():
+    """project_embedding_affine_cpp (src/embedding_utils.cpp:2120-2335), the reference's CPU
+    statement of the landmark affine start, on 800 landmarks x 8 features with a smooth
+    non-linear 2-d layout and 150 queries (one sitting on a landmark), exact 24-NN; three
+    (neighbours, ridge, max extrapolation) settings."""
+    lib = O.ref()
+    rng = np.random.default_rng(5)
+    n_ref, nq, nf, k = 800, 150, 8, 24
+    X = rng.normal(size=(n_ref, nf)).astype(np.float32)
+    L = (X[:, :2] * 3.0 + 0.3 * X[:, 2:4] ** 2).astype(np.float32)
+    Q = (X[:nq] + rng.normal(0, 0.2, (nq, nf))).astype(np.float32)
+    Q[5] = X[123]
+    d2 = ((Q[:, None, :].astype(np.float64) - X[None, :, :]) ** 2).sum(-1)
+    idx = np.argsort(d2, 1, kind="stable")[:, :k].astype(np.int32)
+    dist = np.sqrt(np.take_along_axis(d2, idx, 1)).astype(np.float32)
+    settings = np.array([[8, 1e-3, 1.5], [12, 1e-2, 2.5], [3, 1e-3, 1.0]])
+    layouts = np.zeros((len(settings), nq, 2))
+    fallback = np.zeros((len(settings), nq), np.int32)
+    for t, (m, ridge, ext) in enumerate(settings):
+        out = np.zeros(2 * nq)
+        conf = np.zeros(nq)
+        fb = np.zeros(nq, np.int32)
+        st = lib.ref_project_affine(cm(X, np.float64), n_ref, cm(Q, np.float64), nq, nf, cm(L, np.float64),
+                                    cm(idx + 1, np.int32), cm(dist, np.float64), k, int(m), float(ridge),
+                                    float(ext), out, conf, fb)
+        assert st == 0, lib.ref_last_error()
+        layouts[t] = out.reshape(2, nq).T
+        fallback[t] = fb
+    np.savez_compressed(os.path.join(OUT, "landmark_affine.npz"), X=X, Q=Q, L=L, idx=idx, dist=dist,
+                        settings=settings, layouts=layouts, fallback=fallback)
+
+
 def main():
     O.build(ref=True)
     if len(sys.argv) > 1:
@@ -222,6 +279,8 @@ def main():
     tsne_run_case()
     umap_case()
     transform_case()
+    structure_case()
+    affine_case()
     print("golden fixtures written to", OUT)
 
 

@@ -1,89 +1,15 @@
 """Landmark t-SNE transform (fastembedr_cuda_landmark_tsne_from_device_knn,
-src/embedding_cuda_kernels.cpp:3572-3686): the affine start against a NumPy FP64 restatement of
-landmark_affine_projection_kernel (:552-733), the iterations against the fixed-reference
+src/embedding_cuda_kernels.cpp:3572-3686): the affine start against the reference's CPU
+statement of it (golden) and a NumPy FP64 restatement of landmark_affine_projection_kernel
+(:552-733, pinned to the same golden on the CPU), the iterations against the fixed-reference
 transform from the same start, and the reference's argument checks."""
 import numpy as np
 import pytest
 
+from affine_restatement import affine_start
 from fastembedr_gb300 import _lib, api
 
 pytestmark = pytest.mark.gpu
-
-EPS = 1.4901161193847656e-8
-
-
-def _weighted_mean(L, refs, d, valid, rho, sigma):
-    w = np.where(valid, np.exp(-np.maximum(0.0, d - rho) / max(sigma, EPS)), 0.0)
-    s = w.sum()
-    if not np.isfinite(s) or s <= 0:
-        s = 1.0
-    return (w[:, None] * L[np.where(valid, refs, 0)]).sum(0) / s
-
-
-def affine_start(X, Q, L, idx, dist, off, m_req, ridge, max_ext):
-    """Test-side restatement of the landmark affine start in float64."""
-    nq, k = idx.shape
-    n_ref = L.shape[0]
-    m = max(3, min(m_req, min(k, 12)))
-    out = np.zeros((nq, 2))
-    for i in range(nq):
-        refs = idx[i].astype(np.int64) - off
-        d = dist[i].astype(np.float64)
-        inr = (refs >= 0) & (refs < n_ref)
-        valid = inr & np.isfinite(d) & (d >= 0)
-        rho = d[valid].min() if valid.any() else 0.0
-        zero = np.where(valid & (d <= EPS))[0]
-        if len(zero):
-            out[i] = L[refs[zero[0]]]
-            continue
-        exc = np.where(valid, np.maximum(0.0, d - rho), np.inf)
-        pos = np.sort(exc[np.isfinite(exc) & (exc > EPS)])
-        sigma = np.median(pos) if len(pos) else max(rho, EPS)
-        if not np.isfinite(sigma) or sigma < EPS:
-            sigma = EPS
-        r, vm, im = refs[:m], valid[:m], inr[:m]
-        ex = np.where(vm, np.maximum(0.0, d[:m] - rho), np.inf)
-        w = np.where(im & np.isfinite(ex), np.exp(-ex / sigma), 0.0)
-        if not np.isfinite(w.sum()) or w.sum() <= 0:
-            out[i] = _weighted_mean(L, refs, d, valid, rho, sigma)
-            continue
-        w = w / w.sum()
-        sw = np.sqrt(w)
-        rc = np.where(im, r, 0)
-        Lr = np.where(im[:, None], L[rc], 0.0)
-        cy = (w[:, None] * Lr).sum(0)
-        U = np.where(im[:, None], Lr - cy, 0.0)
-        rhs = sw[:, None] * U
-        radius2 = (U ** 2).sum(1).max()
-        Xr = np.where(im[:, None], X[rc].astype(np.float64), 0.0)
-        xc = (w[:, None] * Xr).sum(0)
-        C = np.where(im[:, None], Xr - xc, 0.0)
-        qc = Q[i].astype(np.float64) - xc
-        G = (C @ C.T) * np.outer(sw, sw)
-        qv = (C @ qc) * sw
-        trace = (w * (C ** 2).sum(1)).sum()
-        G += (ridge * max(trace, EPS) + EPS) * np.eye(m)
-        Lc = np.zeros_like(G)
-        ok = True
-        for j in range(m):
-            dg = G[j, j] - (Lc[j, :j] ** 2).sum()
-            if not np.isfinite(dg) or dg <= EPS:
-                ok = False
-                break
-            Lc[j, j] = np.sqrt(dg)
-            for t in range(j + 1, m):
-                Lc[t, j] = (G[t, j] - (Lc[t, :j] * Lc[j, :j]).sum()) / Lc[j, j]
-        if ok:
-            z = np.linalg.solve(Lc.T, np.linalg.solve(Lc, rhs))
-            disp = qv @ z
-            cap = max_ext * np.sqrt(max(radius2, EPS))
-            nd = np.sqrt((disp ** 2).sum())
-            if nd * nd > cap * cap:
-                disp = disp * cap / (nd + EPS)
-            start = cy + disp
-            ok = np.all(np.isfinite(start))
-        out[i] = start if ok else _weighted_mean(L, refs, d, valid, rho, sigma)
-    return out
 
 
 def _case(seed=3, n_ref=2000, nq=300, nf=10, k=30):
@@ -105,6 +31,21 @@ def test_affine_start_matches_restatement():
     want = affine_start(X, Q, L, idx, dist, 1, 8, 1e-3, 1.5)
     np.testing.assert_allclose(got, want, rtol=0, atol=1e-4 * np.abs(L).max())
     np.testing.assert_array_equal(got[5], L[123])  # distance 0: the landmark itself
+
+
+@pytest.mark.parametrize("case", [0, 1, 2])
+def test_affine_start_matches_reference_golden(golden, case):
+    """The GPU affine start against the reference's CPU statement of it
+    (project_embedding_affine_cpp, src/embedding_utils.cpp:2120-2335, golden made under the test
+    shim) for three (neighbours, ridge, max extrapolation) settings."""
+    g = golden("landmark_affine")
+    m, ridge, ext = g["settings"][case]
+    got = api.landmark_tsne_transform(g["X"], g["Q"], g["L"], g["idx"] + 1, g["dist"], n_iter=0,
+                                      affine_neighbors=int(m), affine_ridge=float(ridge),
+                                      max_extrapolation=float(ext))
+    want = g["layouts"][case]
+    np.testing.assert_allclose(got, want, rtol=0, atol=1e-4 * np.abs(g["L"]).max())
+    np.testing.assert_array_equal(got[5], g["L"][123])
 
 
 def test_exact_iterations_equal_the_fixed_reference_transform():

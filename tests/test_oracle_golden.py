@@ -126,3 +126,33 @@ def test_knn_preservation_known_answers():
     assert O.knn_preservation(line, hi, preserve_k=2) == pytest.approx((0.5 + 1.0 + 0.0 + 1.0 + 0.5) / 5, abs=1e-15)
     # 1-based labels give the same score
     assert O.knn_preservation(line, hi + 1, preserve_k=2, offset=1) == pytest.approx(0.6, abs=1e-15)
+
+
+def test_knn_preservation_matches_reference_golden(golden):
+    """M1 pinned on the reference's own knn_structure_score_cpp (src/embedding_utils.cpp:1386-1579,
+    compiled under the test shim by tests/golden/make_golden.py): preservation of two layouts over
+    every row and every 7th row at preserve_k 10 and 15 equals the reference's to the last bits of
+    the summation order."""
+    g = golden("knn_structure")
+    for a, lay in enumerate(g["layouts"]):
+        for b, keep in enumerate((g["keep_all"], g["keep_sub"])):
+            for c, pk in enumerate(g["preserve_k"]):
+                got = O.knn_preservation(lay, g["idx"], keep=keep, preserve_k=int(pk))
+                assert got == pytest.approx(g["scores"][a, b, c, 0], abs=1e-15), (a, b, c)
+
+
+@pytest.mark.parametrize("case", [0, 1, 2])
+def test_affine_restatement_matches_reference_golden(golden, case):
+    """The FP64 restatement of the landmark affine start that the GPU tests use, against the
+    reference's CPU statement of the start (project_embedding_affine_cpp,
+    src/embedding_utils.cpp:2120-2335, run under the test shim): equal to 1e-8 of the layout
+    scale (about 1e-9 measured: summation order and the float median of the reference)."""
+    from affine_restatement import affine_start
+
+    g = golden("landmark_affine")
+    m, ridge, ext = g["settings"][case]
+    want = g["layouts"][case]
+    got = affine_start(g["X"], g["Q"], g["L"], g["idx"] + 1, g["dist"], 1, int(m), float(ridge), float(ext))
+    assert not g["fallback"][case].any()
+    assert np.abs(got - want).max() <= 1e-8 * np.abs(g["L"]).max()
+    np.testing.assert_array_equal(want[5], g["L"][123].astype(np.float64))  # distance 0: the landmark
