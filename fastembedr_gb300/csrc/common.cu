@@ -61,7 +61,9 @@ struct Stager {
   char* buf[2] = {nullptr, nullptr};
   cudaEvent_t done[2] = {nullptr, nullptr};
   int next = 0;
-  void ensure() {
+  int device = -1;  // the device whose context holds the events
+  void ensure(int dev) {
+    device = dev;
     for (int b = 0; b < 2; ++b) {
       if (!buf[b]) FE_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&buf[b]), kChunk, cudaHostAllocDefault));
       if (!done[b]) FE_CUDA(cudaEventCreateWithFlags(&done[b], cudaEventDisableTiming));
@@ -70,7 +72,7 @@ struct Stager {
 };
 
 Stager& stager() {
-  static Stager* st = new Stager();  // never destroyed: the driver frees pinned memory at exit
+  static Stager* st = new Stager();  // never destroyed: its pinned memory goes with the CUDA context
   return *st;
 }
 
@@ -104,9 +106,15 @@ void upload(void* dst, const void* src, std::size_t bytes, cudaStream_t s) {
     FE_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
     return;
   }
+  int dev = 0;
+  FE_CUDA(cudaGetDevice(&dev));
   Stager& st = stager();
   std::lock_guard<std::mutex> lock(st.mu);
-  st.ensure();
+  if (st.device >= 0 && st.device != dev) {  // staging lives on the first device that used it
+    FE_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+    return;
+  }
+  st.ensure(dev);
   const char* from = static_cast<const char*>(src);
   char* to = static_cast<char*>(dst);
   for (std::size_t off = 0; off < bytes; off += kChunk) {
