@@ -11,9 +11,12 @@
 //                                          (spatial) order (stream of P + L1/L2 gathers of y)
 //   main stream:  scatter_kernel           points -> 64-bit fixed-point charges (deterministic)
 //                 rows_forward_kernel      row FFTs of the charges (x + i y plane, paired mass
-//                                          rows as half spectra) and of the kernel rows
+//                                          rows as half spectra) and of the kernel rows; the top
+//                                          stages run in registers on the values as loaded
 //                 columns_convolve_kernel  column FFTs per conjugate column pair, Z by Parseval,
-//                                          multiply, inverse column FFTs, all in shared memory
+//                                          multiply, inverse column FFTs in shared memory; the
+//                                          passes next to global memory and to the product run
+//                                          in registers
 //                 rows_inverse_kernel      inverse row FFTs -> float4 potentials, Z finalised
 //   join:         update_kernel            potential gather + gains/momentum/step clip +
 //                                          recentring; epilogue reduces the new bounding box and
@@ -366,8 +369,7 @@ __host__ __device__ constexpr int padded(int count) { return count + count / 16;
 // Radix-2 FFTs over `count` sequences of length M = 2^logm stored at buf + seq * M, with R
 // consecutive radix-2 stages fused per shared-memory pass (R <= MAXR <= 4; with 4, M = 2048 takes
 // three passes): each work item keeps the 2^R elements i0 + t * 2^s of one butterfly group in
-// registers. tw[t] = exp(-2 pi i t / M). The forward row pass uses MAXR = 3: its kernel-row blocks
-// transform one sequence, whose 128 radix-16 work items would leave half of 256 threads idle.
+// registers. tw[t] = exp(-2 pi i t / M). The forward row pass uses MAXR = 3.
 __device__ __forceinline__ float2 twiddle(const float2* __restrict__ tw, int x, int shift, bool inverse) {
   float2 w = tw[x << shift];
   if (inverse) w.y = -w.y;
